@@ -1,0 +1,548 @@
+"""CPU oracle: a numpy/scipy restatement of Tenet.jl's MPS hot path.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA library and its host
+mirror) imports this module; only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
+legs of ``bench.py`` use it, as the checker and as the timed CPU baseline.
+
+What it restates (Tenet.jl v0.10.3, file:line relative to the project root):
+
+* ``generic_canonize_site!``      src/Operations/canonize.jl:23-76   (QR / SVD gauge move)
+* ``generic_bond_canonize_site!`` src/Operations/canonize.jl:78-116  (SVD, Λ kept apart)
+* ``generic_mps_canonize!``       src/Operations/canonize.jl:121-252 (form transitions)
+* ``generic_mps_compress!``       src/Operations/compress.jl:21-69   (maxdim, absolute threshold)
+* ``generic_simple_update!``      src/Operations/simple_update.jl:20-92
+* ``overlap``                     src/Operations/overlap.jl:22-50    (⟨b|a⟩ = Σ a·conj(b))
+* ``norm`` / ``normalize!``       src/Operations/norm.jl:17-37, normalize.jl:15-37
+* ``MPS(arrays; order)``          src/Components/MPS.jl:50-94
+* ``rand(MPS)`` bond clamping     src/Components/MPS.jl:113-165
+* ``ProductState(bitstr)``        src/Components/ProductState.jl:72-92
+* ``checkform`` / ``isisometry``  src/Components/MPO.jl:41-83 (atol 1e-12)
+
+The arithmetic itself lives in the un-vendored Muscle.jl (>= 0.3.9): ``binary_einsum``
+(permute + BLAS gemm), ``tensor_qr_thin`` (LAPACK geqrf/ungqr), ``tensor_svd_thin``
+(LAPACK gesdd) and ``simple_update`` (θ = A·B·op → thin SVD → keep ≤ maxdim → √S into
+both sides).  Here those are numpy ``tensordot``/``einsum`` and scipy's LAPACK drivers.
+Muscle choices invisible from Tenet's source are fixed as follows and documented:
+no renormalisation after truncation; exact-zero singular values are kept up to
+``maxdim`` (the CX known answer, test/unit/simple_update.jl:38-42, keeps a zero
+singular value on bond 1-2); the optional absolute ``threshold`` of
+``simple_update`` mirrors compress.jl:54-59 and always keeps at least one value.
+
+Parity pinning: the reference ships no golden vectors for this path (and Julia is not
+available to run it).  The oracle is pinned by the reference's own invariant and
+known-answer tests, ported in tests/test_oracle_reference.py.  Results at the Muscle
+boundary (raw Q, U, V) are gauge-dependent and are compared only through invariants.
+
+Site layout: every site tensor is stored 3-D as (χ_left, d, χ_right), column-major
+semantics kept by numpy index order; the open ends carry a size-1 bond.  This is
+Tenet's ``(:l, :o, :r)`` order with the boundary 2-D tensors lifted to 3-D.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import scipy.linalg as sla
+
+# ----------------------------------------------------------------------------------
+# canonical forms (src/CanonicalForm.jl:10-87)
+# ----------------------------------------------------------------------------------
+
+
+class NonCanonical:
+    def __eq__(self, other):
+        return isinstance(other, NonCanonical)
+
+    def __repr__(self):
+        return "NonCanonical()"
+
+
+class MixedCanonical:
+    """Orthogonality centre = sites lo..hi (1-based, inclusive)."""
+
+    def __init__(self, sites):
+        if isinstance(sites, int):
+            sites = [sites]
+        self.sites = sorted(set(int(s) for s in sites))
+
+    @property
+    def lo(self):
+        return self.sites[0]
+
+    @property
+    def hi(self):
+        return self.sites[-1]
+
+    def __eq__(self, other):
+        return isinstance(other, MixedCanonical) and self.sites == other.sites
+
+    def __repr__(self):
+        return f"MixedCanonical({self.sites})"
+
+
+class BondCanonical:
+    """Orthogonality centre = bond (i, i+1); Λ stored at LambdaSite(bond)."""
+
+    def __init__(self, a, b=None):
+        if b is None:
+            a, b = a
+        self.a, self.b = min(a, b), max(a, b)
+
+    def __eq__(self, other):
+        return isinstance(other, BondCanonical) and (self.a, self.b) == (other.a, other.b)
+
+    def __repr__(self):
+        return f"BondCanonical({self.a}-{self.b})"
+
+
+# ----------------------------------------------------------------------------------
+# MPS container
+# ----------------------------------------------------------------------------------
+
+
+class OMPS:
+    """Oracle MPS: site tensors (χl, d, χr), canonical form, Λ vectors by bond."""
+
+    def __init__(self, sites, form=None):
+        self.sites = [np.asarray(s) for s in sites]
+        self.form = form if form is not None else MixedCanonical(range(1, len(sites) + 1))
+        self.lam = {}  # bond index i (bond i-(i+1)) -> Λ vector
+
+    @property
+    def L(self):
+        return len(self.sites)
+
+    def copy(self):
+        m = OMPS([s.copy() for s in self.sites], self.form)
+        m.lam = {k: v.copy() for k, v in self.lam.items()}
+        return m
+
+    def bondsizes(self):
+        return [self.sites[i].shape[2] for i in range(self.L - 1)]
+
+    def site(self, i):
+        return self.sites[i - 1]
+
+    def set_site(self, i, t):
+        self.sites[i - 1] = t
+
+
+def mps_from_arrays(arrays, order=("l", "r", "o")):
+    """``MPS(arrays; order)`` (src/Components/MPS.jl:50-94), lifted to 3-D sites."""
+    order = tuple(order)
+    assert sorted(order) == ["l", "o", "r"]
+    L = len(arrays)
+    out = []
+    for i, a in enumerate(arrays):
+        a = np.asarray(a)
+        if i == 0:
+            lo = tuple(x for x in order if x != "l")
+            assert a.ndim == 2
+            t = np.moveaxis(a, [lo.index("o"), lo.index("r")], [0, 1])[None, :, :]
+        elif i == L - 1:
+            lo = tuple(x for x in order if x != "r")
+            assert a.ndim == 2
+            t = np.moveaxis(a, [lo.index("l"), lo.index("o")], [0, 1])[:, :, None]
+        else:
+            assert a.ndim == 3
+            t = np.moveaxis(a, [order.index("l"), order.index("o"), order.index("r")], [0, 1, 2])
+        out.append(np.ascontiguousarray(t))
+    return OMPS(out)
+
+
+# ----------------------------------------------------------------------------------
+# Muscle-level primitives (restated)
+# ----------------------------------------------------------------------------------
+
+
+def qr_thin(m):
+    """tensor_qr_thin on a matrix: LAPACK geqrf + ungqr, k = min(rows, cols)."""
+    q, r = np.linalg.qr(m, mode="reduced")
+    return q, r
+
+
+def svd_thin(m):
+    """tensor_svd_thin on a matrix: LAPACK gesdd; s descending; m = U diag(s) Vh."""
+    try:
+        u, s, vh = sla.svd(m, full_matrices=False, lapack_driver="gesdd")
+    except np.linalg.LinAlgError:
+        u, s, vh = sla.svd(m, full_matrices=False, lapack_driver="gesvd")
+    return u, s, vh
+
+
+def isisometry(t, axis, atol=1e-12):
+    """Muscle.isisometry(tensor, index): contracting all other indices with the
+    conjugate gives the identity on ``axis``."""
+    t = np.moveaxis(np.asarray(t), axis, -1)
+    m = t.reshape(-1, t.shape[-1])
+    g = m.conj().T @ m
+    return bool(np.allclose(g, np.eye(g.shape[0]), atol=atol, rtol=0))
+
+
+# ----------------------------------------------------------------------------------
+# gauge moves (src/Operations/canonize.jl:23-116)
+# ----------------------------------------------------------------------------------
+
+
+def canonize_site(psi: OMPS, site: int, direction: str, method="qr"):
+    """generic_canonize_site! (canonize.jl:23-76).  direction 'right' factorises site
+    ``site`` across bond (site, site+1) and pushes R into site+1; 'left' factorises
+    across bond (site-1, site) and pushes into site-1.  Size-1 bonds are skipped
+    (canonize.jl:38)."""
+    A = psi.site(site)
+    if direction == "right":
+        chi = A.shape[2]
+        if chi == 1:
+            return
+        B = psi.site(site + 1)
+        m = A.reshape(-1, chi, order="C")  # rows (χl, d), cols χr
+        if method == "qr":
+            q, r = qr_thin(m)
+        else:
+            u, s, vh = svd_thin(m)
+            q, r = u, s[:, None] * vh
+        k = q.shape[1]
+        psi.set_site(site, q.reshape(A.shape[0], A.shape[1], k))
+        psi.set_site(site + 1, np.tensordot(r, B, axes=(1, 0)))
+    else:
+        chi = A.shape[0]
+        if chi == 1:
+            return
+        B = psi.site(site - 1)
+        m = A.reshape(chi, -1).T  # rows (d, χr), cols χl
+        if method == "qr":
+            q, r = qr_thin(m)
+        else:
+            u, s, vh = svd_thin(m)
+            q, r = u, s[:, None] * vh
+        k = q.shape[1]
+        psi.set_site(site, q.T.reshape(k, A.shape[1], A.shape[2]))
+        psi.set_site(site - 1, np.tensordot(B, r.T, axes=(2, 0)))
+
+
+def bond_canonize_site(psi: OMPS, site: int, bond_a: int):
+    """generic_bond_canonize_site! (canonize.jl:78-116): thin SVD of ``site`` across
+    bond (bond_a, bond_a+1); U stays, V is contracted into the neighbour, Λ kept."""
+    assert bond_a not in psi.lam
+    A = psi.site(site)
+    if site == bond_a:  # factorise towards the right
+        chi = A.shape[2]
+        if chi == 1:
+            return
+        B = psi.site(site + 1)
+        u, s, vh = svd_thin(A.reshape(-1, chi))
+        k = s.size
+        psi.set_site(site, u.reshape(A.shape[0], A.shape[1], k))
+        psi.set_site(site + 1, np.tensordot(vh, B, axes=(1, 0)))
+    else:  # site == bond_a + 1: factorise towards the left
+        chi = A.shape[0]
+        if chi == 1:
+            return
+        B = psi.site(site - 1)
+        u, s, vh = svd_thin(A.reshape(chi, -1).T)
+        k = s.size
+        psi.set_site(site, u.T.reshape(k, A.shape[1], A.shape[2]))
+        psi.set_site(site - 1, np.tensordot(B, vh.T, axes=(2, 0)))
+    psi.lam[bond_a] = s
+
+
+def hadamard_bond(t, lam, axis):
+    """Muscle.hadamard(tensor, Λ) along one index (canonize.jl:198,209)."""
+    shape = [1] * t.ndim
+    shape[axis] = lam.size
+    return t * lam.reshape(shape)
+
+
+# ----------------------------------------------------------------------------------
+# form transitions (src/Operations/canonize.jl:121-252)
+# ----------------------------------------------------------------------------------
+
+
+def canonize(psi: OMPS, new_form):
+    """canonize!(ψ, form); ints and lists of ints mean MixedCanonical, tuples of two
+    ints BondCanonical (canonize.jl:16-20)."""
+    if isinstance(new_form, int) or isinstance(new_form, list):
+        new_form = MixedCanonical(new_form)
+    elif isinstance(new_form, tuple):
+        new_form = BondCanonical(new_form)
+    old = psi.form
+    if isinstance(new_form, NonCanonical):
+        psi.form = NonCanonical()
+        return psi
+    if isinstance(old, NonCanonical):
+        psi.form = MixedCanonical(range(1, psi.L + 1))
+        return canonize(psi, new_form)
+    if isinstance(old, MixedCanonical) and isinstance(new_form, MixedCanonical):
+        if old == new_form:
+            return psi
+        src_left, src_right = old.lo, old.hi
+        dst_left, dst_right = new_form.lo - 1, new_form.hi + 1
+        for i in range(src_left, dst_left + 1):  # canonize.jl:136-139
+            canonize_site(psi, i, "right")
+        for i in range(src_right, dst_right - 1, -1):  # canonize.jl:142-145
+            canonize_site(psi, i, "left")
+        psi.form = MixedCanonical(new_form.sites)
+        return psi
+    if isinstance(old, MixedCanonical) and isinstance(new_form, BondCanonical):
+        old_min, old_max = old.lo, old.hi
+        new_min, new_max = new_form.a, new_form.b
+        if old_max <= new_min:
+            canonize(psi, MixedCanonical(new_min))
+            bond_canonize_site(psi, new_min, new_form.a)
+        elif new_max <= old_min:
+            canonize(psi, MixedCanonical(new_max))
+            bond_canonize_site(psi, new_max, new_form.a)
+        elif old_min <= new_min and new_max <= old_max:
+            canonize(psi, MixedCanonical(new_min))
+            bond_canonize_site(psi, new_min, new_form.a)
+        else:
+            raise ValueError(f"Cannot canonize from {old} to {new_form}")
+        psi.form = new_form
+        return psi
+    if isinstance(old, BondCanonical) and isinstance(new_form, MixedCanonical):
+        old_min, old_max = old.a, old.b
+        new_min, new_max = new_form.lo, new_form.hi
+        lam = psi.lam.pop(old.a)
+        if old_max <= new_min:
+            psi.set_site(old_max, hadamard_bond(psi.site(old_max), lam, 0))
+            psi.form = MixedCanonical(old_max)
+            canonize(psi, new_form)
+        elif new_max <= old_min:
+            psi.set_site(old_min, hadamard_bond(psi.site(old_min), lam, 2))
+            psi.form = MixedCanonical(old_min)
+            canonize(psi, new_form)
+        else:
+            raise ValueError(f"Cannot canonize from {old} to {new_form}")
+        psi.form = new_form
+        return psi
+    if isinstance(old, BondCanonical) and isinstance(new_form, BondCanonical):
+        if old == new_form:
+            return psi
+        old_min, old_max = old.a, old.b
+        new_min, new_max = new_form.a, new_form.b
+        if old_max <= new_min:
+            canonize(psi, MixedCanonical(new_min))
+            bond_canonize_site(psi, new_min, new_form.a)
+        elif new_max <= old_min:
+            canonize(psi, MixedCanonical(new_max))
+            bond_canonize_site(psi, new_max, new_form.a)
+        else:
+            raise ValueError(f"Cannot canonize from {old} to {new_form}")
+        psi.form = new_form
+        return psi
+    raise ValueError(f"Cannot canonize from {old} to {new_form}")
+
+
+def checkform(psi: OMPS, atol=1e-12):
+    """checkform (src/Components/MPO.jl:41-83)."""
+    f = psi.form
+    if isinstance(f, NonCanonical):
+        return True
+    left, right = (f.lo, f.hi) if isinstance(f, MixedCanonical) else (f.a, f.b)
+    for i in range(1, psi.L + 1):
+        if i < left and not isisometry(psi.site(i), 2, atol):
+            raise ValueError(f"site {i} is not left-canonical")
+        if i > right and not isisometry(psi.site(i), 0, atol):
+            raise ValueError(f"site {i} is not right-canonical")
+    return True
+
+
+# ----------------------------------------------------------------------------------
+# compress (src/Operations/compress.jl:21-69)
+# ----------------------------------------------------------------------------------
+
+
+def compress(psi: OMPS, bond=None, maxdim=None, threshold=None):
+    if maxdim is None and threshold is None:
+        raise ValueError("Either `maxdim` or `threshold` must be specified")
+    if maxdim is not None and maxdim <= 0:
+        raise ValueError("maxdim must be a positive integer")
+    if threshold is not None and threshold <= 0:
+        raise ValueError("Threshold must be positive")
+    if bond is None:
+        for i in range(1, psi.L):
+            compress(psi, (i, i + 1), maxdim, threshold)
+        return psi
+    a, b = min(bond), max(bond)
+    canonize(psi, BondCanonical(a, b))
+    if a not in psi.lam:  # size-1 bond: nothing to truncate
+        return psi
+    s = psi.lam[a]
+    keep = np.arange(s.size)
+    if maxdim is not None:
+        keep = keep[: min(maxdim, s.size)]
+    if threshold is not None:
+        keep = keep[np.abs(s[keep]) > threshold]
+    psi.set_site(a, psi.site(a)[:, :, keep])
+    psi.set_site(b, psi.site(b)[keep, :, :])
+    psi.lam[a] = s[keep]
+    return psi
+
+
+# ----------------------------------------------------------------------------------
+# simple update (src/Operations/simple_update.jl:20-92)
+# ----------------------------------------------------------------------------------
+
+
+def simple_update_tensors(A, B, G, maxdim=None, threshold=None):
+    """Muscle.simple_update with AbsorbEqually: θ[l,a,b,r] = Σ G[a,b,a',b'] A[l,a',m]
+    B[m,b',r]; SVD over (l,a)|(b,r); keep ≤ maxdim (then |s| > threshold, ≥ 1 kept);
+    A' = U√S, B' = √S Vh.  Returns (A', B', s_kept, s_full)."""
+    chl, d1, _ = A.shape
+    _, d2, chr_ = B.shape
+    theta = np.tensordot(A, B, axes=(2, 0))  # l, a', b', r
+    theta = np.einsum("abcd,lcdr->labr", G, theta, optimize=True)
+    u, s, vh = svd_thin(theta.reshape(chl * d1, d2 * chr_))
+    k = s.size if maxdim is None else min(maxdim, s.size)
+    if threshold is not None:
+        k = max(1, int(np.count_nonzero(np.abs(s[:k]) > threshold)))
+    sq = np.sqrt(s[:k])
+    An = (u[:, :k] * sq[None, :]).reshape(chl, d1, k)
+    Bn = (sq[:, None] * vh[:k, :]).reshape(k, d2, chr_)
+    return An, Bn, s[:k], s
+
+
+def simple_update(psi: OMPS, G, sites, maxdim=None, threshold=None):
+    """simple_update!(ψ::MPS, op) (simple_update.jl:82-92): move the centre onto the
+    gate's sites, then apply; the 1-site shortcut is simple_update.jl:27-37.
+
+    ``G`` is the gate array; for two sites its index order is
+    [plug a, plug b, plug a', plug b'] with a < b adjacent, primed = input."""
+    sites = sorted(sites)
+    canonize(psi, MixedCanonical(sites))
+    if len(sites) == 1:
+        i = sites[0]
+        psi.set_site(i, np.einsum("ab,lbr->lar", G, psi.site(i)))
+        return psi
+    a, b = sites
+    assert b == a + 1
+    An, Bn, _, _ = simple_update_tensors(psi.site(a), psi.site(b), G, maxdim, threshold)
+    psi.set_site(a, An)
+    psi.set_site(b, Bn)
+    return psi
+
+
+# ----------------------------------------------------------------------------------
+# overlap / norm (src/Operations/overlap.jl:22-50, norm.jl:17-37, normalize.jl:15-37)
+# ----------------------------------------------------------------------------------
+
+
+def overlap(a: OMPS, b: OMPS):
+    """overlap(a::MPS, b::MPS) = ⟨b|a⟩ by a left-environment sweep (overlap.jl:36-50)."""
+    if a.L != b.L:
+        raise ValueError("nsites differ")
+    env = np.ones((1, 1), dtype=np.result_type(a.sites[0], b.sites[0]))
+    for A, B in zip(a.sites, b.sites):
+        t = np.tensordot(env, A, axes=(0, 0))  # y, s, x'
+        env = np.tensordot(t, B.conj(), axes=([0, 1], [0, 1]))  # x', y'
+    return complex(env[0, 0])
+
+
+def product_state_vectors(bits: str):
+    """ProductState(bitstr) (ProductState.jl:72-92)."""
+    table = {
+        "0": [1.0, 0.0],
+        "1": [0.0, 1.0],
+        "+": [1 / np.sqrt(2), 1 / np.sqrt(2)],
+        "-": [1 / np.sqrt(2), -1 / np.sqrt(2)],
+        "u": [1 / np.sqrt(2), -1j / np.sqrt(2)],
+        "↑": [1 / np.sqrt(2), -1j / np.sqrt(2)],
+        "d": [-1 / np.sqrt(2), -1j / np.sqrt(2)],
+        "↓": [-1 / np.sqrt(2), -1j / np.sqrt(2)],
+    }
+    out = []
+    for c in bits:
+        if c not in table:
+            raise ValueError(f"invalid character: {c}")
+        out.append(np.asarray(table[c], dtype=np.complex128))
+    return out
+
+
+def amplitude(vectors, psi: OMPS):
+    """overlap(::ProductState, ::MPS) (overlap.jl:22-32): Σ ψ · v, v not conjugated."""
+    env = np.ones((1,), dtype=np.complex128)
+    for v, A in zip(vectors, psi.sites):
+        M = np.tensordot(A, v, axes=(1, 0))  # l, r
+        env = env @ M
+    return complex(env[0])
+
+
+def norm(psi: OMPS):
+    """norm(ψ::MPS) (norm.jl:17-37); moves the centre like the reference."""
+    f = psi.form
+    if isinstance(f, NonCanonical):
+        psi.form = MixedCanonical(range(1, psi.L + 1))
+        return norm(psi)
+    if isinstance(f, MixedCanonical):
+        canonize(psi, MixedCanonical(f.lo))
+        return float(np.linalg.norm(psi.site(f.lo)))
+    return float(np.linalg.norm(psi.lam[f.a]))
+
+
+def normalize(psi: OMPS):
+    """normalize!(ψ::MPS) (normalize.jl:15-37)."""
+    f = psi.form
+    if isinstance(f, NonCanonical):
+        psi.form = MixedCanonical(range(1, psi.L + 1))
+        return normalize(psi)
+    if isinstance(f, MixedCanonical):
+        canonize(psi, MixedCanonical(f.lo))
+        t = psi.site(f.lo)
+        psi.set_site(f.lo, t / np.linalg.norm(t))
+        return psi
+    psi.lam[f.a] = psi.lam[f.a] / np.linalg.norm(psi.lam[f.a])
+    return psi
+
+
+def local_expectations(psi: OMPS, op):
+    """⟨ψ|O_i|ψ⟩ / ⟨ψ|ψ⟩ for every site i with a left/right environment sweep.
+    Equal to overlap(ψ, O_i ψ) / overlap(ψ, ψ) (the overlap.jl:36-50 convention) at a
+    cost of ~3 overlaps instead of L."""
+    L = psi.L
+    lefts = [np.ones((1, 1), dtype=np.complex128)]
+    for A in psi.sites[:-1]:
+        t = np.tensordot(lefts[-1], A, axes=(0, 0))
+        lefts.append(np.tensordot(t, A.conj(), axes=([0, 1], [0, 1])))
+    rights = [np.ones((1, 1), dtype=np.complex128)]
+    for A in psi.sites[:0:-1]:
+        t = np.tensordot(A, rights[-1], axes=(2, 0))  # l, s, r'
+        rights.append(np.tensordot(t, A.conj(), axes=([1, 2], [1, 2])))
+    rights = rights[::-1]
+    out = np.empty(L, dtype=np.complex128)
+    nrm = None
+    for i, A in enumerate(psi.sites):
+        OA = np.einsum("ab,lbr->lar", op, A)
+        t = np.tensordot(lefts[i], OA, axes=(0, 0))  # y, s, r
+        t = np.tensordot(t, rights[i], axes=(2, 0))  # y, s, r'
+        out[i] = np.tensordot(t, A.conj(), axes=([0, 1, 2], [0, 1, 2]))
+        if nrm is None:
+            t = np.tensordot(lefts[i], A, axes=(0, 0))
+            t = np.tensordot(t, rights[i], axes=(2, 0))
+            nrm = complex(np.tensordot(t, A.conj(), axes=([0, 1, 2], [0, 1, 2])))
+    return out / nrm, nrm
+
+
+def contract_state(psi: OMPS):
+    """Full state vector (small L only): the ``contract(ψ)`` of the reference tests,
+    with Λ absorbed when the MPS is bond-canonical."""
+    sites = [s for s in psi.sites]
+    if isinstance(psi.form, BondCanonical) and psi.form.a in psi.lam:
+        a = psi.form.a
+        sites[a - 1] = hadamard_bond(sites[a - 1], psi.lam[a], 2)
+    v = sites[0]
+    for A in sites[1:]:
+        v = np.tensordot(v, A, axes=(v.ndim - 1, 0))
+    return v.reshape(-1)
+
+
+# ----------------------------------------------------------------------------------
+# TEBD driver (brickwork of 2-site gates, each simple_update! + absolute cutoff)
+# ----------------------------------------------------------------------------------
+
+
+def tebd(psi: OMPS, layers, maxdim, threshold):
+    """Apply brickwork layers [(bond_start, [G...]), ...] left→right."""
+    for start, gates in layers:
+        for j, G in enumerate(gates):
+            a = start + 2 * j
+            simple_update(psi, G, (a, a + 1), maxdim=maxdim, threshold=threshold)
+    return psi

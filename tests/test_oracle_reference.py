@@ -1,0 +1,220 @@
+"""Pins the CPU oracle against the reference's own invariant and known-answer tests.
+
+Each test restates one testset of Tenet.jl's test suite (file:line given) on the same
+deterministic integer fixtures, so the oracle's canonical-form, compression and
+simple-update semantics follow the reference where it has been pinned.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import tenet_oracle as O
+
+
+def jl(arr_range, *shape):
+    """Julia's ``collect(reshape(a:b, shape...))`` (column-major)."""
+    return np.arange(arr_range[0], arr_range[1] + 1, dtype=np.float64).reshape(shape, order="F")
+
+
+def fixture_mps(first=None):
+    """test/unit/mps.jl:63-69 (default order (:l, :r, :o))."""
+    arrays = [
+        jl((1, 16), 4, 4) if first is None else first,
+        jl((1, 64), 4, 4, 4),
+        jl((1, 64), 4, 4, 4),
+        jl((1, 64), 4, 4, 4),
+        jl((1, 16), 4, 4),
+    ]
+    return O.mps_from_arrays(arrays, order=("l", "r", "o"))
+
+
+def iso(psi, site, side):
+    return O.isisometry(psi.site(site), 2 if side == "r" else 0)
+
+
+def state_close(a, b):
+    va, vb = O.contract_state(a), O.contract_state(b)
+    return np.linalg.norm(va - vb) <= np.sqrt(np.finfo(float).eps) * max(np.linalg.norm(va), np.linalg.norm(vb))
+
+
+def test_constructor_order():
+    # test/unit/mps.jl:28-48: order [:r, :o, :l]
+    a = np.ones((1, 2))
+    b = 2 * np.ones((3, 2, 1))
+    c = 3 * np.ones((2, 3))
+    psi = O.mps_from_arrays([a, b, c], order=("r", "o", "l"))
+    assert psi.bondsizes() == [1, 3]
+    assert [s.shape[1] for s in psi.sites] == [2, 2, 2]
+
+
+def test_noncanonical_to_mixed_single_site():
+    # test/unit/mps.jl:62-90
+    psi = fixture_mps()
+    psi.form = O.NonCanonical()
+    c = O.canonize(psi.copy(), 3)
+    assert O.checkform(c)
+    assert c.form == O.MixedCanonical(3)
+    assert iso(c, 1, "r") and iso(c, 2, "r")
+    assert not iso(c, 3, "l") and not iso(c, 3, "r")
+    assert iso(c, 4, "l") and iso(c, 5, "l")
+    assert state_close(c, psi)
+
+
+def test_noncanonical_to_mixed_multi_site():
+    # test/unit/mps.jl:92-119
+    psi = fixture_mps()
+    psi.form = O.NonCanonical()
+    c = O.canonize(psi.copy(), [2, 3])
+    assert c.form == O.MixedCanonical([2, 3]) and O.checkform(c)
+    assert iso(c, 1, "r") and not iso(c, 2, "l") and not iso(c, 3, "r")
+    assert iso(c, 4, "l") and iso(c, 5, "l")
+    assert state_close(c, psi)
+
+
+@pytest.mark.parametrize("start", [5, [3, 4, 5], [1, 2, 3, 4, 5]])
+def test_mixed_to_mixed(start):
+    # test/unit/mps.jl:121-208
+    psi = fixture_mps()
+    O.canonize(psi, start)
+    c = O.canonize(psi.copy(), 3)
+    assert c.form == O.MixedCanonical(3) and O.checkform(c)
+    assert iso(c, 1, "r") and iso(c, 2, "r") and iso(c, 4, "l") and iso(c, 5, "l")
+    assert not iso(c, 3, "l") and not iso(c, 3, "r")
+    assert state_close(c, psi)
+
+
+@pytest.mark.parametrize("start", [None, 5, [3, 4, 5]])
+def test_to_bond_canonical(start):
+    # test/unit/mps.jl:210-335
+    psi = fixture_mps()
+    if start is None:
+        psi.form = O.NonCanonical()
+    else:
+        O.canonize(psi, start)
+    c = O.canonize(psi.copy(), (2, 3))
+    assert c.form == O.BondCanonical(2, 3) and O.checkform(c)
+    assert set(c.lam) == {2}
+    assert iso(c, 1, "r") and not iso(c, 2, "l") and not iso(c, 3, "r")
+    assert iso(c, 4, "l") and iso(c, 5, "l")
+    assert state_close(c, psi)
+
+
+def test_mixed_to_bond_no_overlap():
+    # test/unit/mps.jl:275-305
+    psi = fixture_mps()
+    O.canonize(psi, [3, 4, 5])
+    c = O.canonize(psi.copy(), (1, 2))
+    assert c.form == O.BondCanonical(1, 2) and O.checkform(c)
+    assert not iso(c, 2, "r") and iso(c, 3, "l") and iso(c, 4, "l") and iso(c, 5, "l")
+    assert state_close(c, psi)
+
+
+def test_bond_to_bond_and_back_to_mixed():
+    # test/unit/mps.jl:338-443
+    psi = fixture_mps()
+    O.canonize(psi, (4, 5))
+    c = O.canonize(psi.copy(), (2, 3))
+    assert c.form == O.BondCanonical(2, 3) and O.checkform(c)
+    assert state_close(c, psi)
+    for start, target in [((2, 3), 3), ((4, 5), 3)]:
+        p = fixture_mps()
+        O.canonize(p, start)
+        c = O.canonize(p.copy(), target)
+        assert c.form == O.MixedCanonical(3) and O.checkform(c)
+        assert iso(c, 1, "r") and iso(c, 2, "r") and iso(c, 4, "l") and iso(c, 5, "l")
+        assert state_close(c, p)
+
+
+def test_compress_single_bond():
+    # test/unit/mps.jl:465-495: rank-1 first site => compress to size 1 keeps the state
+    for kw in (dict(maxdim=1), dict(threshold=0.1)):
+        psi = fixture_mps(first=np.ones((4, 4)))
+        c = O.compress(psi.copy(), (1, 2), **kw)
+        assert c.bondsizes()[0] == 1
+        assert state_close(c, psi)
+
+
+def test_compress_all_bonds():
+    # test/unit/mps.jl:497-522
+    psi = fixture_mps(first=np.ones((4, 4)))
+    c = O.compress(psi.copy(), maxdim=1)
+    assert all(b == 1 for b in c.bondsizes())
+    p2 = psi.copy()
+    O.canonize(p2, (1, 2))
+    threshold = p2.lam[1][1] * 1.1
+    c = O.compress(psi.copy(), threshold=threshold)
+    assert c.bondsizes()[0] == 1
+    assert state_close(c, psi)
+
+
+def test_bondsizes_and_truncate():
+    # test/unit/mps.jl:524-531 (rand(MPS; n=8) → [2,4,8,16,8,4,2]; truncate!(maxdim=10))
+    from tenetgb import workloads as W
+
+    psi = O.OMPS(W.random_mps_arrays(8, 2, 128, seed=0))
+    assert psi.bondsizes() == [2, 4, 8, 16, 8, 4, 2]
+    O.compress(psi, maxdim=10)
+    assert max(psi.bondsizes()) == 10
+
+
+def test_simple_update_x():
+    # test/unit/simple_update.jl:4-14 (applied to the MPS form of the product state)
+    psi = O.mps_from_arrays([np.array([[1.0, 0.0]]), np.array([[0.0], [1.0]])], order=("r", "o", "l"))
+    X = np.array([[0, 1], [1, 0]], dtype=float)
+    O.simple_update(psi, X, [1])
+    assert np.allclose(psi.site(1).reshape(-1), [0, 1])
+    O.simple_update(psi, X, [2])
+    assert np.allclose(psi.site(2).reshape(-1), [1, 0])
+
+
+def test_simple_update_cx():
+    # test/unit/simple_update.jl:16-43: CX on |11⟩, gate indices [2, 1, 2', 1']
+    psi = O.mps_from_arrays([np.array([[0.0, 1.0]]), np.array([[0.0], [1.0]])], order=("r", "o", "l"))
+    cx = np.array([[1, 0, 0, 0], [0, 1, 0, 0], [0, 0, 0, 1], [0, 0, 1, 0]], dtype=float)
+    g_jl = cx.reshape(2, 2, 2, 2, order="F")  # Julia reshape: axes (plug2, plug1, plug2', plug1')
+    G = np.transpose(g_jl, (1, 0, 3, 2))  # → [plug1, plug2, plug1', plug2']
+    O.simple_update(psi, G, [1, 2])
+    a, b = psi.site(1), psi.site(2)  # (1, 2, χ), (χ, 2, 1)
+    assert a.shape[2] == 2  # zero singular value kept
+    assert np.allclose(np.abs(a[0, :, 0]), [0, 1]) and np.allclose(np.abs(a[0, :, 1]), [0, 0])
+    assert np.allclose(np.abs(b[0, :, 0]), [1, 0]) and np.allclose(np.abs(b[1, :, 0]), [0, 0])
+
+
+def test_overlap_norm_amplitude_consistency():
+    from tenetgb import workloads as W
+
+    psi = O.OMPS(W.random_mps_arrays(10, 2, 8, seed=11, orthogonalize=False))
+    v = O.contract_state(psi)
+    ov = O.overlap(psi, psi)
+    assert abs(ov - np.vdot(v, v)) <= 1e-12 * abs(ov)
+    n = O.norm(psi.copy())
+    assert abs(n**2 - ov.real) <= 1e-12 * ov.real
+    bits = "0110100101"
+    amp = O.amplitude(O.product_state_vectors(bits), psi)
+    idx = int(bits, 2)  # C-order flattening: site 1 is the most significant
+    assert abs(amp - v[idx]) <= 1e-12 * abs(v).max()
+    z, _ = O.local_expectations(psi, W.pauli_z())
+    zs = []
+    for i in range(10):
+        pz = psi.copy()
+        O.simple_update(pz, W.pauli_z(), [i + 1])
+        zs.append(O.overlap(psi, pz) / ov)
+    assert np.allclose(z, zs, rtol=1e-10, atol=1e-12)
+
+
+def test_tebd_small_unitary_invariants():
+    from tenetgb import workloads as W
+
+    sites, layers = W.tebd_workload(L=12, chi0=4, n_layers=4)
+    psi = O.OMPS(sites)
+    O.tebd(psi, layers, maxdim=None, threshold=None)
+    # no truncation: the evolution is exact and unitary
+    assert abs(O.overlap(psi, psi) - 1) < 1e-12
+    v0 = O.contract_state(O.OMPS(sites))
+    # apply the same gates to the dense vector
+    v = v0.reshape([2] * 12)
+    for start, gates in layers:
+        for j, G in enumerate(gates):
+            a = start + 2 * j - 1
+            v = np.moveaxis(np.tensordot(G, v, axes=([2, 3], [a, a + 1])), [0, 1], [a, a + 1])
+    assert np.allclose(O.contract_state(psi), v.reshape(-1), atol=1e-12)
