@@ -1,0 +1,226 @@
+/*
+ * tenet_gb300.h — C ABI of libtenetgb.so, the GB300 (sm_103a) implementation of the
+ * tensor-network hot path of Tenet.jl v0.10.3: pairwise contraction of Tensors and the
+ * QR/SVD factorisation + truncation behind canonize!, compress!/truncate!,
+ * simple_update!/evolve!, overlap and norm on MPS.
+ *
+ * Tenet never does arithmetic itself: it calls Muscle.jl on Tangles.Tensor values.  The
+ * entry points below are what a Julia `ccall` binding of those Muscle calls binds, plus
+ * device-resident MPS operations that keep a whole sweep on the GPU.  Every function is
+ * `extern "C"`, takes plain pointers and sizes, and returns a tn_status_t (0 = OK).
+ *
+ * Conventions
+ *  - Arrays are column-major (Julia layout).  Complex values are interleaved (re, im),
+ *    identical to Julia's Complex{Float64} / Complex{Float32}.
+ *  - Pointers named d_* or documented as "device" are device pointers (from tn_alloc or
+ *    any CUDA allocation on the context's device); "host" pointers are ordinary memory.
+ *  - All work is enqueued on the context's stream (tn_set_stream); results written to
+ *    host memory are complete when the call returns.
+ *  - On error the call returns a status and tn_last_error_string() describes it.
+ *  - A tn_ctx must not be used from two host threads at once (one context per thread
+ *    or stream).
+ */
+#ifndef TENET_GB300_H
+#define TENET_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (mapped to ArgumentError / OutOfMemoryError / ErrorException by the
+ *      Julia binding, like Tenet's @argcheck, src/Operations/compress.jl:30-32) ---- */
+typedef int32_t tn_status_t;
+#define TN_OK 0
+#define TN_EINVAL 1       /* bad argument: shape, rank, mode labels, null pointer */
+#define TN_ENOMEM 2       /* device allocation failed or the HBM budget is exhausted */
+#define TN_ENOCONV 3      /* Jacobi SVD hit its sweep cap before convergence */
+#define TN_ETIMEOUT 4     /* a bounded device wait or a serving deadline ran out */
+#define TN_ECUDA 5        /* CUDA runtime error (message in tn_last_error_string) */
+#define TN_EUNSUPPORTED 6 /* dtype / precision combination not implemented */
+
+/* element types */
+typedef enum { TN_F32 = 0, TN_F64 = 1, TN_C32 = 2, TN_C64 = 3 } tn_dtype_t;
+
+/* arithmetic modes of the contraction GEMMs and factorisations.
+ * TN_PREC_NATIVE: the dtype's own arithmetic (FP64 for C64/F64, FP32 for C32/F32).
+ * TN_PREC_MIXED: for C64 data, contractions as split-precision tensor-core products and
+ *   the SVD as an FP32 Jacobi pre-pass followed by FP64 Jacobi sweeps; FP64 is kept for
+ *   the rotations, the truncation decision and norm/overlap accumulation. */
+typedef enum { TN_PREC_NATIVE = 0, TN_PREC_MIXED = 1 } tn_precision_t;
+
+#define TN_MAX_RANK 8
+
+typedef struct tn_ctx tn_ctx;
+
+/* ------------------------------------------------------------------------------------
+ * context, memory, stream
+ * ---------------------------------------------------------------------------------- */
+tn_status_t tn_create(tn_ctx** ctx, int device);
+tn_status_t tn_destroy(tn_ctx* ctx);
+/* stream: a cudaStream_t (NULL = the context's own stream) */
+tn_status_t tn_set_stream(tn_ctx* ctx, void* stream);
+void* tn_get_stream(tn_ctx* ctx);
+tn_status_t tn_sync(tn_ctx* ctx);
+tn_status_t tn_alloc(tn_ctx* ctx, size_t bytes, void** dptr);
+tn_status_t tn_free(tn_ctx* ctx, void* dptr);
+tn_status_t tn_memcpy_h2d(tn_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
+tn_status_t tn_memcpy_d2h(tn_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
+tn_status_t tn_memcpy_d2d(tn_ctx* ctx, void* d_dst, const void* d_src, size_t bytes);
+/* device HBM budget for MPS storage and workspaces (0 = unlimited) */
+tn_status_t tn_set_hbm_budget(tn_ctx* ctx, size_t bytes);
+tn_status_t tn_hbm_in_use(tn_ctx* ctx, size_t* bytes);
+/* number of library kernels launched on this context since creation */
+tn_status_t tn_kernel_launches(tn_ctx* ctx, int64_t* count);
+const char* tn_last_error_string(tn_ctx* ctx);
+const char* tn_version(void);
+
+/* ------------------------------------------------------------------------------------
+ * K1 — index permutation (replaces Julia `permutedims` inside Muscle.binary_einsum and
+ * Muscle.fuse; reached from binary_einsum call sites e.g. src/Operations/canonize.jl:61)
+ * out = permutedims(in, perm); out is dense column-major with dims[perm[j]] at j.
+ * in_strides may be NULL (dense column-major input).  perm is 0-based.
+ * ---------------------------------------------------------------------------------- */
+tn_status_t tn_permute(tn_ctx* ctx, tn_dtype_t dtype, int32_t rank, const int64_t* dims,
+                       const int64_t* in_strides, const int32_t* perm, const void* d_in,
+                       void* d_out, int32_t conj);
+
+/* ------------------------------------------------------------------------------------
+ * K2 — batched strided GEMM  C = alpha op(A) op(B) + beta C   (op: 'N', 'T', 'C')
+ * alpha/beta are host scalars of the dtype's real type pair: for complex dtypes two
+ * doubles (re, im); for real dtypes one double.  Replaces the BLAS gemm in
+ * Muscle.binary_einsum.
+ * ---------------------------------------------------------------------------------- */
+tn_status_t tn_gemm(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, char opa, char opb,
+                    int64_t m, int64_t n, int64_t k, const double* alpha, const void* d_A,
+                    int64_t lda, int64_t strideA, const void* d_B, int64_t ldb,
+                    int64_t strideB, const double* beta, void* d_C, int64_t ldc,
+                    int64_t strideC, int64_t batch);
+
+/* ------------------------------------------------------------------------------------
+ * Muscle.binary_einsum(a, b; dims) on dense column-major tensors with integer mode
+ * labels.  Modes of c that appear in both a and b are kept (Hadamard / batch modes,
+ * the `dims=Index[]` case of src/Operations/canonize.jl:44); modes in both a and b but
+ * not in c are contracted; every other mode must appear in exactly one input and in c.
+ * c->dims is filled from a/b.  Call sites: canonize.jl:44,47,61,100;
+ * simple_update.jl:34; overlap.jl:26-46.
+ * ---------------------------------------------------------------------------------- */
+typedef struct {
+  int32_t rank;
+  int64_t dims[TN_MAX_RANK];
+  int32_t modes[TN_MAX_RANK];
+  void* data; /* device, dense column-major */
+} tn_tensor;
+
+tn_status_t tn_contract(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec,
+                        const tn_tensor* a, const tn_tensor* b, tn_tensor* c);
+
+/* ------------------------------------------------------------------------------------
+ * K3 — thin QR (Muscle.tensor_qr_thin, called at src/Operations/canonize.jl:58):
+ * A (m×n, column-major, lda) = Q (m×k) R (k×n), k = min(m,n), batched with strides.
+ * Blocked Householder: R has a real non-negative... (LAPACK sign convention: R_ii real).
+ * ---------------------------------------------------------------------------------- */
+tn_status_t tn_qr_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int64_t m,
+                       int64_t n, const void* d_A, int64_t lda, int64_t strideA, void* d_Q,
+                       int64_t strideQ, void* d_R, int64_t strideR, int64_t batch);
+
+/* ------------------------------------------------------------------------------------
+ * K4 — thin SVD (Muscle.tensor_svd_thin, src/Operations/canonize.jl:41,97;
+ * evolve.jl:62,92): A (m×n) = U diag(S) Vh, k = min(m,n), S real descending (always
+ * FP64 on output), U m×k, Vh k×n.  One-sided Jacobi with warp-shuffle reductions.
+ * ---------------------------------------------------------------------------------- */
+tn_status_t tn_svd_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int64_t m,
+                        int64_t n, const void* d_A, int64_t lda, int64_t strideA, void* d_U,
+                        int64_t strideU, double* d_S, int64_t strideS, void* d_Vh,
+                        int64_t strideVh, int64_t batch);
+
+/* truncation rank select: keep min(maxdim, k) values (maxdim <= 0: no cap), then those
+ * with |s| > threshold (threshold <= 0: no threshold), at least one.  Mirrors
+ * src/Operations/compress.jl:47-59.  S is a device array; rank written to *rank (host). */
+tn_status_t tn_truncation_rank(tn_ctx* ctx, const double* d_S, int64_t k, int64_t maxdim,
+                               double threshold, int64_t* rank);
+
+/* ------------------------------------------------------------------------------------
+ * K5 — small fused ops
+ * ---------------------------------------------------------------------------------- */
+/* Muscle.hadamard(t, s) along `axis` (src/Operations/canonize.jl:198,209):
+ * out = t .* s (broadcast along axis); s is real FP64 of length dims[axis]. */
+tn_status_t tn_hadamard(tn_ctx* ctx, tn_dtype_t dtype, int32_t rank, const int64_t* dims,
+                        int32_t axis, const void* d_t, const double* d_s, void* d_out);
+/* ||x||_2 accumulated in FP64 (LinearAlgebra.norm on a Tensor, norm.jl:27,33) */
+tn_status_t tn_norm2(tn_ctx* ctx, tn_dtype_t dtype, int64_t n, const void* d_x,
+                     double* h_out);
+tn_status_t tn_scale(tn_ctx* ctx, tn_dtype_t dtype, int64_t n, void* d_x, double s);
+
+/* Muscle.simple_update(A, ia, B, ib, bond, op, oa, ob; maxdim, absorb=AbsorbEqually())
+ * (called at src/Operations/simple_update.jl:53-64): A (chl, d1, chm), B (chm, d2, chr),
+ * G (d1, d2, d1, d2) indices [out_a, out_b, in_a, in_b]; θ = Σ G·A·B, thin SVD over
+ * (chl,d1)|(d2,chr), keep (maxdim, threshold) as tn_truncation_rank, A' = U√S (chl,d1,k),
+ * B' = √S Vh (k,d2,chr).  A_out/B_out must hold chl*d1*min(d1*chl, d2*chr) and
+ * min(..)*d2*chr elements.  S_out (device, may be NULL) receives the kept values. */
+tn_status_t tn_simple_update(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec,
+                             int64_t chl, int64_t d1, int64_t chm, int64_t d2, int64_t chr,
+                             const void* d_A, const void* d_B, const void* d_G,
+                             int64_t maxdim, double threshold, void* d_Aout, void* d_Bout,
+                             double* d_Sout, int64_t* rank);
+
+/* ------------------------------------------------------------------------------------
+ * Device-resident MPS (src/Components/MPS.jl:13-94) with the canonical-form trait
+ * (src/CanonicalForm.jl) kept in native code.  Site i (1-based) is a (χ_{i-1}, d, χ_i)
+ * column-major C64 tensor; χ_0 = χ_L = 1.  The operations follow Tenet's algorithms:
+ *  canonize (canonize.jl:121-252), compress (compress.jl:21-69), simple_update
+ *  (simple_update.jl:82-92), overlap (overlap.jl:36-50), amplitude (overlap.jl:22-32),
+ *  norm / normalize (norm.jl:17-37, normalize.jl:15-37).
+ * ---------------------------------------------------------------------------------- */
+typedef struct tn_mps tn_mps;
+
+#define TN_FORM_NONCANONICAL 0
+#define TN_FORM_MIXED 1
+#define TN_FORM_BOND 2
+
+/* create an MPS of L sites, physical dim d; bond_dims[L-1] initial bonds; max_bond caps
+ * the storage reserved per site (0 = the initial bonds only, growing on demand). */
+tn_status_t tn_mps_create(tn_ctx* ctx, int32_t L, int32_t d, const int64_t* bond_dims,
+                          int64_t max_bond, tn_precision_t prec, tn_mps** out);
+tn_status_t tn_mps_destroy(tn_mps* mps);
+tn_status_t tn_mps_copy(const tn_mps* src, tn_mps** out);
+/* host data of site i (1-based), column-major (χl, d, χr) C64 */
+tn_status_t tn_mps_set_site(tn_mps* mps, int32_t site, int64_t chl, int64_t chr,
+                            const void* h_data);
+tn_status_t tn_mps_get_site(const tn_mps* mps, int32_t site, void* h_data);
+tn_status_t tn_mps_bond_dims(const tn_mps* mps, int64_t* h_bonds /* L-1 */);
+tn_status_t tn_mps_set_precision(tn_mps* mps, tn_precision_t prec);
+/* form: kind + (lo, hi) sites for MIXED, (a, a+1) for BOND */
+tn_status_t tn_mps_form(const tn_mps* mps, int32_t* kind, int32_t* lo, int32_t* hi);
+tn_status_t tn_mps_set_form(tn_mps* mps, int32_t kind, int32_t lo, int32_t hi);
+/* Λ at the bond-canonical centre (FP64 host array of length χ_a) */
+tn_status_t tn_mps_get_lambda(const tn_mps* mps, double* h_lambda, int64_t* len);
+
+tn_status_t tn_mps_canonize_mixed(tn_mps* mps, int32_t lo, int32_t hi);
+tn_status_t tn_mps_canonize_bond(tn_mps* mps, int32_t a /* bond a-(a+1) */);
+/* bond a = 0: every bond 1..L-1 in turn; maxdim <= 0 / threshold <= 0 disable each cut */
+tn_status_t tn_mps_compress(tn_mps* mps, int32_t a, int64_t maxdim, double threshold);
+/* gate on sites (a) [n_sites = 1, G d×d] or (a, a+1) [n_sites = 2, G d×d×d×d];
+ * G is a host array (column-major C64). */
+tn_status_t tn_mps_simple_update(tn_mps* mps, int32_t n_sites, int32_t a, const void* h_G,
+                                 int64_t maxdim, double threshold);
+/* whole brickwork circuit: layers x gates; h_gates holds n_gates[l] 2-site gates of
+ * d^4 C64 each per layer, layer l starting at bond starts[l]; gates applied left→right */
+tn_status_t tn_mps_evolve_brickwork(tn_mps* mps, int32_t n_layers, const int32_t* starts,
+                                    const int32_t* n_gates, const void* h_gates,
+                                    int64_t maxdim, double threshold);
+/* ⟨b|a⟩ = Σ a·conj(b); h_out = (re, im) */
+tn_status_t tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* h_out);
+tn_status_t tn_mps_norm(tn_mps* mps, double* h_out);
+tn_status_t tn_mps_normalize(tn_mps* mps);
+/* ⟨bits|ψ⟩ with product vectors (not conjugated): h_vectors is L×d C64 (site-major) */
+tn_status_t tn_mps_amplitude(const tn_mps* mps, const void* h_vectors, double* h_out);
+/* ⟨ψ|O_i|ψ⟩/⟨ψ|ψ⟩ for every site i, O a host d×d C64; h_out is L×(re,im) */
+tn_status_t tn_mps_local_expectations(const tn_mps* mps, const void* h_op, double* h_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TENET_GB300_H */

@@ -1,0 +1,227 @@
+// Internal definitions shared by the translation units of libtenetgb.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "tenet_gb300.h"
+
+// ---------------------------------------------------------------------------------
+// complex scalars: interleaved (re, im) == Julia Complex{T} == cuDoubleComplex layout
+// ---------------------------------------------------------------------------------
+template <typename T>
+struct alignas(2 * sizeof(T)) cx {
+  T x, y;
+};
+using cxd = cx<double>;
+using cxf = cx<float>;
+
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> mkcx(T a, T b) {
+  cx<T> r;
+  r.x = a;
+  r.y = b;
+  return r;
+}
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator+(cx<T> a, cx<T> b) {
+  return mkcx<T>(a.x + b.x, a.y + b.y);
+}
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator-(cx<T> a, cx<T> b) {
+  return mkcx<T>(a.x - b.x, a.y - b.y);
+}
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator*(cx<T> a, cx<T> b) {
+  return mkcx<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> operator*(T s, cx<T> a) {
+  return mkcx<T>(s * a.x, s * a.y);
+}
+template <typename T>
+__host__ __device__ __forceinline__ cx<T> conjg(cx<T> a) {
+  return mkcx<T>(a.x, -a.y);
+}
+template <typename T>
+__host__ __device__ __forceinline__ T abs2(cx<T> a) {
+  return a.x * a.x + a.y * a.y;
+}
+// acc += a * b
+template <typename T>
+__host__ __device__ __forceinline__ void cfma(cx<T>& acc, cx<T> a, cx<T> b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+// acc += conj(a) * b
+template <typename T>
+__host__ __device__ __forceinline__ void cfma_cj(cx<T>& acc, cx<T> a, cx<T> b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------------
+struct tn_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  cudaStream_t own_stream = nullptr;
+  std::string last_error;
+  // workspace arena: reserved per top-level call, carved with ws_take
+  char* ws = nullptr;
+  size_t ws_cap = 0;
+  size_t ws_top = 0;
+  // small pinned host buffer for scalar read-backs
+  void* pinned = nullptr;
+  int* d_flags = nullptr;  // device status / convergence words
+  size_t flags_cap = 0;
+  // accounting
+  size_t budget = 0;  // 0 = unlimited
+  size_t in_use = 0;
+  std::unordered_map<void*, size_t> allocs;
+  int64_t launches = 0;
+  // instantiated CUDA graphs (e.g. one Jacobi sweep), keyed by shape + buffer addresses
+  std::unordered_map<std::string, cudaGraphExec_t> graphs;
+};
+
+tn_status_t tn_set_error(tn_ctx* ctx, tn_status_t st, const char* fmt, ...);
+
+#define TN_CHECK_CUDA(ctx, call)                                                    \
+  do {                                                                              \
+    cudaError_t _e = (call);                                                        \
+    if (_e != cudaSuccess)                                                          \
+      return tn_set_error((ctx), TN_ECUDA, "%s failed: %s (%s:%d)", #call,          \
+                          cudaGetErrorString(_e), __FILE__, __LINE__);              \
+  } while (0)
+
+#define TN_RETURN_IF(st)           \
+  do {                             \
+    tn_status_t _s = (st);         \
+    if (_s != TN_OK) return _s;    \
+  } while (0)
+
+#define TN_ARG(ctx, cond, msg)                                   \
+  do {                                                           \
+    if (!(cond)) return tn_set_error((ctx), TN_EINVAL, "%s", msg); \
+  } while (0)
+
+// after every launch: count it and surface launch errors
+#define TN_LAUNCHED(ctx)                                                               \
+  do {                                                                                 \
+    (ctx)->launches++;                                                                 \
+    cudaError_t _e = cudaGetLastError();                                               \
+    if (_e != cudaSuccess)                                                             \
+      return tn_set_error((ctx), TN_ECUDA, "kernel launch failed: %s (%s:%d)",         \
+                          cudaGetErrorString(_e), __FILE__, __LINE__);                 \
+  } while (0)
+
+// device allocation with accounting against the HBM budget
+tn_status_t tn_dev_alloc(tn_ctx* ctx, size_t bytes, void** p);
+tn_status_t tn_dev_free(tn_ctx* ctx, void* p);
+
+// workspace: reserve (may reallocate: only between operations), then take
+tn_status_t ws_reserve(tn_ctx* ctx, size_t bytes);
+inline size_t ws_round(size_t b) { return (b + 255) & ~size_t(255); }
+template <typename T>
+T* ws_take(tn_ctx* ctx, size_t count) {
+  size_t b = ws_round(count * sizeof(T));
+  char* p = ctx->ws + ctx->ws_top;
+  ctx->ws_top += b;
+  return reinterpret_cast<T*>(p);
+}
+inline void ws_reset(tn_ctx* ctx) { ctx->ws_top = 0; }
+
+// flag words (device ints), at least n, zeroed by caller when needed
+tn_status_t ctx_flags(tn_ctx* ctx, size_t n, int** out);
+
+inline size_t dtype_size(tn_dtype_t t) {
+  switch (t) {
+    case TN_F32: return 4;
+    case TN_F64: return 8;
+    case TN_C32: return 8;
+    case TN_C64: return 16;
+  }
+  return 0;
+}
+inline bool dtype_complex(tn_dtype_t t) { return t == TN_C32 || t == TN_C64; }
+
+inline unsigned cdiv(int64_t a, int64_t b) { return (unsigned)((a + b - 1) / b); }
+
+// ---------------------------------------------------------------------------------
+// internal entry points shared across translation units (typed, no validation)
+// ---------------------------------------------------------------------------------
+template <typename T>
+tn_status_t gemm_cx(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64_t k,
+                    cx<T> alpha, const cx<T>* A, int64_t lda, int64_t sA, const cx<T>* B,
+                    int64_t ldb, int64_t sB, cx<T> beta, cx<T>* C, int64_t ldc, int64_t sC,
+                    int64_t batch);
+
+template <typename T>
+tn_status_t permute_t(tn_ctx* ctx, int rank, const int64_t* dims, const int64_t* in_strides,
+                      const int32_t* perm, const T* in, T* out, bool conj);
+
+// (conjugate) transpose of a batch of column-major m×n matrices: out (n×m)
+template <typename T>
+tn_status_t transpose_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* in, int64_t lda,
+                         int64_t sIn, cx<T>* out, int64_t ldo, int64_t sOut, int64_t batch,
+                         bool conj);
+
+// workspace bytes needed by qr_cx / svd_cx
+template <typename T>
+size_t qr_workspace(int64_t m, int64_t n, int64_t batch);
+template <typename T>
+tn_status_t qr_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda, int64_t sA,
+                  cx<T>* Q, int64_t sQ, cx<T>* R, int64_t sR, int64_t batch);
+
+template <typename T>
+size_t svd_workspace(int64_t m, int64_t n, int64_t batch);
+// one-sided Jacobi SVD, m >= n required here; U m×n, S n (FP64), V n×n (not Vh)
+template <typename T>
+tn_status_t svd_tall_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda,
+                        int64_t sA, cx<T>* U, int64_t sU, double* S, int64_t sS, cx<T>* V,
+                        int64_t sV, int64_t batch, int* sweeps_out);
+
+// mixed precision SVD (C64 data): FP32 Jacobi pre-pass + FP64 polish
+size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch);
+tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int64_t lda,
+                           int64_t sA, cxd* U, int64_t sU, double* S, int64_t sS, cxd* V,
+                           int64_t sV, int64_t batch);
+
+// full thin SVD for any m, n: U m×k, S k, Vh k×n (reserves its own workspace when
+// ws_managed is false)
+size_t svd_any_workspace(tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n,
+                         int64_t batch);
+tn_status_t svd_any(tn_ctx* ctx, tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n,
+                    const void* A, int64_t lda, int64_t sA, void* U, int64_t sU, double* S,
+                    int64_t sS, void* Vh, int64_t sVh, int64_t batch);
+
+// K5 helpers
+tn_status_t rank_select(tn_ctx* ctx, const double* S, int64_t k, int64_t maxdim,
+                        double threshold, int64_t* rank);
+template <typename T>
+tn_status_t scale_cols_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld,
+                            const double* S);
+template <typename T>
+tn_status_t scale_rows_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld,
+                            const double* S);
+tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out);
+tn_status_t copy_matrix_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src,
+                            int64_t lds, cxd* dst, int64_t ldd);

@@ -1,0 +1,812 @@
+// Device-resident MPS and the Tenet operations on it, with the canonical-form trait kept
+// in native code.  Every site tensor stays in HBM between calls; only bond dimensions,
+// the form and scalar results cross to the host.
+//
+//   site i (1-based): (χ_{i-1}, d, χ_i) ComplexF64, column-major — Tenet's (:l, :o, :r)
+//   order (src/Components/MPS.jl:50-94) with the open-end bonds χ_0 = χ_L = 1.
+//
+// Algorithms restated from Tenet.jl v0.10.3:
+//   gauge move            generic_canonize_site!       src/Operations/canonize.jl:23-76
+//   bond gauge move       generic_bond_canonize_site!  src/Operations/canonize.jl:78-116
+//   form transitions      generic_mps_canonize!        src/Operations/canonize.jl:121-252
+//   compress / truncate!  generic_mps_compress!        src/Operations/compress.jl:21-69
+//   simple update         simple_update!(::MPS, op)    src/Operations/simple_update.jl:20-92
+//   overlap               overlap(::MPS, ::MPS)        src/Operations/overlap.jl:36-50
+//   amplitude             overlap(::ProductState, ψ)   src/Operations/overlap.jl:22-32
+//   norm / normalize!                                   src/Operations/norm.jl:17-37, normalize.jl:15-37
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "tn_internal.cuh"
+
+struct tn_mps {
+  tn_ctx* ctx = nullptr;
+  int L = 0, d = 0;
+  std::vector<int64_t> bond;  // L+1 entries, bond[0] = bond[L] = 1
+  std::vector<int64_t> cap_bond;  // storage caps per bond
+  std::vector<cxd*> site;     // 1-based: site[1..L]
+  std::vector<size_t> cap;    // elements reserved per site
+  int kind = TN_FORM_MIXED, lo = 1, hi = 1;
+  double* lam = nullptr;      // Λ at the bond-canonical centre (device, FP64)
+  int64_t lam_len = 0;
+  size_t lam_cap = 0;
+  tn_precision_t prec = TN_PREC_NATIVE;
+  cxd* gates = nullptr;       // device copy of gates for evolve
+  size_t gates_cap = 0;
+};
+
+namespace {
+
+inline int64_t sz(const tn_mps* p, int i) { return p->bond[i - 1] * p->d * p->bond[i]; }
+
+tn_status_t ensure_site(tn_mps* p, int i, size_t elems) {
+  if (elems <= p->cap[i]) return TN_OK;
+  tn_ctx* ctx = p->ctx;
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  void* np = nullptr;
+  TN_RETURN_IF(tn_dev_alloc(ctx, elems * sizeof(cxd), &np));
+  if (p->site[i]) {
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(np, p->site[i], sizeof(cxd) * sz(p, i), cudaMemcpyDeviceToDevice, ctx->stream));
+    TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    TN_RETURN_IF(tn_dev_free(ctx, p->site[i]));
+  }
+  p->site[i] = (cxd*)np;
+  p->cap[i] = elems;
+  return TN_OK;
+}
+
+tn_status_t ensure_lam(tn_mps* p, int64_t n) {
+  if ((size_t)n <= p->lam_cap) return TN_OK;
+  tn_ctx* ctx = p->ctx;
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (p->lam) TN_RETURN_IF(tn_dev_free(ctx, p->lam));
+  void* np = nullptr;
+  size_t c = std::max<size_t>(n, 64);
+  TN_RETURN_IF(tn_dev_alloc(ctx, c * sizeof(double), &np));
+  p->lam = (double*)np;
+  p->lam_cap = c;
+  return TN_OK;
+}
+
+const cxd kOne = {1.0, 0.0};
+const cxd kZero = {0.0, 0.0};
+
+// ---------------------------------------------------------------------------------
+// gauge moves (canonize.jl:23-116)
+// ---------------------------------------------------------------------------------
+
+// QR of site i across bond (i, i+1); R pushed into site i+1
+tn_status_t gauge_right(tn_mps* p, int i, bool svd_lambda) {
+  tn_ctx* ctx = p->ctx;
+  const int64_t chl = p->bond[i - 1], chr = p->bond[i], d = p->d;
+  // size-1 bonds are skipped by the QR move (canonize.jl:38); the bond-canonical move
+  // still factorises them so that a Λ of length 1 exists for norm / compress
+  if (chr == 1 && !svd_lambda) return TN_OK;
+  const int64_t m = chl * d, n = chr, k = std::min(m, n);
+  const int64_t chn = p->bond[i + 1];
+  const int64_t nb_cols = d * chn;  // columns of site i+1 as (χ_i × d χ_{i+1})
+  size_t need = ws_round(sizeof(cxd) * (size_t)(k * n)) + ws_round(sizeof(cxd) * (size_t)(k * nb_cols));
+  if (svd_lambda)
+    need += ws_round(sizeof(cxd) * (size_t)(m * k)) + svd_any_workspace(TN_C64, p->prec, m, n, 1);
+  else
+    need += qr_workspace<double>(m, n, 1);
+  TN_RETURN_IF(ws_reserve(ctx, need));
+  cxd* R = ws_take<cxd>(ctx, (size_t)(k * n));
+  cxd* tmp = ws_take<cxd>(ctx, (size_t)(k * nb_cols));
+  if (svd_lambda) {
+    cxd* U = ws_take<cxd>(ctx, (size_t)(m * k));
+    TN_RETURN_IF(ensure_lam(p, k));
+    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, p->site[i], m, 0, U, 0, p->lam, 0, R, 0, 1));
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], U, sizeof(cxd) * m * k, cudaMemcpyDeviceToDevice, ctx->stream));
+    p->lam_len = k;
+  } else {
+    TN_RETURN_IF(qr_cx<double>(ctx, m, n, p->site[i], m, 0, p->site[i], 0, R, 0, 1));
+  }
+  // site i+1 ← R · B
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k, nb_cols, n, kOne, R, k, 0, p->site[i + 1], n, 0, kZero, tmp, k, 0, 1));
+  TN_RETURN_IF(ensure_site(p, i + 1, (size_t)(k * nb_cols)));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i + 1], tmp, sizeof(cxd) * k * nb_cols, cudaMemcpyDeviceToDevice, ctx->stream));
+  p->bond[i] = k;
+  return TN_OK;
+}
+
+// factorise site i across bond (i-1, i); the non-isometric part goes into site i-1
+tn_status_t gauge_left(tn_mps* p, int i, bool svd_lambda) {
+  tn_ctx* ctx = p->ctx;
+  const int64_t chl = p->bond[i - 1], chr = p->bond[i], d = p->d;
+  if (chl == 1 && !svd_lambda) return TN_OK;
+  const int64_t m = d * chr, n = chl, k = std::min(m, n);  // Mᴴ is (d χ_r) × χ_l
+  const int64_t chp = p->bond[i - 2];
+  const int64_t rows_b = chp * d;  // site i-1 as (χ_{i-2} d × χ_{i-1})
+  size_t need = ws_round(sizeof(cxd) * (size_t)(m * n)) * 2 + ws_round(sizeof(cxd) * (size_t)(k * n)) +
+                ws_round(sizeof(cxd) * (size_t)(rows_b * k));
+  if (svd_lambda)
+    need += svd_any_workspace(TN_C64, p->prec, m, n, 1);
+  else
+    need += qr_workspace<double>(m, n, 1);
+  TN_RETURN_IF(ws_reserve(ctx, need));
+  cxd* Mh = ws_take<cxd>(ctx, (size_t)(m * n));
+  cxd* Q = ws_take<cxd>(ctx, (size_t)(m * n));
+  cxd* R = ws_take<cxd>(ctx, (size_t)(k * n));
+  cxd* tmp = ws_take<cxd>(ctx, (size_t)(rows_b * k));
+  // Mᴴ: site as (χ_l × d χ_r) matrix, conjugate-transposed
+  TN_RETURN_IF(transpose_cx<double>(ctx, n, m, p->site[i], n, 0, Mh, m, 0, 1, true));
+  if (svd_lambda) {
+    TN_RETURN_IF(ensure_lam(p, k));
+    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, Mh, m, 0, Q, 0, p->lam, 0, R, 0, 1));
+    p->lam_len = k;
+  } else {
+    TN_RETURN_IF(qr_cx<double>(ctx, m, n, Mh, m, 0, Q, 0, R, 0, 1));
+  }
+  // new site i = Qᴴ (k × d χ_r)
+  TN_RETURN_IF(transpose_cx<double>(ctx, m, k, Q, m, 0, p->site[i], k, 0, 1, true));
+  // site i-1 ← B · Rᴴ
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'C', rows_b, k, n, kOne, p->site[i - 1], rows_b, 0, R, k, 0, kZero, tmp, rows_b,
+                               0, 1));
+  TN_RETURN_IF(ensure_site(p, i - 1, (size_t)(rows_b * k)));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i - 1], tmp, sizeof(cxd) * rows_b * k, cudaMemcpyDeviceToDevice, ctx->stream));
+  p->bond[i - 1] = k;
+  return TN_OK;
+}
+
+// absorb Λ into a neighbouring site along the bond (canonize.jl:198,209)
+tn_status_t absorb_lambda(tn_mps* p, int i, bool into_left_index) {
+  tn_ctx* ctx = p->ctx;
+  int64_t dims[3] = {p->bond[i - 1], p->d, p->bond[i]};
+  int axis = into_left_index ? 0 : 2;
+  if (dims[axis] != p->lam_len)
+    return tn_set_error(ctx, TN_EINVAL, "absorb: Λ length %lld does not match bond %lld", (long long)p->lam_len,
+                        (long long)dims[axis]);
+  return tn_hadamard(ctx, TN_C64, 3, dims, axis, p->site[i], p->lam, p->site[i]);
+}
+
+// ---------------------------------------------------------------------------------
+// form transitions (canonize.jl:121-252)
+// ---------------------------------------------------------------------------------
+tn_status_t canonize_mixed(tn_mps* p, int lo, int hi);
+
+tn_status_t mixed_to_mixed(tn_mps* p, int lo, int hi) {
+  if (p->kind == TN_FORM_MIXED && p->lo == lo && p->hi == hi) return TN_OK;
+  const int src_left = p->lo, src_right = p->hi;
+  const int dst_left = lo - 1, dst_right = hi + 1;
+  for (int i = src_left; i <= dst_left; ++i) TN_RETURN_IF(gauge_right(p, i, false));
+  for (int i = src_right; i >= dst_right; --i) TN_RETURN_IF(gauge_left(p, i, false));
+  p->kind = TN_FORM_MIXED;
+  p->lo = lo;
+  p->hi = hi;
+  return TN_OK;
+}
+
+// SVD of `site` across bond (a, a+1) without absorbing Λ (canonize.jl:78-116)
+tn_status_t bond_gauge(tn_mps* p, int site, int a) {
+  if (site == a) return gauge_right(p, site, true);
+  return gauge_left(p, site, true);
+}
+
+tn_status_t canonize_bond(tn_mps* p, int a) {
+  const int na = a, nb = a + 1;
+  if (p->kind == TN_FORM_NONCANONICAL) {
+    p->kind = TN_FORM_MIXED;
+    p->lo = 1;
+    p->hi = p->L;
+  }
+  if (p->kind == TN_FORM_BOND) {
+    if (p->lo == na) return TN_OK;
+    const int old_min = p->lo, old_max = p->hi;
+    // BondCanonical → BondCanonical (canonize.jl:221-246) goes through Bond → Mixed
+    int target;
+    if (old_max <= na)
+      target = na;
+    else if (nb <= old_min)
+      target = nb;
+    else
+      return tn_set_error(p->ctx, TN_EINVAL, "Cannot canonize from bond %d-%d to bond %d-%d", old_min, old_max, na, nb);
+    TN_RETURN_IF(canonize_mixed(p, target, target));
+    TN_RETURN_IF(bond_gauge(p, target, a));
+    p->kind = TN_FORM_BOND;
+    p->lo = na;
+    p->hi = nb;
+    return TN_OK;
+  }
+  // Mixed → Bond (canonize.jl:151-179)
+  const int old_min = p->lo, old_max = p->hi;
+  int target;
+  if (old_max <= na)
+    target = na;
+  else if (nb <= old_min)
+    target = nb;
+  else if (old_min <= na && nb <= old_max)
+    target = na;
+  else
+    return tn_set_error(p->ctx, TN_EINVAL, "Cannot canonize from mixed %d..%d to bond %d-%d", old_min, old_max, na, nb);
+  TN_RETURN_IF(mixed_to_mixed(p, target, target));
+  TN_RETURN_IF(bond_gauge(p, target, a));
+  p->kind = TN_FORM_BOND;
+  p->lo = na;
+  p->hi = nb;
+  return TN_OK;
+}
+
+tn_status_t canonize_mixed(tn_mps* p, int lo, int hi) {
+  if (p->kind == TN_FORM_NONCANONICAL) {
+    p->kind = TN_FORM_MIXED;
+    p->lo = 1;
+    p->hi = p->L;
+  }
+  if (p->kind == TN_FORM_BOND) {
+    // Bond → Mixed (canonize.jl:181-219): absorb Λ to one side, then sweep
+    const int old_min = p->lo, old_max = p->hi;
+    if (old_max <= lo) {
+      TN_RETURN_IF(absorb_lambda(p, old_max, true));
+      p->kind = TN_FORM_MIXED;
+      p->lo = p->hi = old_max;
+    } else if (hi <= old_min) {
+      TN_RETURN_IF(absorb_lambda(p, old_min, false));
+      p->kind = TN_FORM_MIXED;
+      p->lo = p->hi = old_min;
+    } else {
+      return tn_set_error(p->ctx, TN_EINVAL, "Cannot canonize from bond %d-%d to mixed %d..%d", old_min, old_max, lo, hi);
+    }
+    p->lam_len = 0;
+  }
+  return mixed_to_mixed(p, lo, hi);
+}
+
+// ---------------------------------------------------------------------------------
+// simple update (simple_update.jl:20-92 + Muscle.simple_update with AbsorbEqually)
+// ---------------------------------------------------------------------------------
+}  // namespace
+
+// Output sizing callback: called once the kept rank r is known; returns where A' and B'
+// go (it may grow and move buffers; the gate inputs have been consumed by then).
+typedef tn_status_t (*su_out_fn)(void* arg, int64_t r, cxd** Aout, cxd** Bout);
+
+// θ = G·(A·B) → thin SVD → keep (maxdim, threshold) → A' = U√S, B' = √S Vh.
+// A (chl·d1 × chm), B (chm × d2·chr), G (d1 d2 × d1 d2) column-major.  Reserves the
+// workspace itself.
+tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, int64_t d1, int64_t chm, int64_t d2,
+                               int64_t chr, const cxd* A, const cxd* B, const cxd* dG, int64_t maxdim, double threshold,
+                               su_out_fn out_fn, void* out_arg, double* Sout, int64_t* rank_out) {
+  const int64_t m = chl * d1, n = d2 * chr, k = std::min(m, n), dd = d1 * d2;
+  size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(m * n)) + ws_round(sizeof(cxd) * (size_t)(m * k)) +
+                ws_round(sizeof(double) * (size_t)k) + ws_round(sizeof(cxd) * (size_t)(k * n)) +
+                svd_any_workspace(TN_C64, prec, m, n, 1);
+  TN_RETURN_IF(ws_reserve(ctx, need));
+  cxd* th0 = ws_take<cxd>(ctx, (size_t)(m * n));
+  cxd* th = ws_take<cxd>(ctx, (size_t)(m * n));
+  cxd* U = ws_take<cxd>(ctx, (size_t)(m * k));
+  double* S = ws_take<double>(ctx, (size_t)k);
+  cxd* Vh = ws_take<cxd>(ctx, (size_t)(k * n));
+  // θ0 = A (χl d1 × χm) · B (χm × d2 χr)
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, chm, kOne, A, m, 0, B, chm, 0, kZero, th0, m, 0, 1));
+  // θ[l, (a b), r] = Σ G[(a b), (a' b')] θ0[l, (a' b'), r]  — batched over r
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, dd, dd, kOne, th0, chl, chl * dd, dG, dd, 0, kZero, th, chl,
+                               chl * dd, chr));
+  TN_RETURN_IF(svd_any(ctx, TN_C64, prec, m, n, th, m, 0, U, 0, S, 0, Vh, 0, 1));
+  int64_t r = 0;
+  TN_RETURN_IF(rank_select(ctx, S, k, maxdim, threshold, &r));
+  cxd *Aout = nullptr, *Bout = nullptr;
+  TN_RETURN_IF(out_fn(out_arg, r, &Aout, &Bout));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(Aout, U, sizeof(cxd) * m * r, cudaMemcpyDeviceToDevice, ctx->stream));
+  TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S));
+  TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r));
+  TN_RETURN_IF(scale_rows_sqrt<double>(ctx, Bout, r, n, r, S));
+  if (Sout) TN_CHECK_CUDA(ctx, cudaMemcpyAsync(Sout, S, sizeof(double) * r, cudaMemcpyDeviceToDevice, ctx->stream));
+  *rank_out = r;
+  return TN_OK;
+}
+
+namespace {
+
+struct PairOut {
+  tn_mps* p;
+  int a;
+};
+tn_status_t pair_out(void* arg, int64_t r, cxd** Aout, cxd** Bout) {
+  PairOut* e = (PairOut*)arg;
+  tn_mps* p = e->p;
+  const int64_t m = p->bond[e->a - 1] * p->d, n = p->d * p->bond[e->a + 1];
+  TN_RETURN_IF(ensure_site(p, e->a, (size_t)(m * r)));
+  TN_RETURN_IF(ensure_site(p, e->a + 1, (size_t)(r * n)));
+  *Aout = p->site[e->a];
+  *Bout = p->site[e->a + 1];
+  return TN_OK;
+}
+
+tn_status_t apply_gate2(tn_mps* p, int a, const cxd* dG, int64_t maxdim, double threshold) {
+  const int64_t d = p->d;
+  PairOut e{p, a};
+  int64_t r = 0;
+  TN_RETURN_IF(simple_update_core(p->ctx, p->prec, p->bond[a - 1], d, p->bond[a], d, p->bond[a + 1], p->site[a],
+                                  p->site[a + 1], dG, maxdim, threshold, pair_out, &e, nullptr, &r));
+  p->bond[a] = r;
+  return TN_OK;
+}
+
+tn_status_t apply_gate1(tn_mps* p, int i, const cxd* dG) {
+  tn_ctx* ctx = p->ctx;
+  const int64_t d = p->d, chl = p->bond[i - 1], chr = p->bond[i];
+  TN_RETURN_IF(ws_reserve(ctx, ws_round(sizeof(cxd) * (size_t)(chl * d * chr))));
+  cxd* tmp = ws_take<cxd>(ctx, (size_t)(chl * d * chr));
+  // new[l, a, r] = Σ_b G[a, b] A[l, b, r]  (batched over r)
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, d, d, kOne, p->site[i], chl, chl * d, dG, d, 0, kZero, tmp, chl,
+                               chl * d, chr));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], tmp, sizeof(cxd) * chl * d * chr, cudaMemcpyDeviceToDevice, ctx->stream));
+  return TN_OK;
+}
+
+tn_status_t upload_gates(tn_mps* p, const void* h, size_t elems) {
+  tn_ctx* ctx = p->ctx;
+  if (elems > p->gates_cap) {
+    TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (p->gates) TN_RETURN_IF(tn_dev_free(ctx, p->gates));
+    void* np = nullptr;
+    TN_RETURN_IF(tn_dev_alloc(ctx, elems * sizeof(cxd), &np));
+    p->gates = (cxd*)np;
+    p->gates_cap = elems;
+  }
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->gates, h, elems * sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
+  return TN_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// environments (overlap.jl:36-50): F (χb × χa) ← Bᴴ · (F · A)
+// ---------------------------------------------------------------------------------
+tn_status_t overlap_impl(const tn_mps* a, const tn_mps* b, cxd* out) {
+  tn_ctx* ctx = a->ctx;
+  const int L = a->L, d = a->d;
+  int64_t mx = 1;
+  for (int i = 0; i <= L; ++i) mx = std::max({mx, a->bond[i], b->bond[i]});
+  size_t env = (size_t)(mx * mx), t = (size_t)(mx * d * mx);
+  TN_RETURN_IF(ws_reserve(ctx, 2 * ws_round(sizeof(cxd) * env) + ws_round(sizeof(cxd) * t)));
+  cxd* F = ws_take<cxd>(ctx, env);
+  cxd* F2 = ws_take<cxd>(ctx, env);
+  cxd* T = ws_take<cxd>(ctx, t);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(F, &kOne, sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
+  for (int i = 1; i <= L; ++i) {
+    const int64_t xa = a->bond[i - 1], xa2 = a->bond[i], yb = b->bond[i - 1], yb2 = b->bond[i];
+    // T (yb × d xa2) = F (yb × xa) · A (xa × d xa2)
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', yb, d * xa2, xa, kOne, F, yb, 0, a->site[i], xa, 0, kZero, T, yb, 0, 1));
+    // F2 (yb2 × xa2) = B_matᴴ ((yb d) × yb2)ᴴ · T ((yb d) × xa2)
+    TN_RETURN_IF(
+        gemm_cx<double>(ctx, 'C', 'N', yb2, xa2, yb * d, kOne, b->site[i], yb * d, 0, T, yb * d, 0, kZero, F2, yb2, 0, 1));
+    std::swap(F, F2);
+  }
+  cxd* hp = reinterpret_cast<cxd*>(ctx->pinned);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, F, sizeof(cxd), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = hp[0];
+  return TN_OK;
+}
+
+__global__ void k_zdotc_partial(int64_t n, const cxd* __restrict__ x, const cxd* __restrict__ y, double* partial) {
+  __shared__ double rx[32], ry[32];
+  cxd s = {0, 0};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    cfma_cj(s, x[i], y[i]);
+  s.x = warp_sum(s.x);
+  s.y = warp_sum(s.y);
+  if ((threadIdx.x & 31) == 0) {
+    rx[threadIdx.x >> 5] = s.x;
+    ry[threadIdx.x >> 5] = s.y;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double vx = threadIdx.x < (blockDim.x >> 5) ? rx[threadIdx.x] : 0.0;
+    double vy = threadIdx.x < (blockDim.x >> 5) ? ry[threadIdx.x] : 0.0;
+    vx = warp_sum(vx);
+    vy = warp_sum(vy);
+    if (threadIdx.x == 0) {
+      partial[2 * blockIdx.x] = vx;
+      partial[2 * blockIdx.x + 1] = vy;
+    }
+  }
+}
+__global__ void k_zsum_final(int n, const double* partial, double* out) {
+  if (threadIdx.x == 0) {
+    double sx = 0, sy = 0;
+    for (int i = 0; i < n; ++i) {
+      sx += partial[2 * i];
+      sy += partial[2 * i + 1];
+    }
+    out[0] = sx;
+    out[1] = sy;
+  }
+}
+
+// Σ conj(x)·y in FP64, fixed reduction order
+tn_status_t zdotc(tn_ctx* ctx, int64_t n, const cxd* x, const cxd* y, cxd* out) {
+  int* flags = nullptr;
+  const int nb = 64;
+  TN_RETURN_IF(ctx_flags(ctx, 4 * nb + 8, &flags));
+  double* part = reinterpret_cast<double*>(flags);
+  k_zdotc_partial<<<nb, 256, 0, ctx->stream>>>(n, x, y, part);
+  TN_LAUNCHED(ctx);
+  k_zsum_final<<<1, 32, 0, ctx->stream>>>(nb, part, part + 2 * nb);
+  TN_LAUNCHED(ctx);
+  double* hp = reinterpret_cast<double*>(ctx->pinned);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, part + 2 * nb, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  out->x = hp[0];
+  out->y = hp[1];
+  return TN_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------
+extern "C" {
+
+tn_status_t tn_mps_create(tn_ctx* ctx, int32_t L, int32_t d, const int64_t* bond_dims, int64_t max_bond,
+                          tn_precision_t prec, tn_mps** out) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, L >= 2 && d >= 1 && out, "tn_mps_create: need L >= 2, d >= 1");
+  TN_ARG(ctx, bond_dims != nullptr, "tn_mps_create: null bond_dims");
+  tn_mps* p = new tn_mps();
+  p->ctx = ctx;
+  p->L = L;
+  p->d = d;
+  p->prec = prec;
+  p->bond.assign(L + 1, 1);
+  p->cap_bond.assign(L + 1, 1);
+  for (int i = 1; i < L; ++i) {
+    if (bond_dims[i - 1] < 1) {
+      delete p;
+      return tn_set_error(ctx, TN_EINVAL, "tn_mps_create: bond %d < 1", i);
+    }
+    p->bond[i] = bond_dims[i - 1];
+    // the largest bond a gauge move or gate can produce: min(d^i, d^(L-i)), capped
+    double lg = std::min(i, L - i) * std::log((double)d);
+    int64_t clamp = lg > 40 ? (int64_t)1 << 40 : (int64_t)std::llround(std::pow((double)d, std::min(i, L - i)));
+    int64_t c = max_bond > 0 ? std::min(max_bond, clamp) : p->bond[i];
+    p->cap_bond[i] = std::max(c, p->bond[i]);
+  }
+  p->site.assign(L + 1, nullptr);
+  p->cap.assign(L + 1, 0);
+  for (int i = 1; i <= L; ++i) {
+    size_t e = (size_t)(p->cap_bond[i - 1] * d * p->cap_bond[i]);
+    tn_status_t st = ensure_site(p, i, e);
+    if (st != TN_OK) {
+      for (int j = 1; j <= L; ++j)
+        if (p->site[j]) tn_dev_free(ctx, p->site[j]);
+      delete p;
+      return st;
+    }
+    TN_CHECK_CUDA(ctx, cudaMemsetAsync(p->site[i], 0, e * sizeof(cxd), ctx->stream));
+  }
+  p->kind = TN_FORM_MIXED;
+  p->lo = 1;
+  p->hi = L;
+  *out = p;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_destroy(tn_mps* p) {
+  if (!p) return TN_OK;
+  tn_ctx* ctx = p->ctx;
+  cudaStreamSynchronize(ctx->stream);
+  for (int i = 1; i <= p->L; ++i)
+    if (p->site[i]) tn_dev_free(ctx, p->site[i]);
+  if (p->lam) tn_dev_free(ctx, p->lam);
+  if (p->gates) tn_dev_free(ctx, p->gates);
+  delete p;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_copy(const tn_mps* src, tn_mps** out) {
+  if (!src || !out) return TN_EINVAL;
+  tn_ctx* ctx = src->ctx;
+  std::vector<int64_t> b(src->bond.begin() + 1, src->bond.end() - 1);
+  tn_mps* p = nullptr;
+  TN_RETURN_IF(tn_mps_create(ctx, src->L, src->d, b.data(), 0, src->prec, &p));
+  for (int i = 1; i <= src->L; ++i) {
+    tn_status_t st = ensure_site(p, i, src->cap[i]);
+    if (st != TN_OK) {
+      tn_mps_destroy(p);
+      return st;
+    }
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], src->site[i], sizeof(cxd) * sz(src, i), cudaMemcpyDeviceToDevice,
+                                       ctx->stream));
+  }
+  p->cap_bond = src->cap_bond;
+  p->kind = src->kind;
+  p->lo = src->lo;
+  p->hi = src->hi;
+  if (src->lam_len > 0) {
+    TN_RETURN_IF(ensure_lam(p, src->lam_len));
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->lam, src->lam, sizeof(double) * src->lam_len, cudaMemcpyDeviceToDevice,
+                                       ctx->stream));
+    p->lam_len = src->lam_len;
+  }
+  *out = p;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_set_site(tn_mps* p, int32_t i, int64_t chl, int64_t chr, const void* h) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, i >= 1 && i <= p->L && h, "tn_mps_set_site: bad site");
+  TN_ARG(ctx, (i > 1 || chl == 1) && (i < p->L || chr == 1), "tn_mps_set_site: open-end bonds must be 1");
+  TN_ARG(ctx, chl == p->bond[i - 1] && chr == p->bond[i],
+         "tn_mps_set_site: bond dimensions differ from the MPS's (set them at creation)");
+  TN_RETURN_IF(ensure_site(p, i, (size_t)(chl * p->d * chr)));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], h, sizeof(cxd) * chl * p->d * chr, cudaMemcpyHostToDevice, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TN_OK;
+}
+
+tn_status_t tn_mps_get_site(const tn_mps* p, int32_t i, void* h) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, i >= 1 && i <= p->L && h, "tn_mps_get_site: bad site");
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h, p->site[i], sizeof(cxd) * sz(p, i), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TN_OK;
+}
+
+tn_status_t tn_mps_bond_dims(const tn_mps* p, int64_t* h) {
+  if (!p || !h) return TN_EINVAL;
+  for (int i = 1; i < p->L; ++i) h[i - 1] = p->bond[i];
+  return TN_OK;
+}
+
+tn_status_t tn_mps_set_precision(tn_mps* p, tn_precision_t prec) {
+  if (!p) return TN_EINVAL;
+  p->prec = prec;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_form(const tn_mps* p, int32_t* kind, int32_t* lo, int32_t* hi) {
+  if (!p || !kind || !lo || !hi) return TN_EINVAL;
+  *kind = p->kind;
+  *lo = p->lo;
+  *hi = p->hi;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_set_form(tn_mps* p, int32_t kind, int32_t lo, int32_t hi) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, kind == TN_FORM_NONCANONICAL || kind == TN_FORM_MIXED, "tn_mps_set_form: only NonCanonical or Mixed");
+  if (kind == TN_FORM_MIXED) TN_ARG(ctx, 1 <= lo && lo <= hi && hi <= p->L, "tn_mps_set_form: bad centre");
+  TN_ARG(ctx, p->kind != TN_FORM_BOND, "tn_mps_set_form: the MPS holds a Λ; canonize it to a mixed form first");
+  p->kind = kind;
+  p->lo = kind == TN_FORM_MIXED ? lo : 1;
+  p->hi = kind == TN_FORM_MIXED ? hi : p->L;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_get_lambda(const tn_mps* p, double* h, int64_t* len) {
+  if (!p || !len) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, p->kind == TN_FORM_BOND, "tn_mps_get_lambda: MPS is not bond-canonical");
+  *len = p->lam_len;
+  if (h && p->lam_len > 0) {
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h, p->lam, sizeof(double) * p->lam_len, cudaMemcpyDeviceToHost, ctx->stream));
+    TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return TN_OK;
+}
+
+tn_status_t tn_mps_canonize_mixed(tn_mps* p, int32_t lo, int32_t hi) {
+  if (!p) return TN_EINVAL;
+  TN_ARG(p->ctx, 1 <= lo && lo <= hi && hi <= p->L, "canonize: centre out of range");
+  return canonize_mixed(p, lo, hi);
+}
+
+tn_status_t tn_mps_canonize_bond(tn_mps* p, int32_t a) {
+  if (!p) return TN_EINVAL;
+  TN_ARG(p->ctx, 1 <= a && a < p->L, "canonize: bond out of range");
+  return canonize_bond(p, a);
+}
+
+tn_status_t tn_mps_compress(tn_mps* p, int32_t a, int64_t maxdim, double threshold) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  // compress.jl:30-32
+  TN_ARG(ctx, maxdim > 0 || threshold > 0, "Either `maxdim` or `threshold` must be specified");
+  TN_ARG(ctx, 0 <= a && a < p->L, "compress: bond out of range");
+  if (a == 0) {
+    for (int i = 1; i < p->L; ++i) TN_RETURN_IF(tn_mps_compress(p, i, maxdim, threshold));
+    return TN_OK;
+  }
+  TN_RETURN_IF(canonize_bond(p, a));
+  if (p->lam_len == 0) return TN_OK;  // size-1 bond: no Λ was produced
+  int64_t k = p->lam_len, r = 0;
+  TN_RETURN_IF(rank_select(ctx, p->lam, k, maxdim, threshold, &r));
+  if (r == k) return TN_OK;
+  // site a (χl d × k): keep the first r columns in place (column-major prefix)
+  // site a+1 (k × d χr): keep the first r rows
+  const int64_t n = p->d * p->bond[a + 1];
+  TN_RETURN_IF(ws_reserve(ctx, ws_round(sizeof(cxd) * (size_t)(r * n))));
+  cxd* tmp = ws_take<cxd>(ctx, (size_t)(r * n));
+  TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, p->site[a + 1], k, tmp, r));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[a + 1], tmp, sizeof(cxd) * r * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  p->bond[a] = r;
+  p->lam_len = r;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_simple_update(tn_mps* p, int32_t n_sites, int32_t a, const void* h_G, int64_t maxdim,
+                                 double threshold) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, h_G != nullptr, "simple_update: null gate");
+  TN_ARG(ctx, n_sites == 1 || n_sites == 2, "Operator must act on one or two sites");
+  TN_ARG(ctx, a >= 1 && a + n_sites - 1 <= p->L, "Operator plugs must be present in the MPS");
+  size_t ge = n_sites == 1 ? (size_t)(p->d * p->d) : (size_t)(p->d * p->d * p->d * p->d);
+  TN_RETURN_IF(upload_gates(p, h_G, ge));
+  TN_RETURN_IF(canonize_mixed(p, a, a + n_sites - 1));
+  if (n_sites == 1) return apply_gate1(p, a, p->gates);
+  return apply_gate2(p, a, p->gates, maxdim, threshold);
+}
+
+tn_status_t tn_mps_evolve_brickwork(tn_mps* p, int32_t n_layers, const int32_t* starts, const int32_t* n_gates,
+                                    const void* h_gates, int64_t maxdim, double threshold) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, n_layers >= 0 && starts && n_gates && h_gates, "evolve: bad arguments");
+  size_t total = 0;
+  const size_t g4 = (size_t)p->d * p->d * p->d * p->d;
+  for (int l = 0; l < n_layers; ++l) {
+    TN_ARG(ctx, n_gates[l] >= 0 && starts[l] >= 1 && starts[l] + 2 * n_gates[l] - 1 <= p->L, "evolve: layer out of range");
+    total += (size_t)n_gates[l] * g4;
+  }
+  if (total == 0) return TN_OK;
+  TN_RETURN_IF(upload_gates(p, h_gates, total));
+  size_t off = 0;
+  for (int l = 0; l < n_layers; ++l) {
+    for (int g = 0; g < n_gates[l]; ++g) {
+      int a = starts[l] + 2 * g;
+      TN_RETURN_IF(canonize_mixed(p, a, a + 1));
+      TN_RETURN_IF(apply_gate2(p, a, p->gates + off, maxdim, threshold));
+      off += g4;
+    }
+  }
+  return TN_OK;
+}
+
+tn_status_t tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* h_out) {
+  if (!a || !b || !h_out) return TN_EINVAL;
+  TN_ARG(a->ctx, a->L == b->L && a->d == b->d, "overlap: nsites differ");
+  TN_ARG(a->ctx, a->ctx == b->ctx, "overlap: MPS belong to different contexts");
+  TN_ARG(a->ctx, a->kind != TN_FORM_BOND && b->kind != TN_FORM_BOND,
+         "overlap: absorb Λ first (canonize the MPS to a mixed form)");
+  cxd v;
+  TN_RETURN_IF(overlap_impl(a, b, &v));
+  h_out[0] = v.x;
+  h_out[1] = v.y;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_norm(tn_mps* p, double* h_out) {
+  if (!p || !h_out) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  if (p->kind == TN_FORM_NONCANONICAL) {
+    p->kind = TN_FORM_MIXED;
+    p->lo = 1;
+    p->hi = p->L;
+  }
+  if (p->kind == TN_FORM_BOND) {
+    int64_t n = p->lam_len;
+    double ss = 0;
+    TN_RETURN_IF(tn_norm2(ctx, TN_F64, n, p->lam, &ss));
+    *h_out = ss;
+    return TN_OK;
+  }
+  const int c = p->lo;
+  TN_RETURN_IF(canonize_mixed(p, c, c));
+  return norm2_cxd(ctx, sz(p, c), p->site[c], h_out);
+}
+
+tn_status_t tn_mps_normalize(tn_mps* p) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  double nrm = 0;
+  TN_RETURN_IF(tn_mps_norm(p, &nrm));
+  TN_ARG(ctx, nrm > 0, "normalize: zero norm");
+  if (p->kind == TN_FORM_BOND) return tn_scale(ctx, TN_F64, p->lam_len, p->lam, 1.0 / nrm);
+  return tn_scale(ctx, TN_C64, sz(p, p->lo), p->site[p->lo], 1.0 / nrm);
+}
+
+tn_status_t tn_mps_amplitude(const tn_mps* p, const void* h_vectors, double* h_out) {
+  if (!p || !h_vectors || !h_out) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, p->kind != TN_FORM_BOND, "amplitude: absorb Λ first (canonize the MPS to a mixed form)");
+  const int L = p->L, d = p->d;
+  int64_t mx = 1;
+  for (int i = 0; i <= L; ++i) mx = std::max(mx, p->bond[i]);
+  TN_RETURN_IF(ws_reserve(ctx, 2 * ws_round(sizeof(cxd) * (size_t)(mx * d)) + ws_round(sizeof(cxd) * (size_t)(L * d))));
+  cxd* e = ws_take<cxd>(ctx, (size_t)(mx * d));
+  cxd* u = ws_take<cxd>(ctx, (size_t)(mx * d));
+  cxd* v = ws_take<cxd>(ctx, (size_t)(L * d));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(v, h_vectors, sizeof(cxd) * L * d, cudaMemcpyHostToDevice, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(e, &kOne, sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
+  for (int i = 1; i <= L; ++i) {
+    const int64_t xl = p->bond[i - 1], xr = p->bond[i];
+    // u (1 × d xr) = e (1 × xl) · A (xl × d xr)
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', 1, d * xr, xl, kOne, e, 1, 0, p->site[i], xl, 0, kZero, u, 1, 0, 1));
+    // e (1 × xr) = vᵀ (1 × d) · u as (d × xr)
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'T', 'N', 1, xr, d, kOne, v + (int64_t)(i - 1) * d, d, 0, u, d, 0, kZero, e, 1, 0, 1));
+  }
+  cxd* hp = reinterpret_cast<cxd*>(ctx->pinned);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, e, sizeof(cxd), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  h_out[0] = hp[0].x;
+  h_out[1] = hp[0].y;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_local_expectations(const tn_mps* p, const void* h_op, double* h_out) {
+  if (!p || !h_op || !h_out) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, p->kind != TN_FORM_BOND, "expectation: absorb Λ first (canonize the MPS to a mixed form)");
+  const int L = p->L, d = p->d;
+  int64_t mx = 1;
+  for (int i = 0; i <= L; ++i) mx = std::max(mx, p->bond[i]);
+  // left envs F_0..F_{L-1} and right envs R_2..R_{L+1}, each ≤ mx², plus scratch
+  const size_t env = (size_t)(mx * mx), t = (size_t)(mx * d * mx);
+  size_t need = 2 * (size_t)(L + 2) * ws_round(sizeof(cxd) * env) + 3 * ws_round(sizeof(cxd) * t) +
+                ws_round(sizeof(cxd) * (size_t)(d * d));
+  TN_RETURN_IF(ws_reserve(ctx, need));
+  std::vector<cxd*> F(L + 2), R(L + 2);
+  for (int i = 0; i <= L + 1; ++i) F[i] = ws_take<cxd>(ctx, env);
+  for (int i = 0; i <= L + 1; ++i) R[i] = ws_take<cxd>(ctx, env);
+  cxd* T1 = ws_take<cxd>(ctx, t);
+  cxd* T2 = ws_take<cxd>(ctx, t);
+  cxd* OA = ws_take<cxd>(ctx, t);
+  cxd* dO = ws_take<cxd>(ctx, (size_t)(d * d));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(dO, h_op, sizeof(cxd) * d * d, cudaMemcpyHostToDevice, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(F[0], &kOne, sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(R[L + 1], &kOne, sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
+  for (int i = 1; i < L; ++i) {
+    const int64_t x = p->bond[i - 1], x2 = p->bond[i];
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', x, d * x2, x, kOne, F[i - 1], x, 0, p->site[i], x, 0, kZero, T1, x, 0, 1));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', x2, x2, x * d, kOne, p->site[i], x * d, 0, T1, x * d, 0, kZero, F[i], x2,
+                                 0, 1));
+  }
+  for (int i = L; i > 1; --i) {
+    const int64_t x = p->bond[i - 1], x2 = p->bond[i];
+    // T1 (x d × x2) = A (x d × x2) · R_{i+1} (x2 × x2)
+    TN_RETURN_IF(
+        gemm_cx<double>(ctx, 'N', 'N', x * d, x2, x2, kOne, p->site[i], x * d, 0, R[i + 1], x2, 0, kZero, T1, x * d, 0, 1));
+    // R_i (x × x) = T1 as (x × d x2) · A as (x × d x2)ᴴ
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'C', x, x, d * x2, kOne, T1, x, 0, p->site[i], x, 0, kZero, R[i], x, 0, 1));
+  }
+  cxd nrm = {0, 0};
+  for (int i = 1; i <= L; ++i) {
+    const int64_t x = p->bond[i - 1], x2 = p->bond[i];
+    for (int pass = 0; pass < (i == 1 ? 2 : 1); ++pass) {
+      const cxd* Ain = p->site[i];
+      if (pass == 0) {
+        // OA[l, a, r] = Σ_b O[a, b] A[l, b, r]
+        TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', x, d, d, kOne, p->site[i], x, x * d, dO, d, 0, kZero, OA, x, x * d, x2));
+        Ain = OA;
+      }
+      TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', x, d * x2, x, kOne, F[i - 1], x, 0, Ain, x, 0, kZero, T1, x, 0, 1));
+      TN_RETURN_IF(
+          gemm_cx<double>(ctx, 'N', 'N', x * d, x2, x2, kOne, T1, x * d, 0, R[i + 1], x2, 0, kZero, T2, x * d, 0, 1));
+      cxd val;
+      TN_RETURN_IF(zdotc(ctx, x * d * x2, p->site[i], T2, &val));
+      if (pass == 0) {
+        h_out[2 * (i - 1)] = val.x;
+        h_out[2 * (i - 1) + 1] = val.y;
+      } else {
+        nrm = val;
+      }
+    }
+  }
+  // divide by ⟨ψ|ψ⟩
+  double nn = nrm.x * nrm.x + nrm.y * nrm.y;
+  for (int i = 0; i < L; ++i) {
+    double a = h_out[2 * i], b = h_out[2 * i + 1];
+    h_out[2 * i] = (a * nrm.x + b * nrm.y) / nn;
+    h_out[2 * i + 1] = (b * nrm.x - a * nrm.y) / nn;
+  }
+  return TN_OK;
+}
+
+}  // extern "C"

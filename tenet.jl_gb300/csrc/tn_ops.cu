@@ -1,0 +1,280 @@
+// K5 — small fused ops: Hadamard (Λ absorption), √S absorption into U / Vh, the
+// truncation-rank decision on the singular-value spectrum, FP64 norms.
+#include "tn_internal.cuh"
+
+namespace {
+
+template <typename E, typename R>
+__global__ void k_hadamard(int64_t total, int64_t inner, int64_t ext, const E* __restrict__ t,
+                           const double* __restrict__ s, E* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+    int64_t a = (i / inner) % ext;
+    out[i] = R::mul(t[i], s[a]);
+  }
+}
+struct MulR64 {
+  __device__ static double mul(double x, double s) { return x * s; }
+};
+struct MulR32 {
+  __device__ static float mul(float x, double s) { return (float)(x * s); }
+};
+struct MulC64 {
+  __device__ static double2 mul(double2 x, double s) { return make_double2(x.x * s, x.y * s); }
+};
+struct MulC32 {
+  __device__ static float2 mul(float2 x, double s) { return make_float2((float)(x.x * s), (float)(x.y * s)); }
+};
+
+// out(r, c) = X(r, c) * sqrt(S[c])   (rows × cols, ld in and out)
+template <typename T>
+__global__ void k_scale_cols_sqrt(cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t % rows, c = t / rows;
+    X[r + c * ld] = T(sqrt(S[c])) * X[r + c * ld];
+  }
+}
+template <typename T>
+__global__ void k_scale_rows_sqrt(cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t % rows, c = t / rows;
+    X[r + c * ld] = T(sqrt(S[r])) * X[r + c * ld];
+  }
+}
+
+// rank = #{ j < min(maxdim, k) : |S_j| > threshold }, at least 1 (S descending)
+__global__ void k_rank_select(const double* S, int64_t k, int64_t maxdim, double threshold, int* out) {
+  __shared__ int cnt;
+  if (threadIdx.x == 0) cnt = 0;
+  __syncthreads();
+  int64_t kk = (maxdim > 0 && maxdim < k) ? maxdim : k;
+  int local = 0;
+  for (int64_t j = threadIdx.x; j < kk; j += blockDim.x) local += (threshold <= 0.0 || fabs(S[j]) > threshold) ? 1 : 0;
+  atomicAdd(&cnt, local);
+  __syncthreads();
+  if (threadIdx.x == 0) out[0] = cnt > 0 ? cnt : 1;
+}
+
+template <typename E>
+__device__ __forceinline__ double nrm2_elem(E v);
+template <>
+__device__ __forceinline__ double nrm2_elem<double>(double v) {
+  return v * v;
+}
+template <>
+__device__ __forceinline__ double nrm2_elem<float>(float v) {
+  return (double)v * v;
+}
+template <>
+__device__ __forceinline__ double nrm2_elem<double2>(double2 v) {
+  return v.x * v.x + v.y * v.y;
+}
+template <>
+__device__ __forceinline__ double nrm2_elem<float2>(float2 v) {
+  return (double)v.x * v.x + (double)v.y * v.y;
+}
+
+// two-level deterministic reduction: fixed grid, per-block partials, then one block
+template <typename E>
+__global__ void k_sumsq_partial(int64_t n, const E* __restrict__ x, double* partial) {
+  __shared__ double red[32];
+  double s = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    s += nrm2_elem<E>(x[i]);
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) partial[blockIdx.x] = v;
+  }
+}
+__global__ void k_sum_final(int n, const double* partial, double* out) {
+  __shared__ double red[32];
+  double s = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += partial[i];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) out[0] = v;
+  }
+}
+
+template <typename E>
+__global__ void k_scale(int64_t n, E* x, double s);
+template <>
+__global__ void k_scale<double>(int64_t n, double* x, double s) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) x[i] *= s;
+}
+template <>
+__global__ void k_scale<float>(int64_t n, float* x, double s) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = (float)(x[i] * s);
+}
+template <>
+__global__ void k_scale<double2>(int64_t n, double2* x, double s) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i].x *= s;
+    x[i].y *= s;
+  }
+}
+template <>
+__global__ void k_scale<float2>(int64_t n, float2* x, double s) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i].x = (float)(x[i].x * s);
+    x[i].y = (float)(x[i].y * s);
+  }
+}
+
+__global__ void k_copy_matrix(int64_t rows, int64_t cols, const cxd* src, int64_t lds, cxd* dst, int64_t ldd) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t % rows, c = t / rows;
+    dst[r + c * ldd] = src[r + c * lds];
+  }
+}
+
+unsigned blocks_for(tn_ctx* ctx, int64_t n) {
+  int64_t b = (n + 255) / 256;
+  int64_t cap = (int64_t)ctx->num_sms * 8;
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+template <typename E>
+tn_status_t sumsq(tn_ctx* ctx, int64_t n, const E* x, double* h_out) {
+  int* flags = nullptr;
+  const int nb = 256;
+  TN_RETURN_IF(ctx_flags(ctx, 2 * (nb + 2), &flags));
+  double* partial = reinterpret_cast<double*>(flags);
+  k_sumsq_partial<E><<<nb, 256, 0, ctx->stream>>>(n, x, partial);
+  TN_LAUNCHED(ctx);
+  k_sum_final<<<1, 256, 0, ctx->stream>>>(nb, partial, partial + nb);
+  TN_LAUNCHED(ctx);
+  double* hp = reinterpret_cast<double*>(ctx->pinned);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, partial + nb, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *h_out = hp[0];
+  return TN_OK;
+}
+
+}  // namespace
+
+tn_status_t rank_select(tn_ctx* ctx, const double* S, int64_t k, int64_t maxdim, double threshold, int64_t* rank) {
+  int* flags = nullptr;
+  TN_RETURN_IF(ctx_flags(ctx, 4, &flags));
+  k_rank_select<<<1, 256, 0, ctx->stream>>>(S, k, maxdim, threshold, flags);
+  TN_LAUNCHED(ctx);
+  int* hp = reinterpret_cast<int*>(ctx->pinned);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *rank = hp[0];
+  return TN_OK;
+}
+
+template <typename T>
+tn_status_t scale_cols_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S) {
+  if (rows * cols == 0) return TN_OK;
+  k_scale_cols_sqrt<T><<<blocks_for(ctx, rows * cols), 256, 0, ctx->stream>>>(X, rows, cols, ld, S);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+template <typename T>
+tn_status_t scale_rows_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S) {
+  if (rows * cols == 0) return TN_OK;
+  k_scale_rows_sqrt<T><<<blocks_for(ctx, rows * cols), 256, 0, ctx->stream>>>(X, rows, cols, ld, S);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+template tn_status_t scale_cols_sqrt<double>(tn_ctx*, cxd*, int64_t, int64_t, int64_t, const double*);
+template tn_status_t scale_cols_sqrt<float>(tn_ctx*, cxf*, int64_t, int64_t, int64_t, const double*);
+template tn_status_t scale_rows_sqrt<double>(tn_ctx*, cxd*, int64_t, int64_t, int64_t, const double*);
+template tn_status_t scale_rows_sqrt<float>(tn_ctx*, cxf*, int64_t, int64_t, int64_t, const double*);
+
+tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out) {
+  double ss = 0;
+  TN_RETURN_IF(sumsq<double2>(ctx, n, reinterpret_cast<const double2*>(x), &ss));
+  *h_out = sqrt(ss);
+  return TN_OK;
+}
+
+tn_status_t copy_matrix_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src, int64_t lds, cxd* dst,
+                            int64_t ldd) {
+  if (rows * cols == 0) return TN_OK;
+  k_copy_matrix<<<blocks_for(ctx, rows * cols), 256, 0, ctx->stream>>>(rows, cols, src, lds, dst, ldd);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+extern "C" {
+
+tn_status_t tn_truncation_rank(tn_ctx* ctx, const double* S, int64_t k, int64_t maxdim, double threshold,
+                               int64_t* rank) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, S && rank && k > 0, "tn_truncation_rank: bad arguments");
+  return rank_select(ctx, S, k, maxdim, threshold, rank);
+}
+
+tn_status_t tn_hadamard(tn_ctx* ctx, tn_dtype_t dtype, int32_t rank, const int64_t* dims, int32_t axis,
+                        const void* t, const double* s, void* out) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, rank >= 1 && rank <= TN_MAX_RANK && axis >= 0 && axis < rank, "tn_hadamard: bad rank/axis");
+  TN_ARG(ctx, dims && t && s && out, "tn_hadamard: null pointer");
+  int64_t inner = 1, total = 1;
+  for (int i = 0; i < rank; ++i) {
+    TN_ARG(ctx, dims[i] >= 0, "tn_hadamard: negative extent");
+    if (i < axis) inner *= dims[i];
+    total *= dims[i];
+  }
+  if (total == 0) return TN_OK;
+  unsigned nb = blocks_for(ctx, total);
+  switch (dtype) {
+    case TN_F64: k_hadamard<double, MulR64><<<nb, 256, 0, ctx->stream>>>(total, inner, dims[axis], (const double*)t, s, (double*)out); break;
+    case TN_F32: k_hadamard<float, MulR32><<<nb, 256, 0, ctx->stream>>>(total, inner, dims[axis], (const float*)t, s, (float*)out); break;
+    case TN_C64: k_hadamard<double2, MulC64><<<nb, 256, 0, ctx->stream>>>(total, inner, dims[axis], (const double2*)t, s, (double2*)out); break;
+    case TN_C32: k_hadamard<float2, MulC32><<<nb, 256, 0, ctx->stream>>>(total, inner, dims[axis], (const float2*)t, s, (float2*)out); break;
+    default: return tn_set_error(ctx, TN_EINVAL, "tn_hadamard: bad dtype");
+  }
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+tn_status_t tn_norm2(tn_ctx* ctx, tn_dtype_t dtype, int64_t n, const void* x, double* h_out) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, n >= 0 && h_out && (n == 0 || x), "tn_norm2: bad arguments");
+  if (n == 0) {
+    *h_out = 0;
+    return TN_OK;
+  }
+  double ss = 0;
+  switch (dtype) {
+    case TN_F64: TN_RETURN_IF(sumsq<double>(ctx, n, (const double*)x, &ss)); break;
+    case TN_F32: TN_RETURN_IF(sumsq<float>(ctx, n, (const float*)x, &ss)); break;
+    case TN_C64: TN_RETURN_IF(sumsq<double2>(ctx, n, (const double2*)x, &ss)); break;
+    case TN_C32: TN_RETURN_IF(sumsq<float2>(ctx, n, (const float2*)x, &ss)); break;
+    default: return tn_set_error(ctx, TN_EINVAL, "tn_norm2: bad dtype");
+  }
+  *h_out = sqrt(ss);
+  return TN_OK;
+}
+
+tn_status_t tn_scale(tn_ctx* ctx, tn_dtype_t dtype, int64_t n, void* x, double s) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, n >= 0 && (n == 0 || x), "tn_scale: bad arguments");
+  if (n == 0) return TN_OK;
+  unsigned nb = blocks_for(ctx, n);
+  switch (dtype) {
+    case TN_F64: k_scale<double><<<nb, 256, 0, ctx->stream>>>(n, (double*)x, s); break;
+    case TN_F32: k_scale<float><<<nb, 256, 0, ctx->stream>>>(n, (float*)x, s); break;
+    case TN_C64: k_scale<double2><<<nb, 256, 0, ctx->stream>>>(n, (double2*)x, s); break;
+    case TN_C32: k_scale<float2><<<nb, 256, 0, ctx->stream>>>(n, (float2*)x, s); break;
+    default: return tn_set_error(ctx, TN_EINVAL, "tn_scale: bad dtype");
+  }
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+}  // extern "C"

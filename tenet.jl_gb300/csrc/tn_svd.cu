@@ -1,0 +1,684 @@
+// K4 — batched one-sided (Hestenes) Jacobi SVD, complex FP64 / FP32.
+//
+// Replaces LAPACK gesdd behind Muscle.tensor_svd_thin (src/Operations/canonize.jl:41,97)
+// and the SVD inside Muscle.simple_update (src/Operations/simple_update.jl:53-64).
+//
+// For A (m×n, m ≥ n) the columns of W = A are rotated pairwise until every pair is
+// orthogonal to tol = 4·√m·ε; then σ_j = ‖w_j‖, u_j = w_j/σ_j and V accumulates the
+// rotations.  Pairs follow the round-robin (circle) ordering, so one step touches n/2
+// disjoint pairs that run in parallel:
+//  * k_jacobi_step — one CTA per (pair, matrix): the three inner products ‖w_i‖²,
+//    ‖w_j‖², w_iᴴw_j are reduced with warp shuffles and a 4-warp shared-memory combine,
+//    then both columns of W and of V are rotated.  Columns stay in HBM/L2; a sweep is
+//    n−1 launches.  This is the large-matrix path (TEBD θ at χ=256 is 512×512).
+//  * k_jacobi_smem — one CTA per matrix with W and V resident in shared memory and all
+//    sweeps inside the kernel (warp per pair, shuffle reductions); the path for the
+//    many small bond matrices of batched canonisation.
+// Both stop on a sweep without rotations or at the sweep cap (status TN_ENOCONV).
+//
+// The complex 2×2 rotation: with γ = |γ|e^{iφ}, ζ = (β−α)/(2|γ|),
+// t = sgn(ζ)/(|ζ|+√(1+ζ²)), c = 1/√(1+t²), s = c·t:
+//   w_i' = c·w_i − s·e^{−iφ}·w_j,   w_j' = s·e^{iφ}·w_i + c·w_j.
+#include <algorithm>
+
+#include "tn_internal.cuh"
+
+namespace {
+
+constexpr int kMaxSweeps = 40;
+constexpr size_t kSmemMax = 200 * 1024;
+
+template <typename T>
+__host__ __device__ inline T jacobi_tol(int64_t m) {
+  const T eps = sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
+  return T(4) * sqrt(T(m > 1 ? m : 1)) * eps;
+}
+
+// circle method: players 0..N-1 (N even), round r in 0..N-2, pair k in 0..N/2-1
+__device__ __forceinline__ void rr_pair(int N, int r, int k, int& i, int& j) {
+  if (k == 0) {
+    i = r % (N - 1);
+    j = N - 1;
+  } else {
+    i = (r + k) % (N - 1);
+    j = (r - k + (N - 1)) % (N - 1);
+  }
+  if (i > j) {
+    int t = i;
+    i = j;
+    j = t;
+  }
+}
+
+template <typename T>
+struct Rot {
+  T c, s, t, ag;
+  cx<T> e;  // e^{iφ}
+  bool apply;
+};
+
+template <typename T>
+__device__ __forceinline__ Rot<T> make_rot(T alpha, T beta, cx<T> g, T tol) {
+  Rot<T> R;
+  T ag = sqrt(abs2(g));
+  R.apply = ag > tol * sqrt(alpha * beta) && ag > T(0);
+  if (!R.apply) {
+    R.c = 1;
+    R.s = 0;
+    R.e = mkcx<T>(1, 0);
+    return R;
+  }
+  T zeta = (beta - alpha) / (T(2) * ag);
+  T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+  R.c = T(1) / sqrt(T(1) + t * t);
+  R.s = R.c * t;
+  R.t = t;
+  R.ag = ag;
+  R.e = mkcx<T>(g.x / ag, g.y / ag);
+  return R;
+}
+
+template <typename T>
+__device__ __forceinline__ void rot_apply(const Rot<T>& R, cx<T>& wi, cx<T>& wj) {
+  // wi' = c wi − s conj(e) wj ; wj' = s e wi + c wj
+  cx<T> se = mkcx<T>(R.s * R.e.x, R.s * R.e.y);
+  cx<T> a = R.c * wi - conjg(se) * wj;
+  cx<T> b = se * wi + R.c * wj;
+  wi = a;
+  wj = b;
+}
+
+// Register-resident step: one CTA per (pair, matrix); each thread keeps its R rows of
+// both columns in registers from the load through the reduction to the rotation, so W is
+// read and written once per step.  EXACT: reduce ‖w_i‖², ‖w_j‖² too (FP32); otherwise
+// use the cached norms nrm[], updated analytically (α' = α − t|γ|, β' = β + t|γ|) and
+// recomputed exactly at the start of every sweep (FP64).  V may be null (no
+// accumulation: the caller recovers Vh from U and A).
+template <typename T, int NT, int R, bool EXACT>
+__global__ void __launch_bounds__(NT)
+    k_jacobi_step_reg(int64_t m, int64_t n, int N, int r, cx<T>* W, int64_t sW, cx<T>* V, int64_t sV, T* nrm,
+                      const int* active, int* rotated, T tol) {
+  const int64_t b = blockIdx.y;
+  if (!active[b]) return;
+  int i, j;
+  rr_pair(N, r, blockIdx.x, i, j);
+  if (j >= n) return;
+  cx<T>* wi = W + b * sW + (int64_t)i * m;
+  cx<T>* wj = W + b * sW + (int64_t)j * m;
+  constexpr int NW = NT / 32;
+  __shared__ T red[NW][4];
+  cx<T> x[R], y[R];
+  cx<T> g = mkcx<T>(0, 0);
+  T al = 0, be = 0;
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int64_t t = threadIdx.x + (int64_t)q * NT;
+    if (t < m) {
+      x[q] = wi[t];
+      y[q] = wj[t];
+      cfma_cj(g, x[q], y[q]);
+      if (EXACT) {
+        al += abs2(x[q]);
+        be += abs2(y[q]);
+      }
+    }
+  }
+  g.x = warp_sum(g.x);
+  g.y = warp_sum(g.y);
+  if (EXACT) {
+    al = warp_sum(al);
+    be = warp_sum(be);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    red[warp][0] = g.x;
+    red[warp][1] = g.y;
+    red[warp][2] = al;
+    red[warp][3] = be;
+  }
+  __syncthreads();
+  g = mkcx<T>(0, 0);
+  al = 0;
+  be = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    g.x += red[w][0];
+    g.y += red[w][1];
+    al += red[w][2];
+    be += red[w][3];
+  }
+  if (!EXACT) {
+    al = nrm[b * n + i];
+    be = nrm[b * n + j];
+  }
+  Rot<T> Rt = make_rot(al, be, g, tol);
+  if (!Rt.apply) return;
+  if (threadIdx.x == 0) {
+    rotated[b] = 1;
+    nrm[b * n + i] = al - Rt.t * Rt.ag;
+    nrm[b * n + j] = be + Rt.t * Rt.ag;
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) {
+    const int64_t t = threadIdx.x + (int64_t)q * NT;
+    if (t < m) {
+      rot_apply(Rt, x[q], y[q]);
+      wi[t] = x[q];
+      wj[t] = y[q];
+    }
+  }
+  if (V) {
+    cx<T>* vi = V + b * sV + (int64_t)i * n;
+    cx<T>* vj = V + b * sV + (int64_t)j * n;
+    for (int64_t t = threadIdx.x; t < n; t += NT) {
+      cx<T> a = vi[t], c = vj[t];
+      rot_apply(Rt, a, c);
+      vi[t] = a;
+      vj[t] = c;
+    }
+  }
+}
+
+// nrm[b][c] = ‖w_c‖² (one warp per column)
+template <typename T>
+__global__ void k_col_norms(int64_t m, int64_t n, const cx<T>* W, int64_t sW, T* nrm, int64_t batch) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t col = gw; col < n * batch; col += nw) {
+    const int64_t b = col / n, c = col % n;
+    const cx<T>* w = W + b * sW + c * m;
+    T s = 0;
+    for (int64_t t = lane; t < m; t += 32) s += abs2(w[t]);
+    s = warp_sum(s);
+    if (lane == 0) nrm[col] = s;
+  }
+}
+
+// whole SVD of one matrix per CTA in shared memory (W m×n and V n×n resident)
+template <typename T>
+__global__ void __launch_bounds__(512)
+    k_jacobi_smem(int64_t m, int64_t n, cx<T>* W, int64_t sW, cx<T>* V, int64_t sV, int* status, T tol,
+                  int max_sweeps, bool v_given) {
+  extern __shared__ unsigned char smem_raw[];
+  cx<T>* sw = reinterpret_cast<cx<T>*>(smem_raw);
+  cx<T>* sv = sw + m * n;
+  __shared__ int s_rot;
+  const int64_t b = blockIdx.x;
+  cx<T>* Wb = W + b * sW;
+  cx<T>* Vb = V + b * sV;
+  for (int64_t t = threadIdx.x; t < m * n; t += blockDim.x) sw[t] = Wb[t];
+  for (int64_t t = threadIdx.x; t < n * n; t += blockDim.x) {
+    int64_t r = t % n, c = t / n;
+    sv[t] = v_given ? Vb[t] : mkcx<T>(r == c ? T(1) : T(0), 0);
+  }
+  __syncthreads();
+  const int N = (int)(n + (n & 1));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
+    for (int r = 0; r < N - 1; ++r) {
+      for (int k = warp; k < N / 2; k += nwarps) {
+        int i, j;
+        rr_pair(N, r, k, i, j);
+        if (j >= n) continue;
+        cx<T>* wi = sw + (int64_t)i * m;
+        cx<T>* wj = sw + (int64_t)j * m;
+        T al = 0, be = 0;
+        cx<T> g = mkcx<T>(0, 0);
+        for (int64_t t = lane; t < m; t += 32) {
+          cx<T> x = wi[t], y = wj[t];
+          al += abs2(x);
+          be += abs2(y);
+          cfma_cj(g, x, y);
+        }
+        al = warp_sum(al);
+        be = warp_sum(be);
+        g.x = warp_sum(g.x);
+        g.y = warp_sum(g.y);
+        Rot<T> R = make_rot(al, be, g, tol);
+        if (!R.apply) continue;
+        if (lane == 0) s_rot = 1;
+        for (int64_t t = lane; t < m; t += 32) {
+          cx<T> x = wi[t], y = wj[t];
+          rot_apply(R, x, y);
+          wi[t] = x;
+          wj[t] = y;
+        }
+        cx<T>* vi = sv + (int64_t)i * n;
+        cx<T>* vj = sv + (int64_t)j * n;
+        for (int64_t t = lane; t < n; t += 32) {
+          cx<T> x = vi[t], y = vj[t];
+          rot_apply(R, x, y);
+          vi[t] = x;
+          vj[t] = y;
+        }
+      }
+      __syncthreads();
+    }
+    int any = s_rot;
+    __syncthreads();
+    if (!any) break;
+  }
+  for (int64_t t = threadIdx.x; t < m * n; t += blockDim.x) Wb[t] = sw[t];
+  for (int64_t t = threadIdx.x; t < n * n; t += blockDim.x) Vb[t] = sv[t];
+  if (threadIdx.x == 0) status[b] = sweep >= max_sweeps ? 1 : 0;
+}
+
+template <typename T>
+__global__ void k_identity(int64_t n, cx<T>* V, int64_t sV, int64_t batch) {
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+      int64_t r = t % n, c = t / n;
+      V[b * sV + t] = mkcx<T>(r == c ? T(1) : T(0), 0);
+    }
+}
+
+template <typename T>
+__global__ void k_copy_mat(int64_t m, int64_t n, const cx<T>* A, int64_t lda, int64_t sA, cx<T>* W, int64_t sW,
+                           int64_t batch) {
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x) {
+      int64_t r = t % m, c = t / m;
+      W[b * sW + t] = A[b * sA + r + c * lda];
+    }
+}
+
+// σ_j = ‖w_j‖ (FP64), then a descending order by a per-matrix bitonic sort in shared
+// memory; order[b][j] = source column of the j-th largest σ.
+template <typename T>
+__global__ void __launch_bounds__(512)
+    k_svd_order(int64_t m, int64_t n, const cx<T>* W, int64_t sW, double* S, int64_t sS, int* order) {
+  extern __shared__ unsigned char smem_raw[];
+  const int64_t b = blockIdx.x;
+  int P2 = 1;
+  while (P2 < n) P2 <<= 1;
+  double* key = reinterpret_cast<double*>(smem_raw);
+  int* idx = reinterpret_cast<int*>(key + P2);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  for (int64_t c = warp; c < P2; c += nwarps) {
+    double s2 = 0;
+    if (c < n) {
+      const cx<T>* w = W + b * sW + c * m;
+      for (int64_t t = lane; t < m; t += 32) s2 += (double)abs2(w[t]);
+      s2 = warp_sum(s2);
+    }
+    if (lane == 0) {
+      key[c] = c < n ? sqrt(s2) : -1.0;
+      idx[c] = (int)c;
+    }
+  }
+  __syncthreads();
+  // bitonic sort, descending by key, ties by index ascending
+  for (int size = 2; size <= P2; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int t = threadIdx.x; t < P2; t += blockDim.x) {
+        int p = t ^ stride;
+        if (p > t) {
+          bool desc = (t & size) == 0;
+          double kt = key[t], kp = key[p];
+          int it = idx[t], ip = idx[p];
+          bool t_first = kt > kp || (kt == kp && it < ip);
+          if (desc != t_first) {
+            key[t] = kp;
+            key[p] = kt;
+            idx[t] = ip;
+            idx[p] = it;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = threadIdx.x; t < n; t += blockDim.x) {
+    S[b * sS + t] = key[t];
+    order[b * n + t] = idx[t];
+  }
+}
+
+// U(:, j) = W(:, order_j) / σ_j ; Vout(:, j) = V(:, order_j)  (as Vh = Vᴴ when vh)
+template <typename T>
+__global__ void k_svd_gather(int64_t m, int64_t n, const cx<T>* W, int64_t sW, const cx<T>* V, int64_t sV,
+                             const double* S, int64_t sS, const int* order, cx<T>* U, int64_t sU, cx<T>* Vo,
+                             int64_t sVo, bool vh, int64_t batch) {
+  const int64_t b = blockIdx.y;
+  if (b >= batch) return;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < m * n; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t % m, c = t / m;
+    int src = order[b * n + c];
+    double s = S[b * sS + c];
+    T inv = s > 0 ? T(1.0 / s) : T(0);
+    U[b * sU + t] = inv * W[b * sW + r + (int64_t)src * m];
+  }
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t % n, c = t / n;
+    int src = order[b * n + c];
+    cx<T> v = V[b * sV + r + (int64_t)src * n];
+    if (vh)
+      Vo[b * sVo + c + r * n] = conjg(v);  // Vh(c, r) = conj(V(r, c))
+    else
+      Vo[b * sVo + t] = v;
+  }
+}
+
+}  // namespace
+
+template <typename T>
+size_t svd_workspace(int64_t m, int64_t n, int64_t batch) {
+  return ws_round(sizeof(cx<T>) * (size_t)(m * n * batch)) + ws_round(sizeof(cx<T>) * (size_t)(n * n * batch)) +
+         ws_round(sizeof(int) * (size_t)(n * batch)) + 2 * ws_round(sizeof(int) * (size_t)(batch + 1)) +
+         ws_round(sizeof(T) * (size_t)(n * batch));
+}
+template size_t svd_workspace<double>(int64_t, int64_t, int64_t);
+template size_t svd_workspace<float>(int64_t, int64_t, int64_t);
+
+// one round-robin step of the register kernel, instantiated by row count
+template <typename T>
+static tn_status_t launch_step(tn_ctx* ctx, int64_t m, int64_t n, int N, int r, cx<T>* W, cx<T>* V, T* nrm,
+                               const int* active, int* rotated, T tol, unsigned gy) {
+  constexpr bool EX = sizeof(T) == 4;
+  const dim3 grid(N / 2, gy);
+  const int64_t sW = m * n, sV = n * n;
+  if (m <= 512)
+    k_jacobi_step_reg<T, 128, 4, EX><<<grid, 128, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol);
+  else if (m <= 1024)
+    k_jacobi_step_reg<T, 256, 4, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol);
+  else if (m <= 2048)
+    k_jacobi_step_reg<T, 256, 8, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol);
+  else if (m <= 4096)
+    k_jacobi_step_reg<T, 256, 16, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol);
+  else
+    return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: more than 4096 rows");
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+// Jacobi sweeps on W (m×n dense, batch stride m·n) accumulating into V (n×n dense; may
+// be null on the large-matrix path).  V is set to the identity first unless v_given.
+// nrm: n·batch reals of workspace.  The n−1 steps of a sweep (plus the flag reset and the
+// norm refresh) are captured once into a CUDA graph, cached on the context by shape and
+// buffer addresses, and replayed per sweep; the host reads one flag word per matrix
+// after each sweep to stop converged matrices.
+template <typename T>
+static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T>* V, int64_t batch, bool v_given,
+                               int* active, int* rotated, T* nrm, int max_sweeps, int* sweeps_out, bool* noconv_out) {
+  const unsigned gy = (unsigned)batch;
+  const T tol = jacobi_tol<T>(m);
+  int sweeps = 0;
+  bool noconv = false;
+  const size_t smem_need = sizeof(cx<T>) * (size_t)(m * n + n * n);
+  if (V && smem_need <= kSmemMax && n <= 256) {
+    TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_jacobi_smem<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+    int threads = n >= 32 ? 512 : 128;
+    k_jacobi_smem<T><<<gy, threads, smem_need, ctx->stream>>>(m, n, W, m * n, V, n * n, rotated, tol, max_sweeps,
+                                                              v_given);
+    TN_LAUNCHED(ctx);
+    std::vector<int> st(batch);
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(st.data(), rotated, sizeof(int) * batch, cudaMemcpyDeviceToHost, ctx->stream));
+    TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    for (int64_t b = 0; b < batch; ++b) noconv |= st[b] != 0;
+    sweeps = -1;
+  } else {
+    if (V && !v_given) {
+      int64_t blocks = std::min<int64_t>((n * n + 255) / 256, 2048);
+      k_identity<T><<<dim3((unsigned)blocks, gy), 256, 0, ctx->stream>>>(n, V, n * n, batch);
+      TN_LAUNCHED(ctx);
+    }
+    std::vector<int> h_act(batch, 1), h_rot(batch);
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
+    const int N = (int)(n + (n & 1));
+    // graph for one sweep
+    char key[256];
+    snprintf(key, sizeof(key), "jac%zu:%lld:%lld:%lld:%p:%p:%p:%p:%p", sizeof(T), (long long)m, (long long)n,
+             (long long)batch, (void*)W, (void*)V, (void*)nrm, (void*)active, (void*)rotated);
+    cudaGraphExec_t ge = nullptr;
+    auto it = ctx->graphs.find(key);
+    if (it != ctx->graphs.end()) {
+      ge = it->second;
+    } else {
+      if (ctx->graphs.size() > 256) {
+        for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
+        ctx->graphs.clear();
+      }
+      cudaGraph_t g = nullptr;
+      TN_CHECK_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      cudaMemsetAsync(rotated, 0, sizeof(int) * batch, ctx->stream);
+      int64_t nb = std::min<int64_t>((n * batch * 32 + 255) / 256, (int64_t)ctx->num_sms * 8);
+      k_col_norms<T><<<(unsigned)std::max<int64_t>(nb, 1), 256, 0, ctx->stream>>>(m, n, W, m * n, nrm, batch);
+      tn_status_t st = TN_OK;
+      for (int r = 0; r < N - 1 && st == TN_OK; ++r) st = launch_step<T>(ctx, m, n, N, r, W, V, nrm, active, rotated, tol, gy);
+      cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+      if (st != TN_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+      }
+      if (e != cudaSuccess) return tn_set_error(ctx, TN_ECUDA, "svd graph capture: %s", cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&ge, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return tn_set_error(ctx, TN_ECUDA, "svd graph instantiate: %s", cudaGetErrorString(e));
+      ctx->graphs[key] = ge;
+      ctx->launches -= (N - 1);  // counted again per replay below
+    }
+    int n_active = (int)batch;
+    for (sweeps = 0; sweeps < max_sweeps && n_active > 0; ++sweeps) {
+      TN_CHECK_CUDA(ctx, cudaGraphLaunch(ge, ctx->stream));
+      ctx->launches += N;  // norm refresh + N-1 steps
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * batch, cudaMemcpyDeviceToHost, ctx->stream));
+      TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      n_active = 0;
+      for (int64_t b = 0; b < batch; ++b) {
+        h_act[b] = h_act[b] && h_rot[b];
+        n_active += h_act[b];
+      }
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    noconv = n_active > 0;
+  }
+  if (sweeps_out) *sweeps_out = sweeps;
+  if (noconv_out) *noconv_out = noconv;
+  return TN_OK;
+}
+
+// σ, ordering, U = W/σ, V (or Vh) from converged W, V
+template <typename T>
+static tn_status_t jacobi_finalize(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* W, const cx<T>* V, int* order,
+                                   cx<T>* U, int64_t sU, double* S, int64_t sS, cx<T>* Vo, int64_t sVo, bool vh,
+                                   int64_t batch) {
+  const unsigned gy = (unsigned)batch;
+  int P2 = 1;
+  while (P2 < n) P2 <<= 1;
+  size_t smem = (sizeof(double) + sizeof(int)) * (size_t)P2;
+  if (smem > kSmemMax) return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: n too large for the sort");
+  TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_svd_order<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+  k_svd_order<T><<<gy, 512, smem, ctx->stream>>>(m, n, W, m * n, S, sS, order);
+  TN_LAUNCHED(ctx);
+  int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 1024);
+  k_svd_gather<T><<<dim3((unsigned)blocks, gy), 256, 0, ctx->stream>>>(m, n, W, m * n, V, n * n, S, sS, order, U, sU,
+                                                                        Vo, sVo, vh, batch);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+// U: m×n, S: n (FP64), Vo: V (n×n) or Vh when vh; workspace reserved by the caller
+template <typename T>
+static tn_status_t svd_tall_impl(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda, int64_t sA,
+                                 cx<T>* U, int64_t sU, double* S, int64_t sS, cx<T>* Vo, int64_t sVo, bool vh,
+                                 int64_t batch, int* sweeps_out) {
+  if (m < n) return tn_set_error(ctx, TN_EINVAL, "svd_tall: m < n");
+  if (n == 0 || batch == 0) return TN_OK;
+  if (batch > 65535) return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: batch > 65535");
+  cx<T>* W = ws_take<cx<T>>(ctx, (size_t)(m * n * batch));
+  cx<T>* V = ws_take<cx<T>>(ctx, (size_t)(n * n * batch));
+  int* order = ws_take<int>(ctx, (size_t)(n * batch));
+  int* active = ws_take<int>(ctx, (size_t)(batch + 1));
+  int* rotated = ws_take<int>(ctx, (size_t)(batch + 1));
+  T* nrm = ws_take<T>(ctx, (size_t)(n * batch));
+  {
+    int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
+    k_copy_mat<T><<<dim3((unsigned)blocks, (unsigned)batch), 256, 0, ctx->stream>>>(m, n, A, lda, sA, W, m * n, batch);
+    TN_LAUNCHED(ctx);
+  }
+  bool noconv = false;
+  TN_RETURN_IF(jacobi_core<T>(ctx, m, n, W, V, batch, false, active, rotated, nrm, kMaxSweeps, sweeps_out, &noconv));
+  TN_RETURN_IF(jacobi_finalize<T>(ctx, m, n, W, V, order, U, sU, S, sS, Vo, sVo, vh, batch));
+  if (noconv) return tn_set_error(ctx, TN_ENOCONV, "Jacobi SVD did not converge within %d sweeps", kMaxSweeps);
+  return TN_OK;
+}
+
+template <typename T>
+tn_status_t svd_tall_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda, int64_t sA, cx<T>* U,
+                        int64_t sU, double* S, int64_t sS, cx<T>* V, int64_t sV, int64_t batch, int* sweeps_out) {
+  return svd_tall_impl<T>(ctx, m, n, A, lda, sA, U, sU, S, sS, V, sV, false, batch, sweeps_out);
+}
+template tn_status_t svd_tall_cx<double>(tn_ctx*, int64_t, int64_t, const cxd*, int64_t, int64_t, cxd*, int64_t,
+                                         double*, int64_t, cxd*, int64_t, int64_t, int*);
+template tn_status_t svd_tall_cx<float>(tn_ctx*, int64_t, int64_t, const cxf*, int64_t, int64_t, cxf*, int64_t,
+                                        double*, int64_t, cxf*, int64_t, int64_t, int*);
+
+// ---------------------------------------------------------------------------------
+// mixed precision (C64 data): the Jacobi sweeps run first in FP32 — on GB300 the FP32
+// pipe is ~64× the FP64 pipe — until the columns are orthogonal to FP32 accuracy.  The
+// FP32 rotations V32 are lifted to FP64, re-orthonormalised by two Newton–Schulz steps
+// V ← V (3I − VᴴV)/2, and W = A·V is formed in FP64; the FP64 Jacobi sweeps then only
+// remove the O(1e-6) residual (quadratic convergence: 2–3 sweeps instead of ~9).
+// Rotations, σ and the truncation decision stay FP64.
+// ---------------------------------------------------------------------------------
+__global__ void k_d2f(int64_t count, const cxd* __restrict__ a, int64_t lda, int64_t rows, cxf* __restrict__ b) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t % rows, c = t / rows;
+    cxd v = a[r + c * lda];
+    b[t] = mkcx<float>((float)v.x, (float)v.y);
+  }
+}
+__global__ void k_f2d(int64_t count, const cxf* __restrict__ a, cxd* __restrict__ b) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+    cxf v = a[t];
+    b[t] = mkcx<double>(v.x, v.y);
+  }
+}
+
+size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
+  size_t s = 0;
+  s += ws_round(sizeof(cxf) * (size_t)(m * n * batch));      // W32
+  s += ws_round(sizeof(cxf) * (size_t)(n * n * batch));      // V32
+  s += ws_round(sizeof(cxd) * (size_t)(m * n * batch));      // W64
+  s += 2 * ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // V64, G
+  s += ws_round(sizeof(int) * (size_t)(n * batch));
+  s += 2 * ws_round(sizeof(int) * (size_t)(batch + 1));
+  s += ws_round(sizeof(double) * (size_t)(n * batch)) + ws_round(sizeof(float) * (size_t)(n * batch));
+  return s;
+}
+
+tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int64_t lda, int64_t sA, cxd* U,
+                           int64_t sU, double* S, int64_t sS, cxd* V, int64_t sV, int64_t batch) {
+  if (m < n) return tn_set_error(ctx, TN_EINVAL, "svd_tall_mixed: m < n");
+  if (n == 0 || batch == 0) return TN_OK;
+  if (batch > 65535) return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: batch > 65535");
+  cxf* W32 = ws_take<cxf>(ctx, (size_t)(m * n * batch));
+  cxf* V32 = ws_take<cxf>(ctx, (size_t)(n * n * batch));
+  cxd* W64 = ws_take<cxd>(ctx, (size_t)(m * n * batch));
+  cxd* V64 = ws_take<cxd>(ctx, (size_t)(n * n * batch));
+  cxd* G = ws_take<cxd>(ctx, (size_t)(n * n * batch));
+  int* order = ws_take<int>(ctx, (size_t)(n * batch));
+  int* active = ws_take<int>(ctx, (size_t)(batch + 1));
+  int* rotated = ws_take<int>(ctx, (size_t)(batch + 1));
+  double* nrm64 = ws_take<double>(ctx, (size_t)(n * batch));
+  float* nrm32 = ws_take<float>(ctx, (size_t)(n * batch));
+  for (int64_t b = 0; b < batch; ++b) {
+    int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
+    k_d2f<<<(unsigned)blocks, 256, 0, ctx->stream>>>(m * n, A + b * sA, lda, m, W32 + b * m * n);
+    TN_LAUNCHED(ctx);
+  }
+  bool noconv = false;
+  TN_RETURN_IF(jacobi_core<float>(ctx, m, n, W32, V32, batch, false, active, rotated, nrm32, kMaxSweeps, nullptr, &noconv));
+  {
+    int64_t cnt = n * n * batch;
+    int64_t blocks = std::min<int64_t>((cnt + 255) / 256, 4096);
+    k_f2d<<<(unsigned)blocks, 256, 0, ctx->stream>>>(cnt, V32, V64);
+    TN_LAUNCHED(ctx);
+  }
+  // Two Newton–Schulz steps  G = VᴴV ; V ← 1.5 V − 0.5 V G  (unitarity error e → 1.5e²:
+  // FP32's ~1e-5 reaches the FP64 floor after two), ping-ponging between V64 and V
+  for (int it = 0; it < 2; ++it) {
+    cxd* src = it == 0 ? V64 : V;
+    cxd* dst = it == 0 ? V : V64;
+    const int64_t s_src = it == 0 ? n * n : sV, s_dst = it == 0 ? sV : n * n;
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', n, n, n, mkcx(1.0, 0.0), src, n, s_src, src, n, s_src, mkcx(0.0, 0.0),
+                                 G, n, n * n, batch));
+    for (int64_t b = 0; b < batch; ++b)
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(dst + b * s_dst, src + b * s_src, sizeof(cxd) * n * n,
+                                         cudaMemcpyDeviceToDevice, ctx->stream));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', n, n, n, mkcx(-0.5, 0.0), src, n, s_src, G, n, n * n, mkcx(1.5, 0.0),
+                                 dst, n, s_dst, batch));
+  }
+  // W = A V  (FP64)
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, n, mkcx(1.0, 0.0), A, lda, sA, V64, n, n * n, mkcx(0.0, 0.0), W64,
+                               m, m * n, batch));
+  TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W64, V64, batch, true, active, rotated, nrm64, kMaxSweeps, nullptr, &noconv));
+  TN_RETURN_IF(jacobi_finalize<double>(ctx, m, n, W64, V64, order, U, sU, S, sS, V, sV, false, batch));
+  if (noconv) return tn_set_error(ctx, TN_ENOCONV, "Jacobi SVD did not converge within %d sweeps", kMaxSweeps);
+  return TN_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// any-shape thin SVD: U m×k, S k, Vh k×n
+// ---------------------------------------------------------------------------------
+size_t svd_any_workspace(tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n, int64_t batch) {
+  const int64_t mm = m >= n ? m : n, nn = m >= n ? n : m;
+  const size_t es = dt == TN_C64 ? 16 : 8;
+  const bool mixed = dt == TN_C64 && prec == TN_PREC_MIXED;
+  size_t core = mixed ? svd_mixed_workspace(mm, nn, batch)
+                      : (dt == TN_C64 ? svd_workspace<double>(mm, nn, batch) : svd_workspace<float>(mm, nn, batch));
+  if (m >= n) return core + (mixed ? ws_round(es * (size_t)(n * n * batch)) : 0);
+  return core + 2 * ws_round(es * (size_t)(m * n * batch));
+}
+
+template <typename T>
+static tn_status_t svd_any_t(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_t n, const cx<T>* A, int64_t lda,
+                             int64_t sA, cx<T>* U, int64_t sU, double* S, int64_t sS, cx<T>* Vh, int64_t sVh,
+                             int64_t batch) {
+  const bool mixed = prec == TN_PREC_MIXED && sizeof(T) == 8;
+  if (m >= n) {
+    if (mixed) {
+      // V (n×n) into Vh then conjugate-transpose in place via a temporary
+      cx<T>* Vt = ws_take<cx<T>>(ctx, (size_t)(n * n * batch));
+      TN_RETURN_IF(svd_tall_mixed(ctx, m, n, (const cxd*)A, lda, sA, (cxd*)U, sU, S, sS, (cxd*)Vt, n * n, batch));
+      return transpose_cx<T>(ctx, n, n, Vt, n, n * n, Vh, n, sVh, batch, true);
+    }
+    return svd_tall_impl<T>(ctx, m, n, A, lda, sA, U, sU, S, sS, Vh, sVh, true, batch, nullptr);
+  }
+  // A = (Aᴴ)ᴴ:  Aᴴ (n×m) = U' S V'ᴴ  ⇒  U = V' (m×m), Vh = U'ᴴ (m×n)
+  cx<T>* B = ws_take<cx<T>>(ctx, (size_t)(m * n * batch));
+  TN_RETURN_IF(transpose_cx<T>(ctx, m, n, A, lda, sA, B, n, m * n, batch, true));
+  cx<T>* Up = ws_take<cx<T>>(ctx, (size_t)(n * m * batch));  // U' (n×m)
+  if (mixed) {
+    TN_RETURN_IF(svd_tall_mixed(ctx, n, m, (const cxd*)B, n, m * n, (cxd*)Up, n * m, S, sS, (cxd*)U, sU, batch));
+  } else {
+    TN_RETURN_IF(svd_tall_impl<T>(ctx, n, m, B, n, m * n, Up, n * m, S, sS, U, sU, false, batch, nullptr));
+  }
+  return transpose_cx<T>(ctx, n, m, Up, n, n * m, Vh, m, sVh, batch, true);
+}
+
+tn_status_t svd_any(tn_ctx* ctx, tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n, const void* A,
+                    int64_t lda, int64_t sA, void* U, int64_t sU, double* S, int64_t sS, void* Vh, int64_t sVh,
+                    int64_t batch) {
+  if (dt == TN_C64)
+    return svd_any_t<double>(ctx, prec, m, n, (const cxd*)A, lda, sA, (cxd*)U, sU, S, sS, (cxd*)Vh, sVh, batch);
+  if (dt == TN_C32)
+    return svd_any_t<float>(ctx, prec, m, n, (const cxf*)A, lda, sA, (cxf*)U, sU, S, sS, (cxf*)Vh, sVh, batch);
+  return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: only C64 and C32 are implemented");
+}
+
+extern "C" tn_status_t tn_svd_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int64_t m, int64_t n,
+                                   const void* A, int64_t lda, int64_t strideA, void* U, int64_t strideU, double* S,
+                                   int64_t strideS, void* Vh, int64_t strideVh, int64_t batch) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, m >= 0 && n >= 0 && batch >= 0, "tn_svd_thin: negative size");
+  TN_ARG(ctx, lda >= (m > 1 ? m : 1), "tn_svd_thin: lda < m");
+  TN_ARG(ctx, (m == 0 || n == 0 || batch == 0) || (A && U && S && Vh), "tn_svd_thin: null pointer");
+  TN_ARG(ctx, dtype == TN_C64 || dtype == TN_C32, "tn_svd_thin: only C64 and C32 are implemented");
+  TN_RETURN_IF(ws_reserve(ctx, svd_any_workspace(dtype, prec, m, n, batch)));
+  return svd_any(ctx, dtype, prec, m, n, A, lda, strideA, U, strideU, S, strideS, Vh, strideVh, batch);
+}

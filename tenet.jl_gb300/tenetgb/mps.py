@@ -1,0 +1,356 @@
+"""Device-resident MPS with Tenet's MPS API (src/Components/MPS.jl, src/Operations/*).
+
+Julia's in-place ``f!`` maps to ``f_`` here (``canonize_``, ``compress_``,
+``simple_update_``, ``normalize_``); the non-mutating forms copy first, as Tenet's
+``canonize(tn, …) = canonize!(copy(tn), …)`` does (src/Operations/canonize.jl:13).
+
+The sites stay in HBM inside a native ``tn_mps`` handle; the canonical-form trait
+(src/CanonicalForm.jl) is tracked in native code and mirrored by the form classes below.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from .core import Context, default_context, precision_code
+
+
+class NonCanonical:
+    def __eq__(self, o):
+        return isinstance(o, NonCanonical)
+
+    def __repr__(self):
+        return "NonCanonical()"
+
+
+class MixedCanonical:
+    """MixedCanonical(orthog_center): sites lo..hi (1-based)."""
+
+    def __init__(self, sites):
+        if isinstance(sites, (int, np.integer)):
+            sites = [int(sites)]
+        self.sites = sorted(set(int(s) for s in sites))
+
+    @property
+    def lo(self):
+        return self.sites[0]
+
+    @property
+    def hi(self):
+        return self.sites[-1]
+
+    def __eq__(self, o):
+        return isinstance(o, MixedCanonical) and (o.lo, o.hi) == (self.lo, self.hi)
+
+    def __repr__(self):
+        return f"MixedCanonical({self.sites})"
+
+
+class BondCanonical:
+    """BondCanonical(bond"a-b") with b = a + 1; Λ stored at LambdaSite(bond)."""
+
+    def __init__(self, a, b=None):
+        if b is None:
+            a, b = a
+        self.a, self.b = min(a, b), max(a, b)
+
+    def __eq__(self, o):
+        return isinstance(o, BondCanonical) and (o.a, o.b) == (self.a, self.b)
+
+    def __repr__(self):
+        return f"BondCanonical({self.a}-{self.b})"
+
+
+def _as_form(f):
+    if isinstance(f, (NonCanonical, MixedCanonical, BondCanonical)):
+        return f
+    if isinstance(f, (int, np.integer, list)):
+        return MixedCanonical(f)
+    if isinstance(f, tuple) and len(f) == 2:
+        return BondCanonical(f)
+    raise ValueError(f"not a canonical form: {f!r}")
+
+
+def _sites_from_arrays(arrays, order=("l", "r", "o")):
+    """MPS(arrays; order) (src/Components/MPS.jl:50-94) → 3-D (χl, d, χr) sites."""
+    order = tuple(order)
+    if sorted(order) != ["l", "o", "r"]:
+        raise ValueError("order must be a permutation of (:l, :r, :o)")
+    n = len(arrays)
+    if n < 2:
+        raise ValueError("an MPS needs at least 2 sites")
+    out = []
+    for i, a in enumerate(arrays):
+        a = np.asarray(a)
+        if i == 0:
+            lo = tuple(x for x in order if x != "l")
+            if a.ndim != 2:
+                raise ValueError("First array must have 2 dimensions")
+            t = np.moveaxis(a, [lo.index("o"), lo.index("r")], [0, 1])[None]
+        elif i == n - 1:
+            lo = tuple(x for x in order if x != "r")
+            if a.ndim != 2:
+                raise ValueError("Last array must have 2 dimensions")
+            t = np.moveaxis(a, [lo.index("l"), lo.index("o")], [0, 1])[:, :, None]
+        else:
+            if a.ndim != 3:
+                raise ValueError("All arrays must have 3 dimensions")
+            t = np.moveaxis(a, [order.index("l"), order.index("o"), order.index("r")], [0, 1, 2])
+        out.append(t.astype(np.complex128))
+    return out
+
+
+class MPS:
+    """MatrixProductState on one GB300.  ``sites`` are (χl, d, χr) arrays (C-ordered
+    numpy accepted; any memory order is fine)."""
+
+    def __init__(self, sites=None, *, arrays=None, order=("l", "r", "o"), ctx: Context | None = None,
+                 max_bond=0, precision="native", _handle=None):
+        self.ctx = ctx or default_context()
+        self.lib = self.ctx.lib
+        if _handle is not None:
+            self.h = _handle
+            return
+        if arrays is not None:
+            sites = _sites_from_arrays(arrays, order)
+        sites = [np.asarray(s, dtype=np.complex128) for s in sites]
+        L_ = len(sites)
+        d = sites[0].shape[1]
+        bonds = [s.shape[2] for s in sites[:-1]]
+        for i in range(L_ - 1):
+            if sites[i].shape[2] != sites[i + 1].shape[0]:
+                raise ValueError(f"bond {i + 1}-{i + 2}: dims differ")
+        if sites[0].shape[0] != 1 or sites[-1].shape[2] != 1:
+            raise ValueError("open boundary: end sites must have a size-1 outer bond")
+        h = C.c_void_p()
+        b = (C.c_int64 * (L_ - 1))(*bonds)
+        self.ctx.check(self.lib.tn_mps_create(self.ctx.h, L_, d, b, int(max_bond), precision_code(precision), C.byref(h)))
+        self.h = h
+        for i, s in enumerate(sites):
+            f = np.asfortranarray(s)
+            self.ctx.check(self.lib.tn_mps_set_site(self.h, i + 1, s.shape[0], s.shape[2], f.ctypes.data_as(C.c_void_p)))
+        self._L, self._d = L_, d
+
+    # -- bookkeeping -----------------------------------------------------------
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                self.lib.tn_mps_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def _chk(self, st):
+        self.ctx.check(st)
+
+    @property
+    def nsites(self):
+        return len(self.bondsizes()) + 1
+
+    def bondsizes(self):
+        n = self._L - 1
+        out = (C.c_int64 * n)()
+        self._chk(self.lib.tn_mps_bond_dims(self.h, out))
+        return list(out)
+
+    def maxbondsize(self):
+        return max(self.bondsizes())
+
+    @property
+    def form(self):
+        k, lo, hi = C.c_int32(), C.c_int32(), C.c_int32()
+        self._chk(self.lib.tn_mps_form(self.h, C.byref(k), C.byref(lo), C.byref(hi)))
+        if k.value == L.TN_FORM_NONCANONICAL:
+            return NonCanonical()
+        if k.value == L.TN_FORM_MIXED:
+            return MixedCanonical(list(range(lo.value, hi.value + 1)))
+        return BondCanonical(lo.value, hi.value)
+
+    def unsafe_setform_(self, form):
+        form = _as_form(form)
+        if isinstance(form, NonCanonical):
+            self._chk(self.lib.tn_mps_set_form(self.h, L.TN_FORM_NONCANONICAL, 0, 0))
+        elif isinstance(form, MixedCanonical):
+            self._chk(self.lib.tn_mps_set_form(self.h, L.TN_FORM_MIXED, form.lo, form.hi))
+        else:
+            raise ValueError("only NonCanonical / MixedCanonical can be set without computation")
+        return self
+
+    def set_precision(self, precision):
+        self._chk(self.lib.tn_mps_set_precision(self.h, precision_code(precision)))
+
+    def copy(self):
+        h = C.c_void_p()
+        self._chk(self.lib.tn_mps_copy(self.h, C.byref(h)))
+        m = MPS(ctx=self.ctx, _handle=h)
+        m._L, m._d = self._L, self._d
+        return m
+
+    def site(self, i):
+        """Site tensor i (1-based) as a (χl, d, χr) numpy array."""
+        b = [1] + self.bondsizes() + [1]
+        shape = (b[i - 1], self._d, b[i])
+        out = np.empty(int(np.prod(shape)), dtype=np.complex128)
+        self._chk(self.lib.tn_mps_get_site(self.h, i, out.ctypes.data_as(C.c_void_p)))
+        return out.reshape(shape, order="F")
+
+    def sites(self):
+        return [self.site(i) for i in range(1, self._L + 1)]
+
+    def lambda_(self):
+        """Λ at the bond-canonical centre (LambdaSite(bond))."""
+        n = C.c_int64()
+        self._chk(self.lib.tn_mps_get_lambda(self.h, None, C.byref(n)))
+        out = np.empty(n.value, dtype=np.float64)
+        self._chk(self.lib.tn_mps_get_lambda(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n)))
+        return out
+
+    # -- Tenet operations --------------------------------------------------------
+    def canonize_(self, form):
+        """canonize!(ψ, form)."""
+        form = _as_form(form)
+        if isinstance(form, NonCanonical):
+            return self.unsafe_setform_(form)
+        if isinstance(form, MixedCanonical):
+            self._chk(self.lib.tn_mps_canonize_mixed(self.h, form.lo, form.hi))
+        else:
+            self._chk(self.lib.tn_mps_canonize_bond(self.h, form.a))
+        return self
+
+    def compress_(self, bond=None, maxdim=None, threshold=None):
+        """compress!(ψ[, bond]; maxdim, threshold) ≡ truncate! (compress.jl:18-69)."""
+        if maxdim is None and threshold is None:
+            raise ValueError("Either `maxdim` or `threshold` must be specified")
+        if maxdim is not None and maxdim <= 0:
+            raise ValueError("maxdim must be a positive integer")
+        if threshold is not None and threshold <= 0:
+            raise ValueError("Threshold must be positive")
+        a = 0 if bond is None else min(bond)
+        self._chk(self.lib.tn_mps_compress(self.h, a, -1 if maxdim is None else int(maxdim),
+                                           -1.0 if threshold is None else float(threshold)))
+        return self
+
+    truncate_ = compress_
+
+    def simple_update_(self, op, sites, maxdim=None, threshold=None):
+        """simple_update!(ψ, op; maxdim) on the given 1-based sites; a 2-site op has
+        index order [plug a, plug b, plug a', plug b'] (a < b adjacent)."""
+        sites = sorted(int(s) for s in np.atleast_1d(sites))
+        op = np.asfortranarray(np.asarray(op, dtype=np.complex128))
+        if len(sites) == 2 and sites[1] != sites[0] + 1:
+            raise ValueError("2-site gates must act on adjacent sites")
+        self._chk(self.lib.tn_mps_simple_update(self.h, len(sites), sites[0], op.ctypes.data_as(C.c_void_p),
+                                                -1 if maxdim is None else int(maxdim),
+                                                -1.0 if threshold is None else float(threshold)))
+        return self
+
+    def evolve_(self, op, sites):
+        """evolve!(ψ, gate) → simple_update! without keyword arguments (evolve.jl:140-143)."""
+        return self.simple_update_(op, sites)
+
+    def evolve_brickwork_(self, layers, maxdim=None, threshold=None):
+        """Apply brickwork layers [(start_bond, [G, …]), …] in one library call."""
+        starts = (C.c_int32 * len(layers))(*[int(s) for s, _ in layers])
+        counts = (C.c_int32 * len(layers))(*[len(g) for _, g in layers])
+        flat = [np.asfortranarray(np.asarray(G, dtype=np.complex128)).reshape(-1, order="F") for _, gs in layers for G in gs]
+        buf = np.ascontiguousarray(np.concatenate(flat)) if flat else np.zeros(1, np.complex128)
+        self._chk(self.lib.tn_mps_evolve_brickwork(self.h, len(layers), starts, counts, buf.ctypes.data_as(C.c_void_p),
+                                                   -1 if maxdim is None else int(maxdim),
+                                                   -1.0 if threshold is None else float(threshold)))
+        return self
+
+    def norm(self):
+        """norm(ψ) (norm.jl:17-37); moves the orthogonality centre like the reference."""
+        v = C.c_double()
+        self._chk(self.lib.tn_mps_norm(self.h, C.byref(v)))
+        return v.value
+
+    def normalize_(self):
+        self._chk(self.lib.tn_mps_normalize(self.h))
+        return self
+
+    def overlap(self, other: "MPS"):
+        """overlap(self, other) = ⟨other|self⟩ (overlap.jl:36-50)."""
+        out = (C.c_double * 2)()
+        self._chk(self.lib.tn_mps_overlap(self.h, other.h, out))
+        return complex(out[0], out[1])
+
+    def amplitude(self, bits):
+        """overlap(ProductState(bits), ψ) (overlap.jl:22-32); ``bits`` is a string of
+        0/1/+/-/u/d or a list of length-d vectors."""
+        if isinstance(bits, str):
+            vecs = _product_vectors(bits)
+        else:
+            vecs = [np.asarray(v, dtype=np.complex128) for v in bits]
+        v = np.ascontiguousarray(np.stack(vecs))
+        out = (C.c_double * 2)()
+        self._chk(self.lib.tn_mps_amplitude(self.h, v.ctypes.data_as(C.c_void_p), out))
+        return complex(out[0], out[1])
+
+    def local_expectations(self, op):
+        """⟨ψ|O_i|ψ⟩/⟨ψ|ψ⟩ for every site i."""
+        o = np.asfortranarray(np.asarray(op, dtype=np.complex128))
+        out = np.empty(2 * self._L, dtype=np.float64)
+        self._chk(self.lib.tn_mps_local_expectations(self.h, o.ctypes.data_as(C.c_void_p),
+                                                     out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out[0::2] + 1j * out[1::2]
+
+
+def _product_vectors(bits):
+    s = 1 / np.sqrt(2)
+    table = {"0": [1, 0], "1": [0, 1], "+": [s, s], "-": [s, -s], "u": [s, -1j * s], "↑": [s, -1j * s],
+             "d": [-s, -1j * s], "↓": [-s, -1j * s]}
+    out = []
+    for c in bits:
+        if c not in table:
+            raise ValueError(f"invalid character: {c}")
+        out.append(np.asarray(table[c], dtype=np.complex128))
+    return out
+
+
+# module-level Tenet-style functions -------------------------------------------------
+def canonize_(psi, form):
+    return psi.canonize_(form)
+
+
+def canonize(psi, form):
+    return psi.copy().canonize_(form)
+
+
+def compress_(psi, bond=None, **kw):
+    return psi.compress_(bond, **kw)
+
+
+def compress(psi, bond=None, **kw):
+    return psi.copy().compress_(bond, **kw)
+
+
+truncate_ = compress_
+truncate = compress
+
+
+def simple_update_(psi, op, sites, **kw):
+    return psi.simple_update_(op, sites, **kw)
+
+
+def evolve_(psi, op, sites):
+    return psi.evolve_(op, sites)
+
+
+def overlap(a, b):
+    return a.overlap(b)
+
+
+def norm(psi):
+    return psi.norm()
+
+
+def normalize_(psi):
+    return psi.normalize_()
+
+
+def normalize(psi):
+    return psi.copy().normalize_()

@@ -1,0 +1,244 @@
+"""GPU parity of the individual kernels (K1 permute, K2 GEMM, K3 QR, K4 SVD, K5 ops)
+against numpy/LAPACK on the same seeded inputs, through the C ABI.
+
+Tolerances: integer-exact for the permutation (it moves bits); FP64 results within
+1e-12 relative (the plain-form bar); FP32 within 1e-5.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import tenetgb
+
+    return tenetgb.Context(0)
+
+
+def cgauss(rng, shape, dtype=np.complex128):
+    return ((rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2)).astype(dtype)
+
+
+@pytest.mark.parametrize("shape,perm", [
+    ((64, 2, 64), (2, 1, 0)),
+    ((3, 5, 7, 11), (1, 3, 0, 2)),
+    ((256, 2, 256), (0, 2, 1)),
+    ((33, 65), (1, 0)),
+    ((1, 17, 1, 9), (3, 2, 1, 0)),
+    ((8, 8, 8, 8, 8), (4, 0, 3, 1, 2)),
+])
+@pytest.mark.parametrize("dtype", [np.complex128, np.complex64, np.float64, np.float32])
+def test_permute_bit_exact(ctx, shape, perm, dtype):
+    import tenetgb
+
+    rng = np.random.default_rng(0)
+    x = cgauss(rng, shape, np.complex128)
+    x = (x if np.iscomplexobj(np.zeros(1, dtype)) else x.real).astype(dtype)
+    labels = [f"i{k}" for k in range(len(shape))]
+    t = tenetgb.DeviceTensor.from_numpy(ctx, x, labels)
+    out = tenetgb.permute(t, [labels[p] for p in perm]).numpy()
+    assert out.dtype == x.dtype
+    np.testing.assert_array_equal(out, np.transpose(x, perm))
+
+
+def test_permute_conj(ctx):
+    import tenetgb
+
+    rng = np.random.default_rng(1)
+    x = cgauss(rng, (40, 3, 50))
+    t = tenetgb.DeviceTensor.from_numpy(ctx, x, ["a", "b", "c"])
+    out = tenetgb.permute(t, ["c", "a", "b"], conj=True).numpy()
+    np.testing.assert_array_equal(out, np.transpose(x, (2, 0, 1)).conj())
+
+
+@pytest.mark.parametrize("opa,opb", [("N", "N"), ("N", "C"), ("C", "N"), ("T", "T"), ("T", "N")])
+@pytest.mark.parametrize("m,n,k,batch", [(130, 70, 90, 1), (8, 512, 256, 1), (37, 11, 5, 3), (512, 512, 512, 1)])
+def test_gemm_c64(ctx, opa, opb, m, n, k, batch):
+    import ctypes as C
+
+    import tenetgb
+
+    rng = np.random.default_rng(2)
+    ra, ca = (m, k) if opa == "N" else (k, m)
+    rb, cb = (k, n) if opb == "N" else (n, k)
+    A = cgauss(rng, (batch, ra, ca))
+    B = cgauss(rng, (batch, rb, cb))
+    Cm = cgauss(rng, (batch, m, n))
+
+    def op(X, o):
+        return X if o == "N" else (np.swapaxes(X, -1, -2) if o == "T" else np.swapaxes(X, -1, -2).conj())
+
+    alpha, beta = 0.7 - 0.2j, 0.3 + 0.1j
+    ref = alpha * op(A, opa) @ op(B, opb) + beta * Cm
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, np.transpose(A, (1, 2, 0)))
+    dB = tenetgb.DeviceTensor.from_numpy(ctx, np.transpose(B, (1, 2, 0)))
+    dC = tenetgb.DeviceTensor.from_numpy(ctx, np.transpose(Cm, (1, 2, 0)))
+    al = (C.c_double * 2)(alpha.real, alpha.imag)
+    be = (C.c_double * 2)(beta.real, beta.imag)
+    ctx.check(ctx.lib.tn_gemm(ctx.h, 3, 0, opa.encode(), opb.encode(), m, n, k, al, C.c_void_p(dA.ptr), ra, ra * ca,
+                              C.c_void_p(dB.ptr), rb, rb * cb, be, C.c_void_p(dC.ptr), m, m * n, batch))
+    out = np.transpose(dC.numpy(), (2, 0, 1))
+    err = np.abs(out - ref).max() / np.abs(ref).max()
+    assert err < 1e-13, err
+
+
+def test_gemm_real_and_c32(ctx):
+    import ctypes as C
+
+    import tenetgb
+
+    rng = np.random.default_rng(3)
+    for dt, code, tol in [(np.float64, 1, 1e-13), (np.float32, 0, 1e-5), (np.complex64, 2, 1e-5)]:
+        A = cgauss(rng, (70, 50)).astype(dt) if np.iscomplexobj(np.zeros(1, dt)) else rng.standard_normal((70, 50)).astype(dt)
+        B = cgauss(rng, (50, 40)).astype(dt) if np.iscomplexobj(np.zeros(1, dt)) else rng.standard_normal((50, 40)).astype(dt)
+        dA = tenetgb.DeviceTensor.from_numpy(ctx, A)
+        dB = tenetgb.DeviceTensor.from_numpy(ctx, B)
+        dC = tenetgb.DeviceTensor(ctx, (70, 40), dt)
+        one = (C.c_double * 2)(1, 0)
+        zero = (C.c_double * 2)(0, 0)
+        ctx.check(ctx.lib.tn_gemm(ctx.h, code, 0, b"N", b"N", 70, 40, 50, one, C.c_void_p(dA.ptr), 70, 0,
+                                  C.c_void_p(dB.ptr), 50, 0, zero, C.c_void_p(dC.ptr), 70, 0, 1))
+        ref = A.astype(np.complex128) @ B.astype(np.complex128)
+        assert np.abs(dC.numpy() - ref).max() / np.abs(ref).max() < tol
+
+
+@pytest.mark.parametrize("m,n", [(128, 64), (512, 256), (64, 128), (1024, 512), (7, 7), (300, 1), (2, 4)])
+def test_qr_thin(ctx, m, n):
+    import tenetgb
+
+    rng = np.random.default_rng(4)
+    A = cgauss(rng, (m, n))
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, A, ["r", "c"])
+    Q, R = tenetgb.tensor_qr_thin(dA, ["r"], ["c"], "v")
+    q, r = Q.numpy(), R.numpy()
+    k = min(m, n)
+    assert q.shape == (m, k) and r.shape == (k, n)
+    np.testing.assert_allclose(q.conj().T @ q, np.eye(k), atol=1e-13)
+    assert np.abs(q @ r - A).max() <= 1e-13 * np.abs(A).max() * max(1, np.sqrt(n))
+    assert np.abs(np.tril(r, -1)).max() == 0
+    assert np.abs(np.diagonal(r).imag).max() == 0
+
+
+def test_qr_rank_deficient(ctx):
+    """Integer fixture of the reference tests (reshape(1:64, 4, 4, 4)) is rank 2."""
+    import tenetgb
+
+    A = np.arange(1, 65, dtype=np.float64).reshape(16, 4, order="F").astype(np.complex128)
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, A, ["r", "c"])
+    Q, R = tenetgb.tensor_qr_thin(dA, ["r"], ["c"], "v")
+    q, r = Q.numpy(), R.numpy()
+    np.testing.assert_allclose(q.conj().T @ q, np.eye(4), atol=1e-13)
+    np.testing.assert_allclose(q @ r, A, atol=1e-12 * np.abs(A).max())
+
+
+@pytest.mark.parametrize("precision", ["native", "mixed"])
+@pytest.mark.parametrize("m,n", [(128, 64), (64, 128), (512, 512), (300, 260), (40, 40), (1024, 16), (3, 1)])
+def test_svd_thin(ctx, m, n, precision):
+    import tenetgb
+
+    rng = np.random.default_rng(5)
+    A = cgauss(rng, (m, n))
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, A, ["r", "c"])
+    U, s, V = tenetgb.tensor_svd_thin(dA, ["r"], ["c"], "s", precision=precision)
+    u, sv, vh = U.numpy(), s.numpy(), V.numpy()
+    ref = np.linalg.svd(A, compute_uv=False)
+    assert np.all(np.diff(sv) <= 0)
+    assert np.abs(sv - ref).max() <= 1e-12 * ref.max()
+    k = min(m, n)
+    np.testing.assert_allclose(u.conj().T @ u, np.eye(k), atol=1e-12)
+    np.testing.assert_allclose(vh @ vh.conj().T, np.eye(k), atol=1e-12)
+    assert np.abs((u * sv) @ vh - A).max() <= 1e-12 * ref.max()
+
+
+def test_svd_c32(ctx):
+    import tenetgb
+
+    rng = np.random.default_rng(6)
+    A = cgauss(rng, (96, 80), np.complex64)
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, A, ["r", "c"])
+    U, s, V = tenetgb.tensor_svd_thin(dA, ["r"], ["c"], "s")
+    ref = np.linalg.svd(A.astype(np.complex128), compute_uv=False)
+    assert np.abs(s.numpy() - ref).max() <= 1e-5 * ref.max()
+
+
+def test_svd_rank_deficient_and_graded(ctx):
+    import tenetgb
+
+    rng = np.random.default_rng(7)
+    m, n = 200, 120
+    Uo, _ = np.linalg.qr(cgauss(rng, (m, n)))
+    Vo, _ = np.linalg.qr(cgauss(rng, (n, n)))
+    sv = np.logspace(0, -14, n)
+    sv[-10:] = 0
+    A = (Uo * sv) @ Vo.conj().T
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, A, ["r", "c"])
+    U, s, V = tenetgb.tensor_svd_thin(dA, ["r"], ["c"], "s")
+    out = s.numpy()
+    assert np.abs(out - sv).max() <= 1e-12
+    assert np.abs((U.numpy() * out) @ V.numpy() - A).max() <= 1e-12
+
+
+@pytest.mark.parametrize("case", [
+    ("ab,bc->ac", (30, 40), (40, 50)),
+    ("abc,cd->abd", (20, 2, 30), (30, 25)),
+    ("abc,dbe->acde", (6, 5, 7), (8, 5, 9)),
+    ("ab,ab->ab", (10, 12), (10, 12)),
+    ("abc,cb->ab", (16, 4, 8), (8, 4)),
+    ("lsr,rtq->lstq", (16, 2, 16), (16, 2, 16)),
+    ("xay,yaz->xz", (7, 3, 9), (9, 3, 11)),
+])
+def test_contract_matches_einsum(ctx, case):
+    import tenetgb
+
+    spec, sa, sb = case
+    rng = np.random.default_rng(8)
+    A, B = cgauss(rng, sa), cgauss(rng, sb)
+    la, rest = spec.split(",")
+    lb, lc = rest.split("->")
+    shared = set(la) & set(lb)
+    dims = [c for c in shared if c not in lc]
+    ta = tenetgb.DeviceTensor.from_numpy(ctx, A, list(la))
+    tb = tenetgb.DeviceTensor.from_numpy(ctx, B, list(lb))
+    tc = tenetgb.binary_einsum(ta, tb, dims=dims, out_inds=list(lc))
+    ref = np.einsum(spec, A, B)
+    assert np.abs(tc.numpy() - ref).max() <= 1e-13 * max(1.0, np.abs(ref).max())
+
+
+def test_hadamard_and_norm(ctx):
+    import tenetgb
+
+    rng = np.random.default_rng(9)
+    A = cgauss(rng, (9, 2, 13))
+    lam = np.abs(rng.standard_normal(13))
+    ta = tenetgb.DeviceTensor.from_numpy(ctx, A, ["l", "o", "r"])
+    ts = tenetgb.DeviceTensor.from_numpy(ctx, lam, ["r"])
+    out = tenetgb.hadamard(ta, ts).numpy()
+    np.testing.assert_array_equal(out, A * lam[None, None, :])
+    assert abs(tenetgb.tensor_norm(ta) - np.linalg.norm(A)) <= 1e-14 * np.linalg.norm(A)
+
+
+@pytest.mark.parametrize("precision", ["native", "mixed"])
+def test_muscle_simple_update(ctx, precision):
+    """Muscle.simple_update against the oracle's restatement: singular values kept and
+    the reconstructed two-site tensor."""
+    import tenetgb
+    from oracle import tenet_oracle as O
+    from tenetgb import workloads as W
+
+    rng = np.random.default_rng(10)
+    A = cgauss(rng, (12, 2, 20))
+    B = cgauss(rng, (20, 2, 9))
+    G = W.gate_tensor(W.haar_unitary(rng, 4))
+    An_o, Bn_o, s_o, _ = O.simple_update_tensors(A, B, G, maxdim=10)
+    ta = tenetgb.DeviceTensor.from_numpy(ctx, A, ["l", "pa", "m"])
+    tb = tenetgb.DeviceTensor.from_numpy(ctx, B, ["m", "pb", "r"])
+    tg = tenetgb.DeviceTensor.from_numpy(ctx, G, ["oa", "ob", "pa", "pb"])
+    An, Bn = tenetgb.simple_update(ta, "pa", tb, "pb", "m", tg, "oa", "ob", maxdim=10, precision=precision)
+    a, b = An.numpy(), Bn.numpy()
+    assert a.shape == (12, 2, 10) and b.shape == (10, 2, 9)
+    th = np.tensordot(a, b, axes=(2, 0))
+    th_o = np.tensordot(An_o, Bn_o, axes=(2, 0))
+    assert np.abs(th - th_o).max() <= 1e-12 * np.abs(th_o).max()
