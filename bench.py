@@ -8,10 +8,12 @@ moves by QR, θ = G·A·B, 512×512 SVD, truncation, √S absorption) on the sat
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-Prints one JSON line.  ``value`` is the device-resident mixed-precision path (FP32
-Jacobi pre-pass + FP64 rotations/truncation/overlaps); ``fp64`` is the plain FP64 GPU
-path on the same input; ``e2e`` runs the same layers through the public MPS API from
-host arrays (H2D of the MPS + gates, D2H of the result each step).  ``--impl reference``
+Prints one JSON line.  ``value`` is the mixed-precision batched form: B independent
+instances (initial states from seeds 2, 1002, …; the same circuit) advanced in lockstep,
+each gate an FP32 Jacobi pre-pass + FP64 rotations / truncation / overlaps; the value
+counts gate-layers of all instances.  ``fp64`` is the plain FP64 GPU path on one
+instance; ``e2e`` runs the batched layers through the public MPS API from host arrays
+(H2D of the MPS + gates, D2H of the result each step).  ``--impl reference``
 times the CPU restatement of the reference algorithm (numpy/LAPACK on all host cores) on
 the same workload.  N>1 runs independent replicas, one per GPU (no collective).
 """
@@ -140,11 +142,13 @@ def run_ours(args):
 
     n_layers = SAT_LAYERS + args.warmup + args.steps
     all_layers = layers_for(n_layers)
-    sites0 = W.random_mps_arrays(L_SITES, 2, CHI0, seed=2)
-    base = tenetgb.MPS(sites0, ctx=ctx, max_bond=CHI_MAX, precision="native")
+    Bt = args.batch
+    insts = [W.random_mps_arrays(L_SITES, 2, CHI0, seed=2 + 1000 * b) for b in range(Bt)]
+    base = tenetgb.MPS.batched(insts, ctx=ctx, max_bond=CHI_MAX, precision="native")
     base.evolve_brickwork_(all_layers[:SAT_LAYERS], maxdim=CHI_MAX, threshold=CUTOFF)
     ctx.sync()
-    host_state = base.sites()
+    host_states = [base.sites(b) for b in range(Bt)]
+    host_state = host_states[0]
     run_layers = all_layers[SAT_LAYERS:]
 
     def timed(psi, layers, warm):
@@ -175,29 +179,32 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
     launches_total = ctx.launches() - launches0
     launches_per_step = launches_total / max(1, len(run_layers))
-    # plain FP64 on the same input
-    psi_fp64 = base.copy()
+    # plain FP64 on one instance (instance 0's saturated state)
+    psi_fp64 = tenetgb.MPS(host_state, ctx=ctx, max_bond=CHI_MAX, precision="native")
     t_fp64 = timed(psi_fp64, run_layers, args.warmup)
-    # accuracy of mixed vs FP64 after the same layers
-    ov_m, ov_f = psi_mixed.overlap(psi_mixed), psi_fp64.overlap(psi_fp64)
-    cross = psi_mixed.overlap(psi_fp64)
-    z_m = psi_mixed.local_expectations(W.pauli_z())
+    # accuracy of mixed vs FP64 after the same layers (instance 0)
+    m0 = tenetgb.MPS(psi_mixed.sites(0), ctx=ctx, max_bond=CHI_MAX)
+    ov_m, ov_f = m0.overlap(m0), psi_fp64.overlap(psi_fp64)
+    cross = m0.overlap(psi_fp64)
+    z_m = m0.local_expectations(W.pauli_z())
     z_f = psi_fp64.local_expectations(W.pauli_z())
+    del m0
     # e2e through the public API from host buffers
     t_e2e, h2d, d2h = [], 0, 0
-    state = host_state
+    states = host_states
     for k, ly in enumerate(run_layers):
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
-        psi = tenetgb.MPS(state, ctx=ctx, max_bond=CHI_MAX, precision="mixed")
+        psi = tenetgb.MPS.batched(states, ctx=ctx, max_bond=CHI_MAX, precision="mixed")
         psi.evolve_brickwork_([ly], maxdim=CHI_MAX, threshold=CUTOFF)
-        state = psi.sites()
+        new_states = [psi.sites(b) for b in range(Bt)]
         dt = time.perf_counter() - t0
         del psi
         if k >= args.warmup:
             t_e2e.append(dt)
-            h2d = sum(s.nbytes for s in host_state) + sum(np.asarray(g).nbytes for g in ly[1])
-            d2h = sum(s.nbytes for s in state)
+            h2d = sum(s.nbytes for st in states for s in st) + sum(np.asarray(g).nbytes for g in ly[1])
+            d2h = sum(s.nbytes for st in new_states for s in st)
+        states = new_states
     # max over ranks
     tm, tf, te = sum(t_mixed), sum(t_fp64), sum(t_e2e)
     if ws > 1:
@@ -205,7 +212,7 @@ def run_ours(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         tm, tf, te = t.tolist()
     K = args.steps
-    value = ws * K / tm
+    value = ws * Bt * K / tm
     out = {
         "metric": METRIC,
         "value": value,
@@ -219,16 +226,17 @@ def run_ours(args):
         "vs_baseline": None,
         "dtype": "c64 (FP32 Jacobi pre-pass, FP64 rotations/truncation/overlaps)",
         "data": "synthetic (seeded Gaussian MPS, Haar gates)",
-        "config": dict(CONFIG, parallelism=f"replicas{ws}", l2="flushed between steps (256 MB write)"),
-        "fp64": {"value": ws * K / tf, "unit": UNIT, "ms_per_step": 1e3 * tf / K,
-                 "mixed_speedup": tf / tm},
+        "config": dict(CONFIG, parallelism=f"replicas{ws}", batch_instances=Bt,
+                       l2="flushed between steps (256 MB write)"),
+        "fp64": {"value": ws * K / tf, "unit": UNIT, "ms_per_step": 1e3 * tf / K, "instances": 1,
+                 "speedup_of_value": (Bt * tf) / tm},
         "accuracy_mixed_vs_fp64": {
             "overlap_rel_err": abs(ov_m - ov_f) / abs(ov_f),
             "fidelity_1_minus": float(1 - abs(cross) ** 2 / (abs(ov_m) * abs(ov_f))),
             "z_max_abs_err": float(np.abs(z_m - z_f).max()),
             "layers_compared": len(run_layers),
         },
-        "e2e": {"value": ws * K / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": ws * Bt * K / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(round(launches_per_step * K)),
         "clocks": clk.summary(),
     }
@@ -345,8 +353,35 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def profile_gate(args):
+    """One saturated two-site gate (θ 512×512) on a χ=256 random MPS of 20 sites: the
+    small case for ncu captures.  Runs the gate twice (the first builds the cached CUDA
+    graphs) and prints the second gate's time."""
+    import torch
+
+    import tenetgb
+    from tenetgb import workloads as W
+
+    ctx = tenetgb.Context(0)
+    sites = W.random_mps_arrays(20, 2, CHI_MAX, seed=7)
+    gate = W.gate_tensor(W.haar_unitary(np.random.default_rng(8), 4))
+    psi = tenetgb.MPS(sites, ctx=ctx, max_bond=CHI_MAX, precision=args.precision)
+    psi.canonize_([10, 11])
+    for rep in range(2):
+        ctx.sync()
+        t0 = time.perf_counter()
+        psi.simple_update_(gate, [10, 11], maxdim=CHI_MAX, threshold=CUTOFF)
+        ctx.sync()
+        dt = time.perf_counter() - t0
+    print(json.dumps({"profile_gate_ms": 1e3 * dt, "precision": args.precision, "bond": psi.bondsizes()[9],
+                      "launches": ctx.launches()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--profile-gate", action="store_true", help="one saturated gate (small ncu case)")
+    ap.add_argument("--precision", default="native", choices=["native", "mixed"])
+    ap.add_argument("--batch", type=int, default=8, help="MPS instances advanced in lockstep")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
@@ -354,7 +389,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    if args.impl == "reference":
+    if args.profile_gate:
+        profile_gate(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -45,11 +45,14 @@ typedef int32_t tn_status_t;
 typedef enum { TN_F32 = 0, TN_F64 = 1, TN_C32 = 2, TN_C64 = 3 } tn_dtype_t;
 
 /* arithmetic modes of the contraction GEMMs and factorisations.
- * TN_PREC_NATIVE: the dtype's own arithmetic (FP64 for C64/F64, FP32 for C32/F32).
- * TN_PREC_MIXED: for C64 data, contractions as split-precision tensor-core products and
- *   the SVD as an FP32 Jacobi pre-pass followed by FP64 Jacobi sweeps; FP64 is kept for
- *   the rotations, the truncation decision and norm/overlap accumulation. */
-typedef enum { TN_PREC_NATIVE = 0, TN_PREC_MIXED = 1 } tn_precision_t;
+ * TN_PREC_NATIVE: the dtype's own arithmetic on the CUDA cores (FP64 for C64/F64, FP32
+ *   for C32/F32).
+ * TN_PREC_MIXED: C32/F32 GEMMs as 3xTF32 split products on the tcgen05 tensor pipe
+ *   (FP32-grade); C64 SVDs as an FP32 Jacobi pre-pass followed by FP64 Jacobi sweeps
+ *   (FP64 is kept for the rotations, the truncation decision and norm/overlap
+ *   accumulation); C64 GEMMs stay FP64.
+ * TN_PREC_TF32: C32/F32 GEMMs as single-pass TF32 tensor-core products. */
+typedef enum { TN_PREC_NATIVE = 0, TN_PREC_MIXED = 1, TN_PREC_TF32 = 2 } tn_precision_t;
 
 #define TN_MAX_RANK 8
 
@@ -184,6 +187,17 @@ typedef struct tn_mps tn_mps;
  * the storage reserved per site (0 = the initial bonds only, growing on demand). */
 tn_status_t tn_mps_create(tn_ctx* ctx, int32_t L, int32_t d, const int64_t* bond_dims,
                           int64_t max_bond, tn_precision_t prec, tn_mps** out);
+/* B instances advanced in lockstep by every operation (same L, d, form and bond
+ * dimensions; different tensors).  Operations returning one value per MPS write B values
+ * (instance-major).  Uneven truncation ranks are padded with zero singular values, so
+ * each instance holds exactly its own truncated state. */
+tn_status_t tn_mps_create_batched(tn_ctx* ctx, int32_t B, int32_t L, int32_t d,
+                                  const int64_t* bond_dims, int64_t max_bond,
+                                  tn_precision_t prec, tn_mps** out);
+tn_status_t tn_mps_batch_size(const tn_mps* mps, int32_t* B);
+tn_status_t tn_mps_set_instance_site(tn_mps* mps, int32_t b, int32_t site, int64_t chl,
+                                     int64_t chr, const void* h_data);
+tn_status_t tn_mps_get_instance_site(const tn_mps* mps, int32_t b, int32_t site, void* h_data);
 tn_status_t tn_mps_destroy(tn_mps* mps);
 tn_status_t tn_mps_copy(const tn_mps* src, tn_mps** out);
 /* host data of site i (1-based), column-major (χl, d, χr) C64 */
@@ -195,7 +209,7 @@ tn_status_t tn_mps_set_precision(tn_mps* mps, tn_precision_t prec);
 /* form: kind + (lo, hi) sites for MIXED, (a, a+1) for BOND */
 tn_status_t tn_mps_form(const tn_mps* mps, int32_t* kind, int32_t* lo, int32_t* hi);
 tn_status_t tn_mps_set_form(tn_mps* mps, int32_t kind, int32_t lo, int32_t hi);
-/* Λ at the bond-canonical centre (FP64 host array of length χ_a) */
+/* Λ at the bond-canonical centre (FP64 host array of B × χ_a) */
 tn_status_t tn_mps_get_lambda(const tn_mps* mps, double* h_lambda, int64_t* len);
 
 tn_status_t tn_mps_canonize_mixed(tn_mps* mps, int32_t lo, int32_t hi);
@@ -211,13 +225,14 @@ tn_status_t tn_mps_simple_update(tn_mps* mps, int32_t n_sites, int32_t a, const 
 tn_status_t tn_mps_evolve_brickwork(tn_mps* mps, int32_t n_layers, const int32_t* starts,
                                     const int32_t* n_gates, const void* h_gates,
                                     int64_t maxdim, double threshold);
-/* ⟨b|a⟩ = Σ a·conj(b); h_out = (re, im) */
+/* ⟨b|a⟩ = Σ a·conj(b); h_out = (re, im) per instance */
 tn_status_t tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* h_out);
 tn_status_t tn_mps_norm(tn_mps* mps, double* h_out);
 tn_status_t tn_mps_normalize(tn_mps* mps);
-/* ⟨bits|ψ⟩ with product vectors (not conjugated): h_vectors is L×d C64 (site-major) */
+/* ⟨bits|ψ⟩ with product vectors (not conjugated): h_vectors is L×d C64 (site-major);
+ * h_out = (re, im) per instance */
 tn_status_t tn_mps_amplitude(const tn_mps* mps, const void* h_vectors, double* h_out);
-/* ⟨ψ|O_i|ψ⟩/⟨ψ|ψ⟩ for every site i, O a host d×d C64; h_out is L×(re,im) */
+/* ⟨ψ|O_i|ψ⟩/⟨ψ|ψ⟩ for every site i, O a host d×d C64; h_out is B×L×(re,im) */
 tn_status_t tn_mps_local_expectations(const tn_mps* mps, const void* h_op, double* h_out);
 
 #ifdef __cplusplus

@@ -121,8 +121,9 @@ tn_status_t tn_create(tn_ctx** out, int device) {
   return TN_OK;
 }
 
-tn_status_t tn_destroy(tn_ctx* ctx) {
-  if (!ctx) return TN_OK;
+}  // extern "C"
+
+void ctx_release(tn_ctx* ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
@@ -132,6 +133,17 @@ tn_status_t tn_destroy(tn_ctx* ctx) {
   if (ctx->pinned) cudaFreeHost(ctx->pinned);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
+}
+
+extern "C" {
+
+tn_status_t tn_destroy(tn_ctx* ctx) {
+  if (!ctx) return TN_OK;
+  if (ctx->refs > 0) {
+    ctx->destroy_requested = true;  // released by the last tn_mps_destroy
+    return TN_OK;
+  }
+  ctx_release(ctx);
   return TN_OK;
 }
 

@@ -9,10 +9,11 @@
 
 #include "tn_internal.cuh"
 
-typedef tn_status_t (*su_out_fn)(void* arg, int64_t r, cxd** Aout, cxd** Bout);
+typedef tn_status_t (*su_out_fn)(void* arg, int64_t r, cxd** Aout, int64_t* sAout, cxd** Bout, int64_t* sBout);
 tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, int64_t d1, int64_t chm, int64_t d2,
-                               int64_t chr, const cxd* A, const cxd* B, const cxd* dG, int64_t maxdim, double threshold,
-                               su_out_fn out_fn, void* out_arg, double* Sout, int64_t* rank_out);
+                               int64_t chr, const cxd* A, int64_t sA, const cxd* Bm, int64_t sB, const cxd* dG,
+                               int64_t maxdim, double threshold, int64_t batch, su_out_fn out_fn, void* out_arg,
+                               double* Sout, int64_t* rank_out);
 
 namespace {
 
@@ -27,11 +28,6 @@ bool is_identity(const std::vector<int32_t>& p) {
     if (p[i] != (int32_t)i) return false;
   return true;
 }
-
-struct Raw {
-  const void* in;
-  void* out;
-};
 
 }  // namespace
 
@@ -124,6 +120,7 @@ extern "C" tn_status_t tn_contract(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t
   if (perm_a) need += ws_round(es * (size_t)(m * k * h));
   if (perm_b) need += ws_round(es * (size_t)(k * n * h));
   if (perm_c) need += ws_round(es * (size_t)(m * n * h));
+  need += gemm_any_workspace(dtype, prec, m, n, k);
   TN_RETURN_IF(ws_reserve(ctx, need));
   const void* A = a->data;
   const void* B = b->data;
@@ -141,8 +138,8 @@ extern "C" tn_status_t tn_contract(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t
   if (perm_c) C = ws_take<char>(ctx, es * (size_t)(m * n * h));
   const double one[2] = {1.0, 0.0}, zero[2] = {0.0, 0.0};
   const int64_t lda = opa == 'N' ? m : k, ldb = opb == 'N' ? k : n;
-  TN_RETURN_IF(tn_gemm(ctx, dtype, prec, opa, opb, m, n, k, one, A, std::max<int64_t>(lda, 1), m * k, B,
-                       std::max<int64_t>(ldb, 1), k * n, zero, C, std::max<int64_t>(m, 1), m * n, h));
+  TN_RETURN_IF(gemm_any(ctx, dtype, prec, opa, opb, m, n, k, one, A, std::max<int64_t>(lda, 1), m * k, B,
+                        std::max<int64_t>(ldb, 1), k * n, zero, C, std::max<int64_t>(m, 1), m * n, h));
   if (perm_c) {
     int64_t dims_t[TN_MAX_RANK];
     int r = 0;
@@ -159,10 +156,12 @@ struct FixedOut {
   cxd* A;
   cxd* B;
 };
-tn_status_t fixed_out(void* arg, int64_t, cxd** Aout, cxd** Bout) {
+tn_status_t fixed_out(void* arg, int64_t, cxd** Aout, int64_t* sA, cxd** Bout, int64_t* sB) {
   FixedOut* f = (FixedOut*)arg;
   *Aout = f->A;
   *Bout = f->B;
+  *sA = 0;
+  *sB = 0;
   return TN_OK;
 }
 }  // namespace
@@ -175,8 +174,7 @@ extern "C" tn_status_t tn_simple_update(tn_ctx* ctx, tn_dtype_t dtype, tn_precis
   TN_ARG(ctx, dtype == TN_C64, "tn_simple_update: only C64 is implemented");
   TN_ARG(ctx, chl >= 1 && d1 >= 1 && chm >= 1 && d2 >= 1 && chr >= 1, "tn_simple_update: sizes must be >= 1");
   TN_ARG(ctx, A && B && G && Aout && Bout && rank, "tn_simple_update: null pointer");
-  // device copy of the gate lives in the flags scratch? no: the gate is a device array
   FixedOut f{(cxd*)Aout, (cxd*)Bout};
-  return simple_update_core(ctx, prec, chl, d1, chm, d2, chr, (const cxd*)A, (const cxd*)B, (const cxd*)G, maxdim,
-                            threshold, fixed_out, &f, Sout, rank);
+  return simple_update_core(ctx, prec, chl, d1, chm, d2, chr, (const cxd*)A, 0, (const cxd*)B, 0, (const cxd*)G, maxdim,
+                            threshold, 1, fixed_out, &f, Sout, rank);
 }

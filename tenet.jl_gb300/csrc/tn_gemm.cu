@@ -219,6 +219,56 @@ tn_status_t gemm_mixed_c64(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n
 
 static bool valid_op(char c) { return c == 'N' || c == 'T' || c == 'C'; }
 
+size_t gemm_any_workspace(tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n, int64_t k) {
+  if ((dt == TN_C32 || dt == TN_F32) && prec != TN_PREC_NATIVE)
+    return tc_gemm_workspace(dt == TN_C32, prec == TN_PREC_TF32 ? 1 : 3, m, n, k);
+  return 0;
+}
+
+tn_status_t gemm_any(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, char opa, char opb, int64_t m, int64_t n,
+                     int64_t k, const double* alpha, const void* A, int64_t lda, int64_t strideA, const void* B,
+                     int64_t ldb, int64_t strideB, const double* beta, void* C, int64_t ldc, int64_t strideC,
+                     int64_t batch) {
+  const bool tc = (dtype == TN_C32 || dtype == TN_F32) && prec != TN_PREC_NATIVE;
+  if (tc) {
+    if (dtype == TN_C32 && (alpha[1] != 0.0 || beta[1] != 0.0))
+      return tn_set_error(ctx, TN_EUNSUPPORTED, "tensor-core GEMM: complex alpha/beta not supported");
+    const int passes = prec == TN_PREC_TF32 ? 1 : 3;
+    const size_t es = dtype == TN_C32 ? 8 : 4;
+    const size_t top = ctx->ws_top;
+    for (int64_t b = 0; b < batch; ++b) {
+      ctx->ws_top = top;
+      TN_RETURN_IF(tc_gemm(ctx, dtype == TN_C32, passes, opa, opb, m, n, k, (float)alpha[0],
+                           (const char*)A + es * b * strideA, lda, (const char*)B + es * b * strideB, ldb, (float)beta[0],
+                           (char*)C + es * b * strideC, ldc));
+    }
+    ctx->ws_top = top;
+    return TN_OK;
+  }
+  switch (dtype) {
+    case TN_C64: {
+      cxd a = mkcx(alpha[0], alpha[1]), b = mkcx(beta[0], beta[1]);
+      if (prec == TN_PREC_MIXED)
+        return gemm_mixed_c64(ctx, opa, opb, m, n, k, a, (const cxd*)A, lda, strideA, (const cxd*)B, ldb, strideB, b,
+                              (cxd*)C, ldc, strideC, batch);
+      return gemm_cx<double>(ctx, opa, opb, m, n, k, a, (const cxd*)A, lda, strideA, (const cxd*)B, ldb, strideB, b,
+                             (cxd*)C, ldc, strideC, batch);
+    }
+    case TN_C32: {
+      cxf a = mkcx((float)alpha[0], (float)alpha[1]), b = mkcx((float)beta[0], (float)beta[1]);
+      return gemm_cx<float>(ctx, opa, opb, m, n, k, a, (const cxf*)A, lda, strideA, (const cxf*)B, ldb, strideB, b,
+                            (cxf*)C, ldc, strideC, batch);
+    }
+    case TN_F64:
+      return gemm_re<double>(ctx, opa, opb, m, n, k, alpha[0], (const double*)A, lda, strideA, (const double*)B, ldb,
+                             strideB, beta[0], (double*)C, ldc, strideC, batch);
+    case TN_F32:
+      return gemm_re<float>(ctx, opa, opb, m, n, k, (float)alpha[0], (const float*)A, lda, strideA, (const float*)B,
+                            ldb, strideB, (float)beta[0], (float*)C, ldc, strideC, batch);
+  }
+  return tn_set_error(ctx, TN_EINVAL, "gemm: bad dtype");
+}
+
 extern "C" tn_status_t tn_gemm(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, char opa, char opb,
                                int64_t m, int64_t n, int64_t k, const double* alpha, const void* A,
                                int64_t lda, int64_t strideA, const void* B, int64_t ldb,
@@ -229,32 +279,11 @@ extern "C" tn_status_t tn_gemm(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t pre
   TN_ARG(ctx, m >= 0 && n >= 0 && k >= 0 && batch >= 0, "tn_gemm: negative size");
   TN_ARG(ctx, alpha && beta, "tn_gemm: null alpha/beta");
   TN_ARG(ctx, (m == 0 || n == 0 || batch == 0) || (A && B && C), "tn_gemm: null matrix");
+  TN_ARG(ctx, dtype_complex(dtype) || (opa != 'C' && opb != 'C'), "tn_gemm: 'C' needs a complex dtype");
   int64_t ra = opa == 'N' ? m : k, rb = opb == 'N' ? k : n;
   TN_ARG(ctx, lda >= (ra > 1 ? ra : 1) && ldb >= (rb > 1 ? rb : 1) && ldc >= (m > 1 ? m : 1),
          "tn_gemm: leading dimension too small");
-  switch (dtype) {
-    case TN_C64: {
-      cxd a = mkcx(alpha[0], alpha[1]), b = mkcx(beta[0], beta[1]);
-      if (prec == TN_PREC_MIXED)
-        return gemm_mixed_c64(ctx, opa, opb, m, n, k, a, (const cxd*)A, lda, strideA, (const cxd*)B, ldb,
-                              strideB, b, (cxd*)C, ldc, strideC, batch);
-      return gemm_cx<double>(ctx, opa, opb, m, n, k, a, (const cxd*)A, lda, strideA, (const cxd*)B, ldb,
-                             strideB, b, (cxd*)C, ldc, strideC, batch);
-    }
-    case TN_C32: {
-      cxf a = mkcx((float)alpha[0], (float)alpha[1]), b = mkcx((float)beta[0], (float)beta[1]);
-      return gemm_cx<float>(ctx, opa, opb, m, n, k, a, (const cxf*)A, lda, strideA, (const cxf*)B, ldb,
-                            strideB, b, (cxf*)C, ldc, strideC, batch);
-    }
-    case TN_F64:
-      TN_ARG(ctx, opa != 'C' && opb != 'C', "tn_gemm: 'C' needs a complex dtype");
-      return gemm_re<double>(ctx, opa, opb, m, n, k, alpha[0], (const double*)A, lda, strideA,
-                             (const double*)B, ldb, strideB, beta[0], (double*)C, ldc, strideC, batch);
-    case TN_F32:
-      TN_ARG(ctx, opa != 'C' && opb != 'C', "tn_gemm: 'C' needs a complex dtype");
-      return gemm_re<float>(ctx, opa, opb, m, n, k, (float)alpha[0], (const float*)A, lda, strideA,
-                            (const float*)B, ldb, strideB, (float)beta[0], (float*)C, ldc, strideC,
-                            batch);
-  }
-  return tn_set_error(ctx, TN_EINVAL, "tn_gemm: bad dtype");
+  TN_RETURN_IF(ws_reserve(ctx, gemm_any_workspace(dtype, prec, m, n, k)));
+  return gemm_any(ctx, dtype, prec, opa, opb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc, strideC,
+                  batch);
 }

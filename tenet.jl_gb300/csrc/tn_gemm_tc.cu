@@ -1,14 +1,376 @@
-// K2 (mixed) — split-precision complex GEMM for ComplexF64 data.
+// K2 (tensor cores) — TMA-fed tcgen05 GEMM with the accumulator in TMEM, kind::tf32.
 //
-// Placeholder translation unit: the tcgen05/TMEM kernel is added here.  Until then the
-// mixed-precision GEMM entry point reports that it is not available, so nothing silently
-// changes precision.
+//   C (M×N, column-major) = Σ_p  A_p ᵀ · B_p      over 1 or 3 operand pairs p
+//
+// Both operands are K-major (the contraction index contiguous), which is the layout the
+// contraction planner produces with the permutation kernel.  Precision modes:
+//   * TF32      — one pass (A, B), FP32 accumulation;
+//   * 3×TF32    — three passes (A_hi·B_hi + A_hi·B_lo + A_lo·B_hi) into the same TMEM
+//                 accumulator, where x = x_hi + x_lo and x_hi has TF32's 10-bit mantissa:
+//                 FP32-grade products from the TF32 tensor pipe.
+// Complex operands use the real 4M form as one real GEMM of twice the size:
+//   [Re C; Im C] = [[Ar, −Ai], [Ai, Ar]] · [Br; Bi]
+// built by a prep kernel that also does the hi/lo split, with an epilogue that writes the
+// two row blocks back as interleaved complex.
+//
+// CTA (128 threads) per 128×128 output tile.  Thread 0 issues TMA loads (128-byte
+// swizzle, 4-stage ring with full/empty mbarriers), thread 32 issues tcgen05.mma
+// (M=128, N=128, K=8 per instruction) and commits each stage back to its empty barrier;
+// all four warps then drain TMEM with tcgen05.ld (warp w owns accumulator rows
+// 32w…32w+31).  Every mbarrier wait is bounded: on timeout the kernel records an error
+// word, skips the remaining work, and still releases its TMEM.
+#include <cuda.h>
+
+#include <cstring>
+
 #include "tn_internal.cuh"
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BKB = 128;  // tile: 128×128 outputs, 128 bytes of K
+constexpr int STAGES = 4;
+constexpr int A_BYTES = BM * BKB, B_BYTES = BN * BKB;
+constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024 /*align*/ + 256 /*barriers*/;
+constexpr long long kSpinLimit = 1ll << 28;
+
+struct Maps {
+  CUtensorMap a[2];  // A_hi, A_lo
+  CUtensorMap b[2];  // B_hi, B_lo
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false (and the error word set) if the phase never completes
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err) {
+  for (long long i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  atomicExch(err, 1);
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(smem_u32(bar)), "r"(x), "r"(y)
+      : "memory");
+}
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sdesc(const void* p) {
+  const uint64_t addr = (uint64_t)smem_u32(p);
+  uint64_t d = (addr & 0x3FFFFull) >> 4;  // start address
+  d |= 1ull << 16;                        // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset: 8 rows × 128 B
+  d |= 1ull << 46;                        // descriptor version for tcgen05
+  d |= 2ull << 61;                        // 128-byte swizzle
+  return d;
+}
+// instruction descriptor: D f32, A/B tf32, both K-major, N = BN, M = BM
+constexpr uint32_t kIdescTF32 = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                                ((uint32_t)(BM >> 4) << 24);
+
+__device__ __forceinline__ void mma_tf32(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          dtmem),
+      "l"(a), "l"(b), "r"(kIdescTF32), "r"(accum)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+template <int EPI>  // 0: real C (float); 1: complex interleaved from [Re; Im] row blocks
+__global__ void __launch_bounds__(128, 1)
+    k_gemm_tf32(const __grid_constant__ Maps maps, int passes, int M, int N, int K, float* __restrict__ C,
+                int64_t ldc, int Mh, float alpha, float beta, int* err) {
+  extern __shared__ unsigned char smem_raw[];
+  const uint32_t base_u = smem_u32(smem_raw);
+  unsigned char* smem = smem_raw + ((1024 - (base_u & 1023)) & 1023);
+  unsigned char* sA = smem;
+  unsigned char* sB = smem + STAGES * A_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * (A_BYTES + B_BYTES));
+  uint64_t* full = bars;
+  uint64_t* empty = bars + STAGES;
+  uint64_t* done = bars + 2 * STAGES;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 32) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(done, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  const int nk = (K + 31) / 32;  // 32 fp32 = 128 bytes of K per tile
+  const int total = passes * nk;
+  if (tid == 0) {
+    // producer
+    for (int t = 0; t < total; ++t) {
+      const int s = t % STAGES;
+      if (t >= STAGES && !mbar_wait(&empty[s], ((t / STAGES) & 1) ^ 1, err)) break;
+      const int pass = t / nk, kt = t % nk;
+      const CUtensorMap* am = &maps.a[pass == 2 ? 1 : 0];
+      const CUtensorMap* bm = &maps.b[pass == 1 ? 1 : 0];
+      mbar_expect_tx(&full[s], A_BYTES + B_BYTES);
+      tma_load_2d(sA + s * A_BYTES, am, &full[s], kt * 32, m0);
+      tma_load_2d(sB + s * B_BYTES, bm, &full[s], kt * 32, n0);
+    }
+  } else if (tid == 32) {
+    // MMA issuer
+    bool ok = true;
+    for (int t = 0; t < total && ok; ++t) {
+      const int s = t % STAGES;
+      ok = mbar_wait(&full[s], (t / STAGES) & 1, err);
+      if (!ok) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk) {  // 4 × (K = 8 tf32 = 32 bytes)
+        const uint64_t a = sdesc(sA + s * A_BYTES) + (uint64_t)((kk * 32) >> 4);
+        const uint64_t b = sdesc(sB + s * B_BYTES) + (uint64_t)((kk * 32) >> 4);
+        mma_tf32(tmem, a, b, (t > 0 || kk > 0) ? 1u : 0u);
+      }
+      mma_commit(&empty[s]);
+    }
+    mma_commit(done);
+  }
+  __syncwarp();
+  // epilogue: all 4 warps
+  const bool ok = mbar_wait(done, 0, err);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const int row = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+            "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (row < M) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int col = n0 + c0 + j;
+          if (col >= N) break;
+          float v = alpha * __uint_as_float(r[j]);
+          float* dst;
+          if (EPI == 0)
+            dst = C + row + (int64_t)col * ldc;
+          else
+            dst = C + 2 * ((int64_t)(row % Mh) + (int64_t)col * ldc) + (row >= Mh ? 1 : 0);
+          if (beta != 0.f) v += beta * *dst;
+          *dst = v;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+}
+
+// ---------------------------------------------------------------------------------
+// operand preparation: K-major real planes (hi, lo) with K padded to Kp (multiple of 32)
+// ---------------------------------------------------------------------------------
+__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+
+// element (r, c) of op(X) for a column-major complex X with leading dimension ld
+__device__ __forceinline__ cxf ld_op(const cxf* X, int64_t ld, char op, int64_t r, int64_t c) {
+  if (op == 'N') return X[r + c * ld];
+  cxf v = X[c + r * ld];
+  if (op == 'C') v.y = -v.y;
+  return v;
+}
+
+// A' (rows i' < 2M, K-major, pitch Kp): i' < M → [Ar, −Ai], i' ≥ M → [Ai, Ar]
+__global__ void k_prep_a_cx(int64_t M, int64_t K, int64_t Kp, const cxf* A, int64_t lda, char op, float* hi, float* lo) {
+  const int64_t total = 2 * M * Kp;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t kp = t % Kp, ip = t / Kp;
+    float v = 0.f;
+    if (kp < 2 * K) {
+      const int64_t i = ip % M, k = kp % K;
+      const cxf a = ld_op(A, lda, op, i, k);
+      const bool top = ip < M, left = kp < K;
+      v = top ? (left ? a.x : -a.y) : (left ? a.y : a.x);
+    }
+    const float h = tf32_hi(v);
+    hi[t] = h;
+    if (lo) lo[t] = v - h;
+  }
+}
+// B' (columns j < N, K-major, pitch Kp): [Br; Bi]
+__global__ void k_prep_b_cx(int64_t N, int64_t K, int64_t Kp, const cxf* B, int64_t ldb, char op, float* hi, float* lo) {
+  const int64_t total = N * Kp;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t kp = t % Kp, j = t / Kp;
+    float v = 0.f;
+    if (kp < 2 * K) {
+      const cxf b = ld_op(B, ldb, op, kp % K, j);
+      v = kp < K ? b.x : b.y;
+    }
+    const float h = tf32_hi(v);
+    hi[t] = h;
+    if (lo) lo[t] = v - h;
+  }
+}
+// real: A' (M rows, K-major) from op(A); B' (N columns, K-major) from op(B)
+__global__ void k_prep_re(int64_t R, int64_t K, int64_t Kp, const float* X, int64_t ld, bool kmajor_src, float* hi,
+                          float* lo) {
+  const int64_t total = R * Kp;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t kp = t % Kp, r = t / Kp;
+    float v = 0.f;
+    if (kp < K) v = kmajor_src ? X[kp + r * ld] : X[r + kp * ld];
+    const float h = tf32_hi(v);
+    hi[t] = h;
+    if (lo) lo[t] = v - h;
+  }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn(tn_ctx* ctx) {
+  static EncodeTiledFn fn = nullptr;
+  if (fn) return fn;
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p) {
+    tn_set_error(ctx, TN_ECUDA, "cuTensorMapEncodeTiled unavailable");
+    return nullptr;
+  }
+  fn = (EncodeTiledFn)p;
+  return fn;
+}
+
+// K-major operand: rows × Kp floats, row pitch Kp·4 bytes; box 32 × 128
+tn_status_t make_map(tn_ctx* ctx, CUtensorMap* map, const float* base, int64_t rows, int64_t Kp) {
+  EncodeTiledFn fn = encode_fn(ctx);
+  if (!fn) return TN_ECUDA;
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)(Kp * 4)};
+  cuuint32_t box[2] = {32, 128};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return tn_set_error(ctx, TN_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return TN_OK;
+}
+
+unsigned blocks_for(tn_ctx* ctx, int64_t n) {
+  int64_t b = (n + 255) / 256;
+  int64_t cap = (int64_t)ctx->num_sms * 16;
+  return (unsigned)std::max<int64_t>(1, std::min(b, cap));
+}
+
+}  // namespace
+
+// Workspace (bytes) for tc_gemm on the given shape.
+size_t tc_gemm_workspace(bool complex_in, int passes, int64_t m, int64_t n, int64_t k) {
+  const int64_t Kp = ((complex_in ? 2 * k : k) + 31) / 32 * 32;
+  const int64_t Ma = complex_in ? 2 * m : m;
+  const int copies = passes > 1 ? 2 : 1;
+  return copies * (ws_round(4 * (size_t)(Ma * Kp)) + ws_round(4 * (size_t)(n * Kp))) + ws_round(sizeof(int) * 4);
+}
+
+// C (m×n) = op(A)·op(B) on the TF32 tensor pipe (passes: 1 = TF32, 3 = 3×TF32).
+// complex_in: A, B, C are interleaved complex (C64 data must be converted by the caller);
+// otherwise real float.  beta applies to C (real).  Workspace reserved by the caller.
+tn_status_t tc_gemm(tn_ctx* ctx, bool complex_in, int passes, char opa, char opb, int64_t m, int64_t n, int64_t k,
+                    float alpha, const void* A, int64_t lda, const void* B, int64_t ldb, float beta, void* C, int64_t ldc) {
+  if (m == 0 || n == 0) return TN_OK;
+  const int64_t Kp = ((complex_in ? 2 * k : k) + 31) / 32 * 32;
+  const int64_t Ma = complex_in ? 2 * m : m;
+  if (Ma > (1ll << 31) - 128 || n > (1ll << 31) - 128) return tn_set_error(ctx, TN_EUNSUPPORTED, "tc_gemm: too large");
+  const bool split = passes > 1;
+  float* Ahi = ws_take<float>(ctx, (size_t)(Ma * Kp));
+  float* Bhi = ws_take<float>(ctx, (size_t)(n * Kp));
+  float* Alo = split ? ws_take<float>(ctx, (size_t)(Ma * Kp)) : nullptr;
+  float* Blo = split ? ws_take<float>(ctx, (size_t)(n * Kp)) : nullptr;
+  int* err = ws_take<int>(ctx, 4);
+  TN_CHECK_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+  if (complex_in) {
+    k_prep_a_cx<<<blocks_for(ctx, Ma * Kp), 256, 0, ctx->stream>>>(m, k, Kp, (const cxf*)A, lda, opa, Ahi, Alo);
+    TN_LAUNCHED(ctx);
+    k_prep_b_cx<<<blocks_for(ctx, n * Kp), 256, 0, ctx->stream>>>(n, k, Kp, (const cxf*)B, ldb, opb, Bhi, Blo);
+    TN_LAUNCHED(ctx);
+  } else {
+    // A' rows are the m rows of op(A): K-major source when op(A) = Aᵀ
+    k_prep_re<<<blocks_for(ctx, m * Kp), 256, 0, ctx->stream>>>(m, k, Kp, (const float*)A, lda, opa != 'N', Ahi, Alo);
+    TN_LAUNCHED(ctx);
+    k_prep_re<<<blocks_for(ctx, n * Kp), 256, 0, ctx->stream>>>(n, k, Kp, (const float*)B, ldb, opb == 'N', Bhi, Blo);
+    TN_LAUNCHED(ctx);
+  }
+  Maps maps;
+  memset(&maps, 0, sizeof(maps));
+  TN_RETURN_IF(make_map(ctx, &maps.a[0], Ahi, Ma, Kp));
+  TN_RETURN_IF(make_map(ctx, &maps.b[0], Bhi, n, Kp));
+  if (split) {
+    TN_RETURN_IF(make_map(ctx, &maps.a[1], Alo, Ma, Kp));
+    TN_RETURN_IF(make_map(ctx, &maps.b[1], Blo, n, Kp));
+  } else {
+    maps.a[1] = maps.a[0];
+    maps.b[1] = maps.b[0];
+  }
+  dim3 grid(cdiv(Ma, BM), cdiv(n, BN));
+  if (grid.y > 65535) return tn_set_error(ctx, TN_EUNSUPPORTED, "tc_gemm: n too large");
+  if (complex_in) {
+    TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tf32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    k_gemm_tf32<1><<<grid, 128, SMEM_BYTES, ctx->stream>>>(maps, passes, (int)Ma, (int)n, (int)Kp, (float*)C, ldc,
+                                                           (int)m, alpha, beta, err);
+  } else {
+    TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tf32<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    k_gemm_tf32<0><<<grid, 128, SMEM_BYTES, ctx->stream>>>(maps, passes, (int)Ma, (int)n, (int)Kp, (float*)C, ldc,
+                                                           (int)m, alpha, beta, err);
+  }
+  TN_LAUNCHED(ctx);
+  int* hp = reinterpret_cast<int*>(ctx->pinned);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (hp[0]) return tn_set_error(ctx, TN_ETIMEOUT, "tc_gemm: a pipeline wait timed out");
+  return TN_OK;
+}
 
 tn_status_t gemm_mixed_c64(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64_t k, cxd alpha, const cxd* A,
                            int64_t lda, int64_t sA, const cxd* B, int64_t ldb, int64_t sB, cxd beta, cxd* C,
                            int64_t ldc, int64_t sC, int64_t batch) {
   (void)opa; (void)opb; (void)m; (void)n; (void)k; (void)alpha; (void)A; (void)lda; (void)sA; (void)B; (void)ldb;
   (void)sB; (void)beta; (void)C; (void)ldc; (void)sC; (void)batch;
-  return tn_set_error(ctx, TN_EUNSUPPORTED, "mixed-precision GEMM is not built yet");
+  return tn_set_error(ctx, TN_EUNSUPPORTED,
+                      "C64 contractions stay FP64: split-TF32 products are FP32-grade (use C32 data for the tensor path)");
 }

@@ -100,7 +100,12 @@ struct tn_ctx {
   int64_t launches = 0;
   // instantiated CUDA graphs (e.g. one Jacobi sweep), keyed by shape + buffer addresses
   std::unordered_map<std::string, cudaGraphExec_t> graphs;
+  // live objects (MPS handles) that refer to this context; tn_destroy defers the
+  // release until the last of them is destroyed
+  int refs = 0;
+  bool destroy_requested = false;
 };
+void ctx_release(tn_ctx* ctx);  // frees the context (called when refs drop to 0)
 
 tn_status_t tn_set_error(tn_ctx* ctx, tn_status_t st, const char* fmt, ...);
 
@@ -213,15 +218,36 @@ tn_status_t svd_any(tn_ctx* ctx, tn_dtype_t dt, tn_precision_t prec, int64_t m, 
                     const void* A, int64_t lda, int64_t sA, void* U, int64_t sU, double* S,
                     int64_t sS, void* Vh, int64_t sVh, int64_t batch);
 
+// any-dtype GEMM (no workspace reservation: the caller reserves gemm_any_workspace)
+size_t gemm_any_workspace(tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n, int64_t k);
+tn_status_t gemm_any(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, char opa, char opb, int64_t m, int64_t n,
+                     int64_t k, const double* alpha, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb,
+                     int64_t sB, const double* beta, void* C, int64_t ldc, int64_t sC, int64_t batch);
+// tcgen05 TF32 GEMM (tn_gemm_tc.cu)
+size_t tc_gemm_workspace(bool complex_in, int passes, int64_t m, int64_t n, int64_t k);
+tn_status_t tc_gemm(tn_ctx* ctx, bool complex_in, int passes, char opa, char opb, int64_t m, int64_t n, int64_t k,
+                    float alpha, const void* A, int64_t lda, const void* B, int64_t ldb, float beta, void* C,
+                    int64_t ldc);
+
 // K5 helpers
 tn_status_t rank_select(tn_ctx* ctx, const double* S, int64_t k, int64_t maxdim,
                         double threshold, int64_t* rank);
+// per-instance ranks; returns the max and zeroes S_b beyond rank_b up to the max so that
+// a common (padded) bond dimension carries exactly each instance's truncated state
+tn_status_t rank_select_batched(tn_ctx* ctx, double* S, int64_t k, int64_t sS, int64_t batch,
+                                int64_t maxdim, double threshold, int64_t* rank_max,
+                                int64_t* ranks);
 template <typename T>
 tn_status_t scale_cols_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld,
-                            const double* S);
+                            const double* S, int64_t sX = 0, int64_t sS = 0, int64_t batch = 1);
 template <typename T>
 tn_status_t scale_rows_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld,
-                            const double* S);
+                            const double* S, int64_t sX = 0, int64_t sS = 0, int64_t batch = 1);
 tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out);
 tn_status_t copy_matrix_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src,
-                            int64_t lds, cxd* dst, int64_t ldd);
+                            int64_t lds, cxd* dst, int64_t ldd, int64_t sSrc = 0,
+                            int64_t sDst = 0, int64_t batch = 1);
+tn_status_t norms_batched(tn_ctx* ctx, bool complex_data, int64_t n, const void* x, int64_t sx,
+                          int64_t batch, double* h_out);
+tn_status_t zdotc_batched(tn_ctx* ctx, int64_t n, const cxd* x, int64_t sx, const cxd* y,
+                          int64_t sy, int64_t batch, double* h_out);

@@ -5,6 +5,13 @@
 //   site i (1-based): (χ_{i-1}, d, χ_i) ComplexF64, column-major — Tenet's (:l, :o, :r)
 //   order (src/Components/MPS.jl:50-94) with the open-end bonds χ_0 = χ_L = 1.
 //
+// A tn_mps holds B ≥ 1 instances that share L, d, the canonical form and the bond
+// dimensions, and are advanced in lockstep by every operation (batched kernels: one
+// launch serves all B instances).  Instance b of site i lives at site[i] + b·cap[i].
+// When truncation ranks differ between instances the common bond dimension is the
+// largest kept rank and each instance's surplus singular values are set to zero before
+// √S is absorbed, so every instance carries exactly its own truncated state.
+//
 // Algorithms restated from Tenet.jl v0.10.3:
 //   gauge move            generic_canonize_site!       src/Operations/canonize.jl:23-76
 //   bond gauge move       generic_bond_canonize_site!  src/Operations/canonize.jl:78-116
@@ -22,32 +29,62 @@
 
 struct tn_mps {
   tn_ctx* ctx = nullptr;
-  int L = 0, d = 0;
-  std::vector<int64_t> bond;  // L+1 entries, bond[0] = bond[L] = 1
+  int L = 0, d = 0, B = 1;
+  std::vector<int64_t> bond;      // L+1 entries, bond[0] = bond[L] = 1
   std::vector<int64_t> cap_bond;  // storage caps per bond
-  std::vector<cxd*> site;     // 1-based: site[1..L]
-  std::vector<size_t> cap;    // elements reserved per site
+  std::vector<cxd*> site;         // 1-based: site[1..L], B instances each
+  std::vector<size_t> cap;        // elements reserved per site and instance (= instance stride)
   int kind = TN_FORM_MIXED, lo = 1, hi = 1;
-  double* lam = nullptr;      // Λ at the bond-canonical centre (device, FP64)
+  double* lam = nullptr;  // Λ at the bond-canonical centre, B instances at stride lam_cap
   int64_t lam_len = 0;
   size_t lam_cap = 0;
   tn_precision_t prec = TN_PREC_NATIVE;
-  cxd* gates = nullptr;       // device copy of gates for evolve
+  cxd* gates = nullptr;  // device copy of gates
   size_t gates_cap = 0;
 };
+
+// Output sizing callback of the gate core: called once the kept rank r is known; returns
+// where A' and B' go with their instance strides (it may grow and move buffers: the gate
+// inputs have been consumed by then).
+typedef tn_status_t (*su_out_fn)(void* arg, int64_t r, cxd** Aout, int64_t* sAout, cxd** Bout, int64_t* sBout);
 
 namespace {
 
 inline int64_t sz(const tn_mps* p, int i) { return p->bond[i - 1] * p->d * p->bond[i]; }
+
+const cxd kOne = {1.0, 0.0};
+const cxd kZero = {0.0, 0.0};
+
+// strided copy of B instances of `elems` elements
+tn_status_t copy_instances(tn_ctx* ctx, cxd* dst, size_t dst_stride, const cxd* src, size_t src_stride, size_t elems,
+                           int B) {
+  if (elems == 0 || B == 0) return TN_OK;
+  TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(dst, dst_stride * sizeof(cxd), src, src_stride * sizeof(cxd), elems * sizeof(cxd),
+                                       B, cudaMemcpyDeviceToDevice, ctx->stream));
+  return TN_OK;
+}
+
+__global__ void k_set_one(cxd* x, int64_t stride, int64_t B) {
+  for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < B; b += (int64_t)gridDim.x * blockDim.x) {
+    x[b * stride].x = 1.0;
+    x[b * stride].y = 0.0;
+  }
+}
+
+tn_status_t set_one(tn_ctx* ctx, cxd* x, int64_t stride, int64_t B) {
+  k_set_one<<<(unsigned)((B + 127) / 128), 128, 0, ctx->stream>>>(x, stride, B);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
 
 tn_status_t ensure_site(tn_mps* p, int i, size_t elems) {
   if (elems <= p->cap[i]) return TN_OK;
   tn_ctx* ctx = p->ctx;
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   void* np = nullptr;
-  TN_RETURN_IF(tn_dev_alloc(ctx, elems * sizeof(cxd), &np));
+  TN_RETURN_IF(tn_dev_alloc(ctx, elems * sizeof(cxd) * p->B, &np));
   if (p->site[i]) {
-    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(np, p->site[i], sizeof(cxd) * sz(p, i), cudaMemcpyDeviceToDevice, ctx->stream));
+    TN_RETURN_IF(copy_instances(ctx, (cxd*)np, elems, p->site[i], p->cap[i], (size_t)sz(p, i), p->B));
     TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     TN_RETURN_IF(tn_dev_free(ctx, p->site[i]));
   }
@@ -63,50 +100,48 @@ tn_status_t ensure_lam(tn_mps* p, int64_t n) {
   if (p->lam) TN_RETURN_IF(tn_dev_free(ctx, p->lam));
   void* np = nullptr;
   size_t c = std::max<size_t>(n, 64);
-  TN_RETURN_IF(tn_dev_alloc(ctx, c * sizeof(double), &np));
+  TN_RETURN_IF(tn_dev_alloc(ctx, c * sizeof(double) * p->B, &np));
   p->lam = (double*)np;
   p->lam_cap = c;
   return TN_OK;
 }
 
-const cxd kOne = {1.0, 0.0};
-const cxd kZero = {0.0, 0.0};
-
 // ---------------------------------------------------------------------------------
-// gauge moves (canonize.jl:23-116)
+// gauge moves (canonize.jl:23-116), all B instances at once
 // ---------------------------------------------------------------------------------
 
-// QR of site i across bond (i, i+1); R pushed into site i+1
+// factorise site i across bond (i, i+1) — QR, or SVD keeping Λ — and push the
+// non-isometric factor into site i+1
 tn_status_t gauge_right(tn_mps* p, int i, bool svd_lambda) {
   tn_ctx* ctx = p->ctx;
+  const int B = p->B;
   const int64_t chl = p->bond[i - 1], chr = p->bond[i], d = p->d;
   // size-1 bonds are skipped by the QR move (canonize.jl:38); the bond-canonical move
   // still factorises them so that a Λ of length 1 exists for norm / compress
   if (chr == 1 && !svd_lambda) return TN_OK;
   const int64_t m = chl * d, n = chr, k = std::min(m, n);
-  const int64_t chn = p->bond[i + 1];
-  const int64_t nb_cols = d * chn;  // columns of site i+1 as (χ_i × d χ_{i+1})
-  size_t need = ws_round(sizeof(cxd) * (size_t)(k * n)) + ws_round(sizeof(cxd) * (size_t)(k * nb_cols));
+  const int64_t nbc = d * p->bond[i + 1];  // columns of site i+1 as (χ_i × d χ_{i+1})
+  size_t need = ws_round(sizeof(cxd) * (size_t)(B * k * n)) + ws_round(sizeof(cxd) * (size_t)(B * k * nbc));
   if (svd_lambda)
-    need += ws_round(sizeof(cxd) * (size_t)(m * k)) + svd_any_workspace(TN_C64, p->prec, m, n, 1);
+    need += ws_round(sizeof(cxd) * (size_t)(B * m * k)) + svd_any_workspace(TN_C64, p->prec, m, n, B);
   else
-    need += qr_workspace<double>(m, n, 1);
+    need += qr_workspace<double>(m, n, B);
   TN_RETURN_IF(ws_reserve(ctx, need));
-  cxd* R = ws_take<cxd>(ctx, (size_t)(k * n));
-  cxd* tmp = ws_take<cxd>(ctx, (size_t)(k * nb_cols));
+  cxd* R = ws_take<cxd>(ctx, (size_t)(B * k * n));
+  cxd* tmp = ws_take<cxd>(ctx, (size_t)(B * k * nbc));
   if (svd_lambda) {
-    cxd* U = ws_take<cxd>(ctx, (size_t)(m * k));
+    cxd* U = ws_take<cxd>(ctx, (size_t)(B * m * k));
     TN_RETURN_IF(ensure_lam(p, k));
-    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, p->site[i], m, 0, U, 0, p->lam, 0, R, 0, 1));
-    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], U, sizeof(cxd) * m * k, cudaMemcpyDeviceToDevice, ctx->stream));
+    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, p->site[i], m, p->cap[i], U, m * k, p->lam, p->lam_cap, R, k * n, B));
+    TN_RETURN_IF(copy_instances(ctx, p->site[i], p->cap[i], U, m * k, m * k, B));
     p->lam_len = k;
   } else {
-    TN_RETURN_IF(qr_cx<double>(ctx, m, n, p->site[i], m, 0, p->site[i], 0, R, 0, 1));
+    TN_RETURN_IF(qr_cx<double>(ctx, m, n, p->site[i], m, p->cap[i], p->site[i], p->cap[i], R, k * n, B));
   }
-  // site i+1 ← R · B
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k, nb_cols, n, kOne, R, k, 0, p->site[i + 1], n, 0, kZero, tmp, k, 0, 1));
-  TN_RETURN_IF(ensure_site(p, i + 1, (size_t)(k * nb_cols)));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i + 1], tmp, sizeof(cxd) * k * nb_cols, cudaMemcpyDeviceToDevice, ctx->stream));
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k, nbc, n, kOne, R, k, k * n, p->site[i + 1], n, p->cap[i + 1], kZero, tmp,
+                               k, k * nbc, B));
+  TN_RETURN_IF(ensure_site(p, i + 1, (size_t)(k * nbc)));
+  TN_RETURN_IF(copy_instances(ctx, p->site[i + 1], p->cap[i + 1], tmp, k * nbc, k * nbc, B));
   p->bond[i] = k;
   return TN_OK;
 }
@@ -114,38 +149,34 @@ tn_status_t gauge_right(tn_mps* p, int i, bool svd_lambda) {
 // factorise site i across bond (i-1, i); the non-isometric part goes into site i-1
 tn_status_t gauge_left(tn_mps* p, int i, bool svd_lambda) {
   tn_ctx* ctx = p->ctx;
+  const int B = p->B;
   const int64_t chl = p->bond[i - 1], chr = p->bond[i], d = p->d;
   if (chl == 1 && !svd_lambda) return TN_OK;
   const int64_t m = d * chr, n = chl, k = std::min(m, n);  // Mᴴ is (d χ_r) × χ_l
-  const int64_t chp = p->bond[i - 2];
-  const int64_t rows_b = chp * d;  // site i-1 as (χ_{i-2} d × χ_{i-1})
-  size_t need = ws_round(sizeof(cxd) * (size_t)(m * n)) * 2 + ws_round(sizeof(cxd) * (size_t)(k * n)) +
-                ws_round(sizeof(cxd) * (size_t)(rows_b * k));
-  if (svd_lambda)
-    need += svd_any_workspace(TN_C64, p->prec, m, n, 1);
-  else
-    need += qr_workspace<double>(m, n, 1);
+  const int64_t rows_b = p->bond[i - 2] * d;                // site i-1 as (χ_{i-2} d × χ_{i-1})
+  size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(B * m * n)) + ws_round(sizeof(cxd) * (size_t)(B * k * n)) +
+                ws_round(sizeof(cxd) * (size_t)(B * rows_b * k));
+  need += svd_lambda ? svd_any_workspace(TN_C64, p->prec, m, n, B) : qr_workspace<double>(m, n, B);
   TN_RETURN_IF(ws_reserve(ctx, need));
-  cxd* Mh = ws_take<cxd>(ctx, (size_t)(m * n));
-  cxd* Q = ws_take<cxd>(ctx, (size_t)(m * n));
-  cxd* R = ws_take<cxd>(ctx, (size_t)(k * n));
-  cxd* tmp = ws_take<cxd>(ctx, (size_t)(rows_b * k));
-  // Mᴴ: site as (χ_l × d χ_r) matrix, conjugate-transposed
-  TN_RETURN_IF(transpose_cx<double>(ctx, n, m, p->site[i], n, 0, Mh, m, 0, 1, true));
+  cxd* Mh = ws_take<cxd>(ctx, (size_t)(B * m * n));
+  cxd* Q = ws_take<cxd>(ctx, (size_t)(B * m * n));
+  cxd* R = ws_take<cxd>(ctx, (size_t)(B * k * n));
+  cxd* tmp = ws_take<cxd>(ctx, (size_t)(B * rows_b * k));
+  TN_RETURN_IF(transpose_cx<double>(ctx, n, m, p->site[i], n, p->cap[i], Mh, m, m * n, B, true));
   if (svd_lambda) {
     TN_RETURN_IF(ensure_lam(p, k));
-    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, Mh, m, 0, Q, 0, p->lam, 0, R, 0, 1));
+    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, Mh, m, m * n, Q, m * n, p->lam, p->lam_cap, R, k * n, B));
     p->lam_len = k;
   } else {
-    TN_RETURN_IF(qr_cx<double>(ctx, m, n, Mh, m, 0, Q, 0, R, 0, 1));
+    TN_RETURN_IF(qr_cx<double>(ctx, m, n, Mh, m, m * n, Q, m * n, R, k * n, B));
   }
   // new site i = Qᴴ (k × d χ_r)
-  TN_RETURN_IF(transpose_cx<double>(ctx, m, k, Q, m, 0, p->site[i], k, 0, 1, true));
+  TN_RETURN_IF(transpose_cx<double>(ctx, m, k, Q, m, m * n, p->site[i], k, p->cap[i], B, true));
   // site i-1 ← B · Rᴴ
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'C', rows_b, k, n, kOne, p->site[i - 1], rows_b, 0, R, k, 0, kZero, tmp, rows_b,
-                               0, 1));
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'C', rows_b, k, n, kOne, p->site[i - 1], rows_b, p->cap[i - 1], R, k, k * n,
+                               kZero, tmp, rows_b, rows_b * k, B));
   TN_RETURN_IF(ensure_site(p, i - 1, (size_t)(rows_b * k)));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i - 1], tmp, sizeof(cxd) * rows_b * k, cudaMemcpyDeviceToDevice, ctx->stream));
+  TN_RETURN_IF(copy_instances(ctx, p->site[i - 1], p->cap[i - 1], tmp, rows_b * k, rows_b * k, B));
   p->bond[i - 1] = k;
   return TN_OK;
 }
@@ -158,7 +189,10 @@ tn_status_t absorb_lambda(tn_mps* p, int i, bool into_left_index) {
   if (dims[axis] != p->lam_len)
     return tn_set_error(ctx, TN_EINVAL, "absorb: Λ length %lld does not match bond %lld", (long long)p->lam_len,
                         (long long)dims[axis]);
-  return tn_hadamard(ctx, TN_C64, 3, dims, axis, p->site[i], p->lam, p->site[i]);
+  for (int b = 0; b < p->B; ++b)
+    TN_RETURN_IF(tn_hadamard(ctx, TN_C64, 3, dims, axis, p->site[i] + b * p->cap[i], p->lam + b * p->lam_cap,
+                             p->site[i] + b * p->cap[i]));
+  return TN_OK;
 }
 
 // ---------------------------------------------------------------------------------
@@ -180,6 +214,7 @@ tn_status_t mixed_to_mixed(tn_mps* p, int lo, int hi) {
 
 // SVD of `site` across bond (a, a+1) without absorbing Λ (canonize.jl:78-116)
 tn_status_t bond_gauge(tn_mps* p, int site, int a) {
+  p->lam_len = 0;
   if (site == a) return gauge_right(p, site, true);
   return gauge_left(p, site, true);
 }
@@ -253,46 +288,47 @@ tn_status_t canonize_mixed(tn_mps* p, int lo, int hi) {
   return mixed_to_mixed(p, lo, hi);
 }
 
-// ---------------------------------------------------------------------------------
-// simple update (simple_update.jl:20-92 + Muscle.simple_update with AbsorbEqually)
-// ---------------------------------------------------------------------------------
 }  // namespace
 
-// Output sizing callback: called once the kept rank r is known; returns where A' and B'
-// go (it may grow and move buffers; the gate inputs have been consumed by then).
-typedef tn_status_t (*su_out_fn)(void* arg, int64_t r, cxd** Aout, cxd** Bout);
-
-// θ = G·(A·B) → thin SVD → keep (maxdim, threshold) → A' = U√S, B' = √S Vh.
-// A (chl·d1 × chm), B (chm × d2·chr), G (d1 d2 × d1 d2) column-major.  Reserves the
-// workspace itself.
+// ---------------------------------------------------------------------------------
+// simple update core (Muscle.simple_update with AbsorbEqually), batched
+// A (chl·d1 × chm), B (chm × d2·chr), G (d1 d2 × d1 d2) column-major, instance strides
+// sA, sB; G shared by all instances.  Reserves the workspace itself.
+// ---------------------------------------------------------------------------------
 tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, int64_t d1, int64_t chm, int64_t d2,
-                               int64_t chr, const cxd* A, const cxd* B, const cxd* dG, int64_t maxdim, double threshold,
-                               su_out_fn out_fn, void* out_arg, double* Sout, int64_t* rank_out) {
+                               int64_t chr, const cxd* A, int64_t sA, const cxd* Bm, int64_t sB, const cxd* dG,
+                               int64_t maxdim, double threshold, int64_t batch, su_out_fn out_fn, void* out_arg,
+                               double* Sout, int64_t* rank_out) {
   const int64_t m = chl * d1, n = d2 * chr, k = std::min(m, n), dd = d1 * d2;
-  size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(m * n)) + ws_round(sizeof(cxd) * (size_t)(m * k)) +
-                ws_round(sizeof(double) * (size_t)k) + ws_round(sizeof(cxd) * (size_t)(k * n)) +
-                svd_any_workspace(TN_C64, prec, m, n, 1);
+  size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(batch * m * n)) + ws_round(sizeof(cxd) * (size_t)(batch * m * k)) +
+                ws_round(sizeof(double) * (size_t)(batch * k)) + ws_round(sizeof(cxd) * (size_t)(batch * k * n)) +
+                svd_any_workspace(TN_C64, prec, m, n, batch);
   TN_RETURN_IF(ws_reserve(ctx, need));
-  cxd* th0 = ws_take<cxd>(ctx, (size_t)(m * n));
-  cxd* th = ws_take<cxd>(ctx, (size_t)(m * n));
-  cxd* U = ws_take<cxd>(ctx, (size_t)(m * k));
-  double* S = ws_take<double>(ctx, (size_t)k);
-  cxd* Vh = ws_take<cxd>(ctx, (size_t)(k * n));
+  cxd* th0 = ws_take<cxd>(ctx, (size_t)(batch * m * n));
+  cxd* th = ws_take<cxd>(ctx, (size_t)(batch * m * n));
+  cxd* U = ws_take<cxd>(ctx, (size_t)(batch * m * k));
+  double* S = ws_take<double>(ctx, (size_t)(batch * k));
+  cxd* Vh = ws_take<cxd>(ctx, (size_t)(batch * k * n));
   // θ0 = A (χl d1 × χm) · B (χm × d2 χr)
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, chm, kOne, A, m, 0, B, chm, 0, kZero, th0, m, 0, 1));
-  // θ[l, (a b), r] = Σ G[(a b), (a' b')] θ0[l, (a' b'), r]  — batched over r
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, chm, kOne, A, m, sA, Bm, chm, sB, kZero, th0, m, m * n, batch));
+  // θ[l, (a b), r] = Σ G[(a b), (a' b')] θ0[l, (a' b'), r] — batched over (r, instance),
+  // which are contiguous blocks of chl·dd elements
   TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, dd, dd, kOne, th0, chl, chl * dd, dG, dd, 0, kZero, th, chl,
-                               chl * dd, chr));
-  TN_RETURN_IF(svd_any(ctx, TN_C64, prec, m, n, th, m, 0, U, 0, S, 0, Vh, 0, 1));
+                               chl * dd, chr * batch));
+  TN_RETURN_IF(svd_any(ctx, TN_C64, prec, m, n, th, m, m * n, U, m * k, S, k, Vh, k * n, batch));
   int64_t r = 0;
-  TN_RETURN_IF(rank_select(ctx, S, k, maxdim, threshold, &r));
+  TN_RETURN_IF(rank_select_batched(ctx, S, k, k, batch, maxdim, threshold, &r, nullptr));
   cxd *Aout = nullptr, *Bout = nullptr;
-  TN_RETURN_IF(out_fn(out_arg, r, &Aout, &Bout));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(Aout, U, sizeof(cxd) * m * r, cudaMemcpyDeviceToDevice, ctx->stream));
-  TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S));
-  TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r));
-  TN_RETURN_IF(scale_rows_sqrt<double>(ctx, Bout, r, n, r, S));
-  if (Sout) TN_CHECK_CUDA(ctx, cudaMemcpyAsync(Sout, S, sizeof(double) * r, cudaMemcpyDeviceToDevice, ctx->stream));
+  int64_t sAo = 0, sBo = 0;
+  TN_RETURN_IF(out_fn(out_arg, r, &Aout, &sAo, &Bout, &sBo));
+  // A' = U[:, :r] √S ; B' = √S Vh[:r, :]
+  TN_RETURN_IF(copy_matrix_cxd(ctx, m * r, 1, U, m * r, Aout, m * r, m * k, sAo, batch));
+  TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
+  TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
+  TN_RETURN_IF(scale_rows_sqrt<double>(ctx, Bout, r, n, r, S, sBo, k, batch));
+  if (Sout)
+    TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(Sout, sizeof(double) * r, S, sizeof(double) * k, sizeof(double) * r, batch,
+                                         cudaMemcpyDeviceToDevice, ctx->stream));
   *rank_out = r;
   return TN_OK;
 }
@@ -303,14 +339,16 @@ struct PairOut {
   tn_mps* p;
   int a;
 };
-tn_status_t pair_out(void* arg, int64_t r, cxd** Aout, cxd** Bout) {
+tn_status_t pair_out(void* arg, int64_t r, cxd** Aout, int64_t* sAo, cxd** Bout, int64_t* sBo) {
   PairOut* e = (PairOut*)arg;
   tn_mps* p = e->p;
   const int64_t m = p->bond[e->a - 1] * p->d, n = p->d * p->bond[e->a + 1];
   TN_RETURN_IF(ensure_site(p, e->a, (size_t)(m * r)));
   TN_RETURN_IF(ensure_site(p, e->a + 1, (size_t)(r * n)));
   *Aout = p->site[e->a];
+  *sAo = p->cap[e->a];
   *Bout = p->site[e->a + 1];
+  *sBo = p->cap[e->a + 1];
   return TN_OK;
 }
 
@@ -319,21 +357,22 @@ tn_status_t apply_gate2(tn_mps* p, int a, const cxd* dG, int64_t maxdim, double 
   PairOut e{p, a};
   int64_t r = 0;
   TN_RETURN_IF(simple_update_core(p->ctx, p->prec, p->bond[a - 1], d, p->bond[a], d, p->bond[a + 1], p->site[a],
-                                  p->site[a + 1], dG, maxdim, threshold, pair_out, &e, nullptr, &r));
+                                  p->cap[a], p->site[a + 1], p->cap[a + 1], dG, maxdim, threshold, p->B, pair_out, &e,
+                                  nullptr, &r));
   p->bond[a] = r;
   return TN_OK;
 }
 
 tn_status_t apply_gate1(tn_mps* p, int i, const cxd* dG) {
   tn_ctx* ctx = p->ctx;
-  const int64_t d = p->d, chl = p->bond[i - 1], chr = p->bond[i];
-  TN_RETURN_IF(ws_reserve(ctx, ws_round(sizeof(cxd) * (size_t)(chl * d * chr))));
-  cxd* tmp = ws_take<cxd>(ctx, (size_t)(chl * d * chr));
-  // new[l, a, r] = Σ_b G[a, b] A[l, b, r]  (batched over r)
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, d, d, kOne, p->site[i], chl, chl * d, dG, d, 0, kZero, tmp, chl,
-                               chl * d, chr));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], tmp, sizeof(cxd) * chl * d * chr, cudaMemcpyDeviceToDevice, ctx->stream));
-  return TN_OK;
+  const int64_t d = p->d, chl = p->bond[i - 1], chr = p->bond[i], e = chl * d * chr;
+  TN_RETURN_IF(ws_reserve(ctx, ws_round(sizeof(cxd) * (size_t)(p->B * e))));
+  cxd* tmp = ws_take<cxd>(ctx, (size_t)(p->B * e));
+  // new[l, a, r] = Σ_b G[a, b] A[l, b, r]  (batched over r within each instance)
+  for (int b = 0; b < p->B; ++b)
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, d, d, kOne, p->site[i] + b * p->cap[i], chl, chl * d, dG, d, 0,
+                                 kZero, tmp + b * e, chl, chl * d, chr));
+  return copy_instances(ctx, p->site[i], p->cap[i], tmp, e, e, p->B);
 }
 
 tn_status_t upload_gates(tn_mps* p, const void* h, size_t elems) {
@@ -351,85 +390,38 @@ tn_status_t upload_gates(tn_mps* p, const void* h, size_t elems) {
 }
 
 // ---------------------------------------------------------------------------------
-// environments (overlap.jl:36-50): F (χb × χa) ← Bᴴ · (F · A)
+// environments (overlap.jl:36-50): F (χb × χa) ← Bᴴ · (F · A), all instances
 // ---------------------------------------------------------------------------------
-tn_status_t overlap_impl(const tn_mps* a, const tn_mps* b, cxd* out) {
+tn_status_t overlap_impl(const tn_mps* a, const tn_mps* b, double* h_out) {
   tn_ctx* ctx = a->ctx;
-  const int L = a->L, d = a->d;
+  const int L = a->L, d = a->d, B = a->B;
   int64_t mx = 1;
   for (int i = 0; i <= L; ++i) mx = std::max({mx, a->bond[i], b->bond[i]});
-  size_t env = (size_t)(mx * mx), t = (size_t)(mx * d * mx);
-  TN_RETURN_IF(ws_reserve(ctx, 2 * ws_round(sizeof(cxd) * env) + ws_round(sizeof(cxd) * t)));
-  cxd* F = ws_take<cxd>(ctx, env);
-  cxd* F2 = ws_take<cxd>(ctx, env);
-  cxd* T = ws_take<cxd>(ctx, t);
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(F, &kOne, sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
+  const size_t env = (size_t)(mx * mx), t = (size_t)(mx * d * mx);
+  TN_RETURN_IF(ws_reserve(ctx, 2 * ws_round(sizeof(cxd) * env * B) + ws_round(sizeof(cxd) * t * B)));
+  cxd* F = ws_take<cxd>(ctx, env * B);
+  cxd* F2 = ws_take<cxd>(ctx, env * B);
+  cxd* T = ws_take<cxd>(ctx, t * B);
+  TN_RETURN_IF(set_one(ctx, F, env, B));
   for (int i = 1; i <= L; ++i) {
     const int64_t xa = a->bond[i - 1], xa2 = a->bond[i], yb = b->bond[i - 1], yb2 = b->bond[i];
     // T (yb × d xa2) = F (yb × xa) · A (xa × d xa2)
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', yb, d * xa2, xa, kOne, F, yb, 0, a->site[i], xa, 0, kZero, T, yb, 0, 1));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', yb, d * xa2, xa, kOne, F, yb, env, a->site[i], xa, a->cap[i], kZero, T,
+                                 yb, t, B));
     // F2 (yb2 × xa2) = B_matᴴ ((yb d) × yb2)ᴴ · T ((yb d) × xa2)
-    TN_RETURN_IF(
-        gemm_cx<double>(ctx, 'C', 'N', yb2, xa2, yb * d, kOne, b->site[i], yb * d, 0, T, yb * d, 0, kZero, F2, yb2, 0, 1));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', yb2, xa2, yb * d, kOne, b->site[i], yb * d, b->cap[i], T, yb * d, t,
+                                 kZero, F2, yb2, env, B));
     std::swap(F, F2);
   }
-  cxd* hp = reinterpret_cast<cxd*>(ctx->pinned);
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, F, sizeof(cxd), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(h_out, sizeof(cxd), F, env * sizeof(cxd), sizeof(cxd), B, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  *out = hp[0];
   return TN_OK;
 }
 
-__global__ void k_zdotc_partial(int64_t n, const cxd* __restrict__ x, const cxd* __restrict__ y, double* partial) {
-  __shared__ double rx[32], ry[32];
-  cxd s = {0, 0};
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    cfma_cj(s, x[i], y[i]);
-  s.x = warp_sum(s.x);
-  s.y = warp_sum(s.y);
-  if ((threadIdx.x & 31) == 0) {
-    rx[threadIdx.x >> 5] = s.x;
-    ry[threadIdx.x >> 5] = s.y;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    double vx = threadIdx.x < (blockDim.x >> 5) ? rx[threadIdx.x] : 0.0;
-    double vy = threadIdx.x < (blockDim.x >> 5) ? ry[threadIdx.x] : 0.0;
-    vx = warp_sum(vx);
-    vy = warp_sum(vy);
-    if (threadIdx.x == 0) {
-      partial[2 * blockIdx.x] = vx;
-      partial[2 * blockIdx.x + 1] = vy;
-    }
-  }
-}
-__global__ void k_zsum_final(int n, const double* partial, double* out) {
-  if (threadIdx.x == 0) {
-    double sx = 0, sy = 0;
-    for (int i = 0; i < n; ++i) {
-      sx += partial[2 * i];
-      sy += partial[2 * i + 1];
-    }
-    out[0] = sx;
-    out[1] = sy;
-  }
-}
-
-// Σ conj(x)·y in FP64, fixed reduction order
-tn_status_t zdotc(tn_ctx* ctx, int64_t n, const cxd* x, const cxd* y, cxd* out) {
-  int* flags = nullptr;
-  const int nb = 64;
-  TN_RETURN_IF(ctx_flags(ctx, 4 * nb + 8, &flags));
-  double* part = reinterpret_cast<double*>(flags);
-  k_zdotc_partial<<<nb, 256, 0, ctx->stream>>>(n, x, y, part);
-  TN_LAUNCHED(ctx);
-  k_zsum_final<<<1, 32, 0, ctx->stream>>>(nb, part, part + 2 * nb);
-  TN_LAUNCHED(ctx);
-  double* hp = reinterpret_cast<double*>(ctx->pinned);
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, part + 2 * nb, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  out->x = hp[0];
-  out->y = hp[1];
+tn_status_t check_site_arg(const tn_mps* p, int32_t b, int32_t i) {
+  if (b < 0 || b >= p->B) return tn_set_error(p->ctx, TN_EINVAL, "instance %d out of range (B=%d)", b, p->B);
+  if (i < 1 || i > p->L) return tn_set_error(p->ctx, TN_EINVAL, "site %d out of range", i);
   return TN_OK;
 }
 
@@ -440,15 +432,17 @@ tn_status_t zdotc(tn_ctx* ctx, int64_t n, const cxd* x, const cxd* y, cxd* out) 
 // ---------------------------------------------------------------------------------
 extern "C" {
 
-tn_status_t tn_mps_create(tn_ctx* ctx, int32_t L, int32_t d, const int64_t* bond_dims, int64_t max_bond,
-                          tn_precision_t prec, tn_mps** out) {
+tn_status_t tn_mps_create_batched(tn_ctx* ctx, int32_t B, int32_t L, int32_t d, const int64_t* bond_dims,
+                                  int64_t max_bond, tn_precision_t prec, tn_mps** out) {
   if (!ctx) return TN_EINVAL;
   TN_ARG(ctx, L >= 2 && d >= 1 && out, "tn_mps_create: need L >= 2, d >= 1");
+  TN_ARG(ctx, B >= 1 && B <= 8192, "tn_mps_create: batch must be in 1..8192");
   TN_ARG(ctx, bond_dims != nullptr, "tn_mps_create: null bond_dims");
   tn_mps* p = new tn_mps();
   p->ctx = ctx;
   p->L = L;
   p->d = d;
+  p->B = B;
   p->prec = prec;
   p->bond.assign(L + 1, 1);
   p->cap_bond.assign(L + 1, 1);
@@ -475,12 +469,24 @@ tn_status_t tn_mps_create(tn_ctx* ctx, int32_t L, int32_t d, const int64_t* bond
       delete p;
       return st;
     }
-    TN_CHECK_CUDA(ctx, cudaMemsetAsync(p->site[i], 0, e * sizeof(cxd), ctx->stream));
+    TN_CHECK_CUDA(ctx, cudaMemsetAsync(p->site[i], 0, e * B * sizeof(cxd), ctx->stream));
   }
   p->kind = TN_FORM_MIXED;
   p->lo = 1;
   p->hi = L;
+  ctx->refs++;
   *out = p;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_create(tn_ctx* ctx, int32_t L, int32_t d, const int64_t* bond_dims, int64_t max_bond,
+                          tn_precision_t prec, tn_mps** out) {
+  return tn_mps_create_batched(ctx, 1, L, d, bond_dims, max_bond, prec, out);
+}
+
+tn_status_t tn_mps_batch_size(const tn_mps* p, int32_t* B) {
+  if (!p || !B) return TN_EINVAL;
+  *B = p->B;
   return TN_OK;
 }
 
@@ -493,6 +499,7 @@ tn_status_t tn_mps_destroy(tn_mps* p) {
   if (p->lam) tn_dev_free(ctx, p->lam);
   if (p->gates) tn_dev_free(ctx, p->gates);
   delete p;
+  if (--ctx->refs == 0 && ctx->destroy_requested) ctx_release(ctx);
   return TN_OK;
 }
 
@@ -501,15 +508,14 @@ tn_status_t tn_mps_copy(const tn_mps* src, tn_mps** out) {
   tn_ctx* ctx = src->ctx;
   std::vector<int64_t> b(src->bond.begin() + 1, src->bond.end() - 1);
   tn_mps* p = nullptr;
-  TN_RETURN_IF(tn_mps_create(ctx, src->L, src->d, b.data(), 0, src->prec, &p));
+  TN_RETURN_IF(tn_mps_create_batched(ctx, src->B, src->L, src->d, b.data(), 0, src->prec, &p));
   for (int i = 1; i <= src->L; ++i) {
     tn_status_t st = ensure_site(p, i, src->cap[i]);
+    if (st == TN_OK) st = copy_instances(ctx, p->site[i], p->cap[i], src->site[i], src->cap[i], (size_t)sz(src, i), src->B);
     if (st != TN_OK) {
       tn_mps_destroy(p);
       return st;
     }
-    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], src->site[i], sizeof(cxd) * sz(src, i), cudaMemcpyDeviceToDevice,
-                                       ctx->stream));
   }
   p->cap_bond = src->cap_bond;
   p->kind = src->kind;
@@ -517,35 +523,45 @@ tn_status_t tn_mps_copy(const tn_mps* src, tn_mps** out) {
   p->hi = src->hi;
   if (src->lam_len > 0) {
     TN_RETURN_IF(ensure_lam(p, src->lam_len));
-    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->lam, src->lam, sizeof(double) * src->lam_len, cudaMemcpyDeviceToDevice,
-                                       ctx->stream));
+    TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(p->lam, p->lam_cap * sizeof(double), src->lam, src->lam_cap * sizeof(double),
+                                         src->lam_len * sizeof(double), src->B, cudaMemcpyDeviceToDevice, ctx->stream));
     p->lam_len = src->lam_len;
   }
   *out = p;
   return TN_OK;
 }
 
-tn_status_t tn_mps_set_site(tn_mps* p, int32_t i, int64_t chl, int64_t chr, const void* h) {
+tn_status_t tn_mps_set_instance_site(tn_mps* p, int32_t b, int32_t i, int64_t chl, int64_t chr, const void* h) {
   if (!p) return TN_EINVAL;
   tn_ctx* ctx = p->ctx;
-  TN_ARG(ctx, i >= 1 && i <= p->L && h, "tn_mps_set_site: bad site");
+  TN_RETURN_IF(check_site_arg(p, b, i));
+  TN_ARG(ctx, h != nullptr, "tn_mps_set_site: null data");
   TN_ARG(ctx, (i > 1 || chl == 1) && (i < p->L || chr == 1), "tn_mps_set_site: open-end bonds must be 1");
   TN_ARG(ctx, chl == p->bond[i - 1] && chr == p->bond[i],
          "tn_mps_set_site: bond dimensions differ from the MPS's (set them at creation)");
   TN_RETURN_IF(ensure_site(p, i, (size_t)(chl * p->d * chr)));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], h, sizeof(cxd) * chl * p->d * chr, cudaMemcpyHostToDevice, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i] + (size_t)b * p->cap[i], h, sizeof(cxd) * chl * p->d * chr,
+                                     cudaMemcpyHostToDevice, ctx->stream));
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return TN_OK;
 }
 
-tn_status_t tn_mps_get_site(const tn_mps* p, int32_t i, void* h) {
+tn_status_t tn_mps_get_instance_site(const tn_mps* p, int32_t b, int32_t i, void* h) {
   if (!p) return TN_EINVAL;
   tn_ctx* ctx = p->ctx;
-  TN_ARG(ctx, i >= 1 && i <= p->L && h, "tn_mps_get_site: bad site");
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h, p->site[i], sizeof(cxd) * sz(p, i), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_RETURN_IF(check_site_arg(p, b, i));
+  TN_ARG(ctx, h != nullptr, "tn_mps_get_site: null output");
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h, p->site[i] + (size_t)b * p->cap[i], sizeof(cxd) * sz(p, i),
+                                     cudaMemcpyDeviceToHost, ctx->stream));
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return TN_OK;
 }
+
+tn_status_t tn_mps_set_site(tn_mps* p, int32_t i, int64_t chl, int64_t chr, const void* h) {
+  return tn_mps_set_instance_site(p, 0, i, chl, chr, h);
+}
+
+tn_status_t tn_mps_get_site(const tn_mps* p, int32_t i, void* h) { return tn_mps_get_instance_site(p, 0, i, h); }
 
 tn_status_t tn_mps_bond_dims(const tn_mps* p, int64_t* h) {
   if (!p || !h) return TN_EINVAL;
@@ -585,7 +601,8 @@ tn_status_t tn_mps_get_lambda(const tn_mps* p, double* h, int64_t* len) {
   TN_ARG(ctx, p->kind == TN_FORM_BOND, "tn_mps_get_lambda: MPS is not bond-canonical");
   *len = p->lam_len;
   if (h && p->lam_len > 0) {
-    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h, p->lam, sizeof(double) * p->lam_len, cudaMemcpyDeviceToHost, ctx->stream));
+    TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(h, sizeof(double) * p->lam_len, p->lam, sizeof(double) * p->lam_cap,
+                                         sizeof(double) * p->lam_len, p->B, cudaMemcpyDeviceToHost, ctx->stream));
     TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   }
   return TN_OK;
@@ -614,17 +631,18 @@ tn_status_t tn_mps_compress(tn_mps* p, int32_t a, int64_t maxdim, double thresho
     return TN_OK;
   }
   TN_RETURN_IF(canonize_bond(p, a));
-  if (p->lam_len == 0) return TN_OK;  // size-1 bond: no Λ was produced
-  int64_t k = p->lam_len, r = 0;
-  TN_RETURN_IF(rank_select(ctx, p->lam, k, maxdim, threshold, &r));
+  if (p->lam_len == 0) return TN_OK;
+  const int64_t k = p->lam_len;
+  int64_t r = 0;
+  TN_RETURN_IF(rank_select_batched(ctx, p->lam, k, p->lam_cap, p->B, maxdim, threshold, &r, nullptr));
   if (r == k) return TN_OK;
-  // site a (χl d × k): keep the first r columns in place (column-major prefix)
-  // site a+1 (k × d χr): keep the first r rows
+  // site a (χl d × k): the first r columns are a column-major prefix; site a+1 (k × d χr)
+  // keeps its first r rows
   const int64_t n = p->d * p->bond[a + 1];
-  TN_RETURN_IF(ws_reserve(ctx, ws_round(sizeof(cxd) * (size_t)(r * n))));
-  cxd* tmp = ws_take<cxd>(ctx, (size_t)(r * n));
-  TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, p->site[a + 1], k, tmp, r));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[a + 1], tmp, sizeof(cxd) * r * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  TN_RETURN_IF(ws_reserve(ctx, ws_round(sizeof(cxd) * (size_t)(p->B * r * n))));
+  cxd* tmp = ws_take<cxd>(ctx, (size_t)(p->B * r * n));
+  TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, p->site[a + 1], k, tmp, r, p->cap[a + 1], r * n, p->B));
+  TN_RETURN_IF(copy_instances(ctx, p->site[a + 1], p->cap[a + 1], tmp, r * n, r * n, p->B));
   p->bond[a] = r;
   p->lam_len = r;
   return TN_OK;
@@ -652,7 +670,8 @@ tn_status_t tn_mps_evolve_brickwork(tn_mps* p, int32_t n_layers, const int32_t* 
   size_t total = 0;
   const size_t g4 = (size_t)p->d * p->d * p->d * p->d;
   for (int l = 0; l < n_layers; ++l) {
-    TN_ARG(ctx, n_gates[l] >= 0 && starts[l] >= 1 && starts[l] + 2 * n_gates[l] - 1 <= p->L, "evolve: layer out of range");
+    TN_ARG(ctx, n_gates[l] >= 0 && starts[l] >= 1 && starts[l] + 2 * n_gates[l] - 1 <= p->L,
+           "evolve: layer out of range");
     total += (size_t)n_gates[l] * g4;
   }
   if (total == 0) return TN_OK;
@@ -672,14 +691,11 @@ tn_status_t tn_mps_evolve_brickwork(tn_mps* p, int32_t n_layers, const int32_t* 
 tn_status_t tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* h_out) {
   if (!a || !b || !h_out) return TN_EINVAL;
   TN_ARG(a->ctx, a->L == b->L && a->d == b->d, "overlap: nsites differ");
+  TN_ARG(a->ctx, a->B == b->B, "overlap: batch sizes differ");
   TN_ARG(a->ctx, a->ctx == b->ctx, "overlap: MPS belong to different contexts");
   TN_ARG(a->ctx, a->kind != TN_FORM_BOND && b->kind != TN_FORM_BOND,
          "overlap: absorb Λ first (canonize the MPS to a mixed form)");
-  cxd v;
-  TN_RETURN_IF(overlap_impl(a, b, &v));
-  h_out[0] = v.x;
-  h_out[1] = v.y;
-  return TN_OK;
+  return overlap_impl(a, b, h_out);
 }
 
 tn_status_t tn_mps_norm(tn_mps* p, double* h_out) {
@@ -690,53 +706,53 @@ tn_status_t tn_mps_norm(tn_mps* p, double* h_out) {
     p->lo = 1;
     p->hi = p->L;
   }
-  if (p->kind == TN_FORM_BOND) {
-    int64_t n = p->lam_len;
-    double ss = 0;
-    TN_RETURN_IF(tn_norm2(ctx, TN_F64, n, p->lam, &ss));
-    *h_out = ss;
-    return TN_OK;
-  }
+  if (p->kind == TN_FORM_BOND) return norms_batched(ctx, false, p->lam_len, p->lam, p->lam_cap, p->B, h_out);
   const int c = p->lo;
   TN_RETURN_IF(canonize_mixed(p, c, c));
-  return norm2_cxd(ctx, sz(p, c), p->site[c], h_out);
+  return norms_batched(ctx, true, sz(p, c), p->site[c], p->cap[c], p->B, h_out);
 }
 
 tn_status_t tn_mps_normalize(tn_mps* p) {
   if (!p) return TN_EINVAL;
   tn_ctx* ctx = p->ctx;
-  double nrm = 0;
-  TN_RETURN_IF(tn_mps_norm(p, &nrm));
-  TN_ARG(ctx, nrm > 0, "normalize: zero norm");
-  if (p->kind == TN_FORM_BOND) return tn_scale(ctx, TN_F64, p->lam_len, p->lam, 1.0 / nrm);
-  return tn_scale(ctx, TN_C64, sz(p, p->lo), p->site[p->lo], 1.0 / nrm);
+  std::vector<double> nrm(p->B);
+  TN_RETURN_IF(tn_mps_norm(p, nrm.data()));
+  for (int b = 0; b < p->B; ++b) {
+    TN_ARG(ctx, nrm[b] > 0, "normalize: zero norm");
+    if (p->kind == TN_FORM_BOND)
+      TN_RETURN_IF(tn_scale(ctx, TN_F64, p->lam_len, p->lam + b * p->lam_cap, 1.0 / nrm[b]));
+    else
+      TN_RETURN_IF(tn_scale(ctx, TN_C64, sz(p, p->lo), p->site[p->lo] + b * p->cap[p->lo], 1.0 / nrm[b]));
+  }
+  return TN_OK;
 }
 
 tn_status_t tn_mps_amplitude(const tn_mps* p, const void* h_vectors, double* h_out) {
   if (!p || !h_vectors || !h_out) return TN_EINVAL;
   tn_ctx* ctx = p->ctx;
   TN_ARG(ctx, p->kind != TN_FORM_BOND, "amplitude: absorb Λ first (canonize the MPS to a mixed form)");
-  const int L = p->L, d = p->d;
+  const int L = p->L, d = p->d, B = p->B;
   int64_t mx = 1;
   for (int i = 0; i <= L; ++i) mx = std::max(mx, p->bond[i]);
-  TN_RETURN_IF(ws_reserve(ctx, 2 * ws_round(sizeof(cxd) * (size_t)(mx * d)) + ws_round(sizeof(cxd) * (size_t)(L * d))));
-  cxd* e = ws_take<cxd>(ctx, (size_t)(mx * d));
-  cxd* u = ws_take<cxd>(ctx, (size_t)(mx * d));
+  const size_t ve = (size_t)(mx * d);
+  TN_RETURN_IF(ws_reserve(ctx, 2 * ws_round(sizeof(cxd) * ve * B) + ws_round(sizeof(cxd) * (size_t)(L * d))));
+  cxd* e = ws_take<cxd>(ctx, ve * B);
+  cxd* u = ws_take<cxd>(ctx, ve * B);
   cxd* v = ws_take<cxd>(ctx, (size_t)(L * d));
   TN_CHECK_CUDA(ctx, cudaMemcpyAsync(v, h_vectors, sizeof(cxd) * L * d, cudaMemcpyHostToDevice, ctx->stream));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(e, &kOne, sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
+  TN_RETURN_IF(set_one(ctx, e, ve, B));
   for (int i = 1; i <= L; ++i) {
     const int64_t xl = p->bond[i - 1], xr = p->bond[i];
     // u (1 × d xr) = e (1 × xl) · A (xl × d xr)
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', 1, d * xr, xl, kOne, e, 1, 0, p->site[i], xl, 0, kZero, u, 1, 0, 1));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', 1, d * xr, xl, kOne, e, 1, ve, p->site[i], xl, p->cap[i], kZero, u, 1,
+                                 ve, B));
     // e (1 × xr) = vᵀ (1 × d) · u as (d × xr)
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'T', 'N', 1, xr, d, kOne, v + (int64_t)(i - 1) * d, d, 0, u, d, 0, kZero, e, 1, 0, 1));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'T', 'N', 1, xr, d, kOne, v + (int64_t)(i - 1) * d, d, 0, u, d, ve, kZero, e, 1,
+                                 ve, B));
   }
-  cxd* hp = reinterpret_cast<cxd*>(ctx->pinned);
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, e, sizeof(cxd), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(h_out, sizeof(cxd), e, ve * sizeof(cxd), sizeof(cxd), B, cudaMemcpyDeviceToHost,
+                                       ctx->stream));
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  h_out[0] = hp[0].x;
-  h_out[1] = hp[0].y;
   return TN_OK;
 }
 
@@ -744,67 +760,76 @@ tn_status_t tn_mps_local_expectations(const tn_mps* p, const void* h_op, double*
   if (!p || !h_op || !h_out) return TN_EINVAL;
   tn_ctx* ctx = p->ctx;
   TN_ARG(ctx, p->kind != TN_FORM_BOND, "expectation: absorb Λ first (canonize the MPS to a mixed form)");
-  const int L = p->L, d = p->d;
+  const int L = p->L, d = p->d, B = p->B;
   int64_t mx = 1;
   for (int i = 0; i <= L; ++i) mx = std::max(mx, p->bond[i]);
-  // left envs F_0..F_{L-1} and right envs R_2..R_{L+1}, each ≤ mx², plus scratch
+  // right environments R_2..R_{L+1} kept; the left environment is swept
   const size_t env = (size_t)(mx * mx), t = (size_t)(mx * d * mx);
-  size_t need = 2 * (size_t)(L + 2) * ws_round(sizeof(cxd) * env) + 3 * ws_round(sizeof(cxd) * t) +
+  size_t need = (size_t)(L + 4) * ws_round(sizeof(cxd) * env * B) + 3 * ws_round(sizeof(cxd) * t * B) +
                 ws_round(sizeof(cxd) * (size_t)(d * d));
   TN_RETURN_IF(ws_reserve(ctx, need));
-  std::vector<cxd*> F(L + 2), R(L + 2);
-  for (int i = 0; i <= L + 1; ++i) F[i] = ws_take<cxd>(ctx, env);
-  for (int i = 0; i <= L + 1; ++i) R[i] = ws_take<cxd>(ctx, env);
-  cxd* T1 = ws_take<cxd>(ctx, t);
-  cxd* T2 = ws_take<cxd>(ctx, t);
-  cxd* OA = ws_take<cxd>(ctx, t);
+  std::vector<cxd*> R(L + 2);
+  for (int i = 0; i <= L + 1; ++i) R[i] = ws_take<cxd>(ctx, env * B);
+  cxd* F = ws_take<cxd>(ctx, env * B);
+  cxd* F2 = ws_take<cxd>(ctx, env * B);
+  cxd* T1 = ws_take<cxd>(ctx, t * B);
+  cxd* T2 = ws_take<cxd>(ctx, t * B);
+  cxd* OA = ws_take<cxd>(ctx, t * B);
   cxd* dO = ws_take<cxd>(ctx, (size_t)(d * d));
   TN_CHECK_CUDA(ctx, cudaMemcpyAsync(dO, h_op, sizeof(cxd) * d * d, cudaMemcpyHostToDevice, ctx->stream));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(F[0], &kOne, sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(R[L + 1], &kOne, sizeof(cxd), cudaMemcpyHostToDevice, ctx->stream));
-  for (int i = 1; i < L; ++i) {
-    const int64_t x = p->bond[i - 1], x2 = p->bond[i];
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', x, d * x2, x, kOne, F[i - 1], x, 0, p->site[i], x, 0, kZero, T1, x, 0, 1));
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', x2, x2, x * d, kOne, p->site[i], x * d, 0, T1, x * d, 0, kZero, F[i], x2,
-                                 0, 1));
-  }
+  TN_RETURN_IF(set_one(ctx, F, env, B));
+  TN_RETURN_IF(set_one(ctx, R[L + 1], env, B));
   for (int i = L; i > 1; --i) {
     const int64_t x = p->bond[i - 1], x2 = p->bond[i];
     // T1 (x d × x2) = A (x d × x2) · R_{i+1} (x2 × x2)
-    TN_RETURN_IF(
-        gemm_cx<double>(ctx, 'N', 'N', x * d, x2, x2, kOne, p->site[i], x * d, 0, R[i + 1], x2, 0, kZero, T1, x * d, 0, 1));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', x * d, x2, x2, kOne, p->site[i], x * d, p->cap[i], R[i + 1], x2, env,
+                                 kZero, T1, x * d, t, B));
     // R_i (x × x) = T1 as (x × d x2) · A as (x × d x2)ᴴ
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'C', x, x, d * x2, kOne, T1, x, 0, p->site[i], x, 0, kZero, R[i], x, 0, 1));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'C', x, x, d * x2, kOne, T1, x, t, p->site[i], x, p->cap[i], kZero, R[i], x,
+                                 env, B));
   }
-  cxd nrm = {0, 0};
+  std::vector<double> val(2 * B), nrm(2 * B);
   for (int i = 1; i <= L; ++i) {
     const int64_t x = p->bond[i - 1], x2 = p->bond[i];
     for (int pass = 0; pass < (i == 1 ? 2 : 1); ++pass) {
       const cxd* Ain = p->site[i];
+      int64_t sAin = p->cap[i];
       if (pass == 0) {
         // OA[l, a, r] = Σ_b O[a, b] A[l, b, r]
-        TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', x, d, d, kOne, p->site[i], x, x * d, dO, d, 0, kZero, OA, x, x * d, x2));
+        for (int b = 0; b < B; ++b)
+          TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', x, d, d, kOne, p->site[i] + b * p->cap[i], x, x * d, dO, d, 0,
+                                       kZero, OA + b * t, x, x * d, x2));
         Ain = OA;
+        sAin = t;
       }
-      TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', x, d * x2, x, kOne, F[i - 1], x, 0, Ain, x, 0, kZero, T1, x, 0, 1));
-      TN_RETURN_IF(
-          gemm_cx<double>(ctx, 'N', 'N', x * d, x2, x2, kOne, T1, x * d, 0, R[i + 1], x2, 0, kZero, T2, x * d, 0, 1));
-      cxd val;
-      TN_RETURN_IF(zdotc(ctx, x * d * x2, p->site[i], T2, &val));
-      if (pass == 0) {
-        h_out[2 * (i - 1)] = val.x;
-        h_out[2 * (i - 1) + 1] = val.y;
-      } else {
-        nrm = val;
-      }
+      TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', x, d * x2, x, kOne, F, x, env, Ain, x, sAin, kZero, T1, x, t, B));
+      TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', x * d, x2, x2, kOne, T1, x * d, t, R[i + 1], x2, env, kZero, T2, x * d,
+                                   t, B));
+      TN_RETURN_IF(zdotc_batched(ctx, x * d * x2, p->site[i], p->cap[i], T2, t, B, pass == 0 ? val.data() : nrm.data()));
+      if (pass == 0)
+        for (int b = 0; b < B; ++b) {
+          h_out[2 * ((size_t)b * L + i - 1)] = val[2 * b];
+          h_out[2 * ((size_t)b * L + i - 1) + 1] = val[2 * b + 1];
+        }
+    }
+    if (i < L) {
+      // F ← Aᴴ · (F · A)
+      TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', x, d * x2, x, kOne, F, x, env, p->site[i], x, p->cap[i], kZero, T1, x,
+                                   t, B));
+      TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', x2, x2, x * d, kOne, p->site[i], x * d, p->cap[i], T1, x * d, t, kZero,
+                                   F2, x2, env, B));
+      std::swap(F, F2);
     }
   }
-  // divide by ⟨ψ|ψ⟩
-  double nn = nrm.x * nrm.x + nrm.y * nrm.y;
-  for (int i = 0; i < L; ++i) {
-    double a = h_out[2 * i], b = h_out[2 * i + 1];
-    h_out[2 * i] = (a * nrm.x + b * nrm.y) / nn;
-    h_out[2 * i + 1] = (b * nrm.x - a * nrm.y) / nn;
+  // divide by ⟨ψ|ψ⟩ per instance
+  for (int b = 0; b < B; ++b) {
+    const double nx = nrm[2 * b], ny = nrm[2 * b + 1], nn = nx * nx + ny * ny;
+    for (int i = 0; i < L; ++i) {
+      double* o = h_out + 2 * ((size_t)b * L + i);
+      const double a = o[0], c = o[1];
+      o[0] = (a * nx + c * ny) / nn;
+      o[1] = (c * nx - a * ny) / nn;
+    }
   }
   return TN_OK;
 }

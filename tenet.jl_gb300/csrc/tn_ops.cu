@@ -25,33 +25,46 @@ struct MulC32 {
   __device__ static float2 mul(float2 x, double s) { return make_float2((float)(x.x * s), (float)(x.y * s)); }
 };
 
-// out(r, c) = X(r, c) * sqrt(S[c])   (rows × cols, ld in and out)
+// X_b(r, c) *= sqrt(S_b[c])   (rows × cols, ld; batch strides sX, sS)
 template <typename T>
-__global__ void k_scale_cols_sqrt(cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = t % rows, c = t / rows;
-    X[r + c * ld] = T(sqrt(S[c])) * X[r + c * ld];
-  }
+__global__ void k_scale_cols_sqrt(cx<T>* X, int64_t rows, int64_t cols, int64_t ld, int64_t sX, const double* S,
+                                  int64_t sS, int64_t batch) {
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
+      int64_t r = t % rows, c = t / rows;
+      X[b * sX + r + c * ld] = T(sqrt(S[b * sS + c])) * X[b * sX + r + c * ld];
+    }
 }
+// X_b(r, c) *= sqrt(S_b[r])
 template <typename T>
-__global__ void k_scale_rows_sqrt(cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = t % rows, c = t / rows;
-    X[r + c * ld] = T(sqrt(S[r])) * X[r + c * ld];
-  }
+__global__ void k_scale_rows_sqrt(cx<T>* X, int64_t rows, int64_t cols, int64_t ld, int64_t sX, const double* S,
+                                  int64_t sS, int64_t batch) {
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
+      int64_t r = t % rows, c = t / rows;
+      X[b * sX + r + c * ld] = T(sqrt(S[b * sS + r])) * X[b * sX + r + c * ld];
+    }
 }
 
-// rank = #{ j < min(maxdim, k) : |S_j| > threshold }, at least 1 (S descending)
-__global__ void k_rank_select(const double* S, int64_t k, int64_t maxdim, double threshold, int* out) {
+// rank_b = #{ j < min(maxdim, k) : |S_b[j]| > threshold }, at least 1 (S descending);
+// one block per instance
+__global__ void k_rank_select(const double* S, int64_t k, int64_t sS, int64_t maxdim, double threshold, int* out) {
   __shared__ int cnt;
+  const double* Sb = S + blockIdx.x * sS;
   if (threadIdx.x == 0) cnt = 0;
   __syncthreads();
   int64_t kk = (maxdim > 0 && maxdim < k) ? maxdim : k;
   int local = 0;
-  for (int64_t j = threadIdx.x; j < kk; j += blockDim.x) local += (threshold <= 0.0 || fabs(S[j]) > threshold) ? 1 : 0;
+  for (int64_t j = threadIdx.x; j < kk; j += blockDim.x) local += (threshold <= 0.0 || fabs(Sb[j]) > threshold) ? 1 : 0;
   atomicAdd(&cnt, local);
   __syncthreads();
-  if (threadIdx.x == 0) out[0] = cnt > 0 ? cnt : 1;
+  if (threadIdx.x == 0) out[blockIdx.x] = cnt > 0 ? cnt : 1;
+}
+// S_b[j] = 0 for rank_b <= j < r (padding of a common bond dimension)
+__global__ void k_zero_tail(double* S, int64_t sS, const int* rank, int64_t r, int64_t batch) {
+  const int64_t b = blockIdx.x;
+  if (b >= batch) return;
+  for (int64_t j = rank[b] + threadIdx.x; j < r; j += blockDim.x) S[b * sS + j] = 0.0;
 }
 
 template <typename E>
@@ -129,11 +142,13 @@ __global__ void k_scale<float2>(int64_t n, float2* x, double s) {
   }
 }
 
-__global__ void k_copy_matrix(int64_t rows, int64_t cols, const cxd* src, int64_t lds, cxd* dst, int64_t ldd) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
-    int64_t r = t % rows, c = t / rows;
-    dst[r + c * ldd] = src[r + c * lds];
-  }
+__global__ void k_copy_matrix(int64_t rows, int64_t cols, const cxd* src, int64_t lds, int64_t sSrc, cxd* dst,
+                              int64_t ldd, int64_t sDst, int64_t batch) {
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
+      int64_t r = t % rows, c = t / rows;
+      dst[b * sDst + r + c * ldd] = src[b * sSrc + r + c * lds];
+    }
 }
 
 unsigned blocks_for(tn_ctx* ctx, int64_t n) {
@@ -163,36 +178,57 @@ tn_status_t sumsq(tn_ctx* ctx, int64_t n, const E* x, double* h_out) {
 
 }  // namespace
 
-tn_status_t rank_select(tn_ctx* ctx, const double* S, int64_t k, int64_t maxdim, double threshold, int64_t* rank) {
+tn_status_t rank_select_batched(tn_ctx* ctx, double* S, int64_t k, int64_t sS, int64_t batch, int64_t maxdim,
+                                double threshold, int64_t* rank_max, int64_t* ranks) {
   int* flags = nullptr;
-  TN_RETURN_IF(ctx_flags(ctx, 4, &flags));
-  k_rank_select<<<1, 256, 0, ctx->stream>>>(S, k, maxdim, threshold, flags);
+  TN_RETURN_IF(ctx_flags(ctx, (size_t)batch + 4, &flags));
+  if (batch > 8192) return tn_set_error(ctx, TN_EUNSUPPORTED, "rank select: batch > 8192");
+  k_rank_select<<<(unsigned)batch, 256, 0, ctx->stream>>>(S, k, sS, maxdim, threshold, flags);
   TN_LAUNCHED(ctx);
   int* hp = reinterpret_cast<int*>(ctx->pinned);
-  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, flags, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(hp, flags, sizeof(int) * batch, cudaMemcpyDeviceToHost, ctx->stream));
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  *rank = hp[0];
+  int64_t r = 0;
+  bool uneven = false;
+  for (int64_t b = 0; b < batch; ++b) {
+    if (ranks) ranks[b] = hp[b];
+    r = hp[b] > r ? hp[b] : r;
+  }
+  for (int64_t b = 0; b < batch; ++b) uneven |= hp[b] != r;
+  if (uneven) {
+    k_zero_tail<<<(unsigned)batch, 128, 0, ctx->stream>>>(S, sS, flags, r, batch);
+    TN_LAUNCHED(ctx);
+  }
+  *rank_max = r;
   return TN_OK;
 }
 
+tn_status_t rank_select(tn_ctx* ctx, const double* S, int64_t k, int64_t maxdim, double threshold, int64_t* rank) {
+  return rank_select_batched(ctx, const_cast<double*>(S), k, k, 1, maxdim, threshold, rank, nullptr);
+}
+
 template <typename T>
-tn_status_t scale_cols_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S) {
-  if (rows * cols == 0) return TN_OK;
-  k_scale_cols_sqrt<T><<<blocks_for(ctx, rows * cols), 256, 0, ctx->stream>>>(X, rows, cols, ld, S);
+tn_status_t scale_cols_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S,
+                            int64_t sX, int64_t sS, int64_t batch) {
+  if (rows * cols * batch == 0) return TN_OK;
+  dim3 g(blocks_for(ctx, rows * cols), (unsigned)(batch < 65535 ? batch : 65535));
+  k_scale_cols_sqrt<T><<<g, 256, 0, ctx->stream>>>(X, rows, cols, ld, sX, S, sS, batch);
   TN_LAUNCHED(ctx);
   return TN_OK;
 }
 template <typename T>
-tn_status_t scale_rows_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S) {
-  if (rows * cols == 0) return TN_OK;
-  k_scale_rows_sqrt<T><<<blocks_for(ctx, rows * cols), 256, 0, ctx->stream>>>(X, rows, cols, ld, S);
+tn_status_t scale_rows_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld, const double* S,
+                            int64_t sX, int64_t sS, int64_t batch) {
+  if (rows * cols * batch == 0) return TN_OK;
+  dim3 g(blocks_for(ctx, rows * cols), (unsigned)(batch < 65535 ? batch : 65535));
+  k_scale_rows_sqrt<T><<<g, 256, 0, ctx->stream>>>(X, rows, cols, ld, sX, S, sS, batch);
   TN_LAUNCHED(ctx);
   return TN_OK;
 }
-template tn_status_t scale_cols_sqrt<double>(tn_ctx*, cxd*, int64_t, int64_t, int64_t, const double*);
-template tn_status_t scale_cols_sqrt<float>(tn_ctx*, cxf*, int64_t, int64_t, int64_t, const double*);
-template tn_status_t scale_rows_sqrt<double>(tn_ctx*, cxd*, int64_t, int64_t, int64_t, const double*);
-template tn_status_t scale_rows_sqrt<float>(tn_ctx*, cxf*, int64_t, int64_t, int64_t, const double*);
+template tn_status_t scale_cols_sqrt<double>(tn_ctx*, cxd*, int64_t, int64_t, int64_t, const double*, int64_t, int64_t, int64_t);
+template tn_status_t scale_cols_sqrt<float>(tn_ctx*, cxf*, int64_t, int64_t, int64_t, const double*, int64_t, int64_t, int64_t);
+template tn_status_t scale_rows_sqrt<double>(tn_ctx*, cxd*, int64_t, int64_t, int64_t, const double*, int64_t, int64_t, int64_t);
+template tn_status_t scale_rows_sqrt<float>(tn_ctx*, cxf*, int64_t, int64_t, int64_t, const double*, int64_t, int64_t, int64_t);
 
 tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out) {
   double ss = 0;
@@ -202,10 +238,99 @@ tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out) {
 }
 
 tn_status_t copy_matrix_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src, int64_t lds, cxd* dst,
-                            int64_t ldd) {
-  if (rows * cols == 0) return TN_OK;
-  k_copy_matrix<<<blocks_for(ctx, rows * cols), 256, 0, ctx->stream>>>(rows, cols, src, lds, dst, ldd);
+                            int64_t ldd, int64_t sSrc, int64_t sDst, int64_t batch) {
+  if (rows * cols * batch == 0) return TN_OK;
+  dim3 g(blocks_for(ctx, rows * cols), (unsigned)(batch < 65535 ? batch : 65535));
+  k_copy_matrix<<<g, 256, 0, ctx->stream>>>(rows, cols, src, lds, sSrc, dst, ldd, sDst, batch);
   TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+// per-instance Σ|x|² for a batch of equal-length vectors at stride sx (FP64), to host
+__global__ void k_sumsq_batched(int64_t n, const double2* x, int64_t sx, double* out) {
+  __shared__ double red[32];
+  const double2* xb = x + blockIdx.x * sx;
+  double s = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += xb[i].x * xb[i].x + xb[i].y * xb[i].y;
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) out[blockIdx.x] = v;
+  }
+}
+__global__ void k_sumsq_real_batched(int64_t n, const double* x, int64_t sx, double* out) {
+  __shared__ double red[32];
+  const double* xb = x + blockIdx.x * sx;
+  double s = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) s += xb[i] * xb[i];
+  s = warp_sum(s);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double v = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+    v = warp_sum(v);
+    if (threadIdx.x == 0) out[blockIdx.x] = v;
+  }
+}
+tn_status_t norms_batched(tn_ctx* ctx, bool complex_data, int64_t n, const void* x, int64_t sx, int64_t batch,
+                          double* h_out) {
+  int* flags = nullptr;
+  TN_RETURN_IF(ctx_flags(ctx, 2 * (size_t)batch + 8, &flags));
+  double* d = reinterpret_cast<double*>(flags);
+  if (complex_data)
+    k_sumsq_batched<<<(unsigned)batch, 512, 0, ctx->stream>>>(n, (const double2*)x, sx, d);
+  else
+    k_sumsq_real_batched<<<(unsigned)batch, 512, 0, ctx->stream>>>(n, (const double*)x, sx, d);
+  TN_LAUNCHED(ctx);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_out, d, sizeof(double) * batch, cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int64_t b = 0; b < batch; ++b) h_out[b] = sqrt(h_out[b]);
+  return TN_OK;
+}
+
+// batched zdotc: out_b = Σ conj(x_b)·y_b (FP64, fixed order), to host
+__global__ void k_zdotc_batched(int64_t n, const double2* x, int64_t sx, const double2* y, int64_t sy, double* out) {
+  __shared__ double rx[32], ry[32];
+  const double2* xb = x + blockIdx.x * sx;
+  const double2* yb = y + blockIdx.x * sy;
+  double sr = 0, si = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    double2 a = xb[i], c = yb[i];
+    sr = fma(a.x, c.x, sr);
+    sr = fma(a.y, c.y, sr);
+    si = fma(a.x, c.y, si);
+    si = fma(-a.y, c.x, si);
+  }
+  sr = warp_sum(sr);
+  si = warp_sum(si);
+  if ((threadIdx.x & 31) == 0) {
+    rx[threadIdx.x >> 5] = sr;
+    ry[threadIdx.x >> 5] = si;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double vx = threadIdx.x < (blockDim.x >> 5) ? rx[threadIdx.x] : 0.0;
+    double vy = threadIdx.x < (blockDim.x >> 5) ? ry[threadIdx.x] : 0.0;
+    vx = warp_sum(vx);
+    vy = warp_sum(vy);
+    if (threadIdx.x == 0) {
+      out[2 * blockIdx.x] = vx;
+      out[2 * blockIdx.x + 1] = vy;
+    }
+  }
+}
+tn_status_t zdotc_batched(tn_ctx* ctx, int64_t n, const cxd* x, int64_t sx, const cxd* y, int64_t sy, int64_t batch,
+                          double* h_out) {
+  int* flags = nullptr;
+  TN_RETURN_IF(ctx_flags(ctx, 4 * (size_t)batch + 8, &flags));
+  double* d = reinterpret_cast<double*>(flags);
+  k_zdotc_batched<<<(unsigned)batch, 512, 0, ctx->stream>>>(n, (const double2*)x, sx, (const double2*)y, sy, d);
+  TN_LAUNCHED(ctx);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_out, d, 2 * sizeof(double) * batch, cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   return TN_OK;
 }
 

@@ -1,0 +1,241 @@
+# TenetGB300.jl — Julia binding of libtenetgb.so (C ABI: include/tenet_gb300.h).
+#
+# Tenet.jl never computes itself: every contraction, QR, SVD and simple update goes
+# through Muscle.jl on `Tangles.Tensor{T,N,A}` values, dispatched on the array type `A`.
+# This module adds a device array type `GB300Array` and Muscle methods for it, so Tenet's
+# call sites (src/Operations/canonize.jl:41-100, simple_update.jl:53-64,
+# overlap.jl:26-46, compress.jl:47-59) reach the sm_103a kernels unchanged.
+#
+# It also exposes the device-resident MPS (`GB300MPS`), which keeps whole sweeps on the
+# GPU (canonize!, compress!, simple_update!, evolve!, overlap, norm) — the fast path.
+#
+# No Julia toolchain exists in the build container, so this file is shipped unexecuted;
+# the same entry points are exercised from Python (tenet.jl_gb300/tenetgb) by the tests.
+module TenetGB300
+
+using LinearAlgebra
+
+const libtenetgb = get(ENV, "TENETGB_LIB", joinpath(@__DIR__, "..", "tenetgb", "_lib", "libtenetgb.so"))
+
+const TN_OK = Int32(0)
+const TN_C64 = Int32(3)
+const TN_C32 = Int32(2)
+const TN_F64 = Int32(1)
+const TN_F32 = Int32(0)
+const TN_PREC_NATIVE = Int32(0)
+const TN_PREC_MIXED = Int32(1)
+
+dtype(::Type{ComplexF64}) = TN_C64
+dtype(::Type{ComplexF32}) = TN_C32
+dtype(::Type{Float64}) = TN_F64
+dtype(::Type{Float32}) = TN_F32
+
+# ---- context ---------------------------------------------------------------------------
+mutable struct Context
+    h::Ptr{Cvoid}
+end
+
+function check(st::Int32, ctx::Ptr{Cvoid})
+    st == TN_OK && return nothing
+    msg = unsafe_string(ccall((:tn_last_error_string, libtenetgb), Cstring, (Ptr{Cvoid},), ctx))
+    st == 1 && throw(ArgumentError(msg))          # TN_EINVAL ↔ Tenet's @argcheck
+    st == 2 && throw(OutOfMemoryError())           # TN_ENOMEM
+    throw(ErrorException("libtenetgb status $st: $msg"))
+end
+
+function Context(device::Integer=0)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:tn_create, libtenetgb), Int32, (Ref{Ptr{Cvoid}}, Cint), r, device), C_NULL)
+    ctx = Context(r[])
+    finalizer(c -> ccall((:tn_destroy, libtenetgb), Int32, (Ptr{Cvoid},), c.h), ctx)
+    return ctx
+end
+
+const DEFAULT = Ref{Union{Nothing,Context}}(nothing)
+default_context() = something(DEFAULT[], (DEFAULT[] = Context(0)))
+
+# ---- device array ----------------------------------------------------------------------
+"""
+    GB300Array{T,N}
+
+Dense column-major device array owned by a libtenetgb context (tn_alloc / tn_free).
+"""
+mutable struct GB300Array{T,N} <: AbstractArray{T,N}
+    ptr::Ptr{Cvoid}
+    dims::NTuple{N,Int}
+    ctx::Context
+end
+
+Base.size(a::GB300Array) = a.dims
+Base.getindex(::GB300Array, ::Int...) = error("GB300Array: scalar indexing is disabled; use Array(a)")
+
+function GB300Array{T}(::UndefInitializer, dims::NTuple{N,Int}; ctx=default_context()) where {T,N}
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:tn_alloc, libtenetgb), Int32, (Ptr{Cvoid}, Csize_t, Ref{Ptr{Cvoid}}), ctx.h, max(1, prod(dims) * sizeof(T)), r), ctx.h)
+    a = GB300Array{T,N}(r[], dims, ctx)
+    finalizer(x -> ccall((:tn_free, libtenetgb), Int32, (Ptr{Cvoid}, Ptr{Cvoid}), x.ctx.h, x.ptr), a)
+    return a
+end
+
+function GB300Array(x::Array{T,N}; ctx=default_context()) where {T,N}
+    a = GB300Array{T}(undef, size(x); ctx)
+    GC.@preserve x check(ccall((:tn_memcpy_h2d, libtenetgb), Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Csize_t), ctx.h, a.ptr, pointer(x), sizeof(x)), ctx.h)
+    return a
+end
+
+function Base.Array(a::GB300Array{T,N}) where {T,N}
+    x = Array{T,N}(undef, a.dims)
+    GC.@preserve x check(ccall((:tn_memcpy_d2h, libtenetgb), Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Csize_t), a.ctx.h, pointer(x), a.ptr, sizeof(x)), a.ctx.h)
+    return x
+end
+
+# ---- Muscle-level entry points ---------------------------------------------------------
+# tn_tensor {int32 rank; int64 dims[8]; int32 modes[8]; void* data}
+struct TnTensor
+    rank::Int32
+    dims::NTuple{8,Int64}
+    modes::NTuple{8,Int32}
+    data::Ptr{Cvoid}
+end
+
+pad8(v, fill) = ntuple(i -> i <= length(v) ? v[i] : fill, 8)
+
+"""
+    binary_einsum(a, a_inds, b, b_inds, c_inds; precision=TN_PREC_NATIVE)
+
+`Muscle.binary_einsum` on GB300 arrays: labels are integers; labels shared by `a` and `b`
+and present in `c_inds` are kept (Hadamard modes), shared labels absent from `c_inds`
+are contracted (src/Operations/canonize.jl:44,61).
+"""
+function binary_einsum(a::GB300Array{T}, ai::Vector{Int}, b::GB300Array{T}, bi::Vector{Int}, ci::Vector{Int};
+                       precision=TN_PREC_NATIVE) where {T}
+    cdims = [i in ai ? size(a, findfirst(==(i), ai)) : size(b, findfirst(==(i), bi)) for i in ci]
+    c = GB300Array{T}(undef, Tuple(cdims); ctx=a.ctx)
+    ta = Ref(TnTensor(length(ai), pad8(collect(size(a)), 0), pad8(Int32.(ai), Int32(0)), a.ptr))
+    tb = Ref(TnTensor(length(bi), pad8(collect(size(b)), 0), pad8(Int32.(bi), Int32(0)), b.ptr))
+    tc = Ref(TnTensor(length(ci), pad8(cdims, 0), pad8(Int32.(ci), Int32(0)), c.ptr))
+    check(ccall((:tn_contract, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int32, Ref{TnTensor}, Ref{TnTensor}, Ref{TnTensor}),
+                a.ctx.h, dtype(T), precision, ta, tb, tc), a.ctx.h)
+    return c
+end
+
+"""
+    tensor_qr_thin(A::GB300Array{ComplexF64,2}) -> (Q, R)
+
+Thin QR of a matrix (the caller permutes `inds_q` first, as Muscle does):
+src/Operations/canonize.jl:58.
+"""
+function tensor_qr_thin(A::GB300Array{T,2}; precision=TN_PREC_NATIVE) where {T}
+    m, n = size(A)
+    k = min(m, n)
+    Q = GB300Array{T}(undef, (m, k); ctx=A.ctx)
+    R = GB300Array{T}(undef, (k, n); ctx=A.ctx)
+    check(ccall((:tn_qr_thin, libtenetgb), Int32,
+                (Ptr{Cvoid}, Int32, Int32, Int64, Int64, Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}, Int64, Ptr{Cvoid}, Int64, Int64),
+                A.ctx.h, dtype(T), precision, m, n, A.ptr, max(m, 1), 0, Q.ptr, 0, R.ptr, 0, 1), A.ctx.h)
+    return Q, R
+end
+
+"""
+    tensor_svd_thin(A::GB300Array{ComplexF64,2}) -> (U, s, V)
+
+Thin SVD A = U diag(s) V with s real descending (src/Operations/canonize.jl:41,97).
+"""
+function tensor_svd_thin(A::GB300Array{T,2}; precision=TN_PREC_NATIVE) where {T}
+    m, n = size(A)
+    k = min(m, n)
+    U = GB300Array{T}(undef, (m, k); ctx=A.ctx)
+    s = GB300Array{Float64}(undef, (k,); ctx=A.ctx)
+    V = GB300Array{T}(undef, (k, n); ctx=A.ctx)
+    check(ccall((:tn_svd_thin, libtenetgb), Int32,
+                (Ptr{Cvoid}, Int32, Int32, Int64, Int64, Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}, Int64, Ptr{Cvoid}, Int64,
+                 Ptr{Cvoid}, Int64, Int64),
+                A.ctx.h, dtype(T), precision, m, n, A.ptr, max(m, 1), 0, U.ptr, 0, s.ptr, 0, V.ptr, 0, 1), A.ctx.h)
+    return U, s, V
+end
+
+"""
+    simple_update(A, B, G; maxdim=-1, threshold=-1.0) -> (A′, B′)
+
+`Muscle.simple_update(...; absorb=AbsorbEqually())` (src/Operations/simple_update.jl:53-64)
+for A (χl, d1, χm), B (χm, d2, χr), G (d1, d2, d1, d2) with index order
+[out_a, out_b, in_a, in_b].
+"""
+function simple_update(A::GB300Array{ComplexF64,3}, B::GB300Array{ComplexF64,3}, G::GB300Array{ComplexF64,4};
+                       maxdim=-1, threshold=-1.0, precision=TN_PREC_NATIVE)
+    chl, d1, chm = size(A)
+    _, d2, chr = size(B)
+    kmax = min(chl * d1, d2 * chr)
+    An = GB300Array{ComplexF64}(undef, (chl, d1, kmax); ctx=A.ctx)
+    Bn = GB300Array{ComplexF64}(undef, (kmax, d2, chr); ctx=A.ctx)
+    r = Ref{Int64}(0)
+    check(ccall((:tn_simple_update, libtenetgb), Int32,
+                (Ptr{Cvoid}, Int32, Int32, Int64, Int64, Int64, Int64, Int64, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int64,
+                 Float64, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Int64}),
+                A.ctx.h, TN_C64, precision, chl, d1, chm, d2, chr, A.ptr, B.ptr, G.ptr, maxdim, threshold, An.ptr, Bn.ptr,
+                C_NULL, r), A.ctx.h)
+    An.dims = (chl, d1, Int(r[]))  # the kept columns are a column-major prefix
+    Bn.dims = (Int(r[]), d2, chr)  # compacted by the library to leading dimension r
+    return An, Bn
+end
+
+# ---- device-resident MPS ---------------------------------------------------------------
+mutable struct GB300MPS
+    h::Ptr{Cvoid}
+    ctx::Context
+    L::Int
+    d::Int
+end
+
+"""
+    GB300MPS(arrays; max_bond=0) where arrays are (χl, d, χr) Complex{Float64} site arrays
+
+(Tenet's (:l, :o, :r) order, src/Components/MPS.jl:50-94, with the boundary tensors
+lifted to 3-D.)
+"""
+function GB300MPS(arrays::Vector{Array{ComplexF64,3}}; max_bond=0, precision=TN_PREC_NATIVE, ctx=default_context())
+    L = length(arrays)
+    d = size(arrays[1], 2)
+    bonds = Int64[size(a, 3) for a in arrays[1:(end - 1)]]
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:tn_mps_create, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int32, Ptr{Int64}, Int64, Int32, Ref{Ptr{Cvoid}}),
+                ctx.h, L, d, bonds, max_bond, precision, r), ctx.h)
+    mps = GB300MPS(r[], ctx, L, d)
+    finalizer(m -> ccall((:tn_mps_destroy, libtenetgb), Int32, (Ptr{Cvoid},), m.h), mps)
+    for (i, a) in enumerate(arrays)
+        check(ccall((:tn_mps_set_site, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int64, Int64, Ptr{Cvoid}),
+                    mps.h, i, size(a, 1), size(a, 3), a), ctx.h)
+    end
+    return mps
+end
+
+canonize!(ψ::GB300MPS, lo::Integer, hi::Integer=lo) =
+    (check(ccall((:tn_mps_canonize_mixed, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int32), ψ.h, lo, hi), ψ.ctx.h); ψ)
+canonize_bond!(ψ::GB300MPS, a::Integer) =
+    (check(ccall((:tn_mps_canonize_bond, libtenetgb), Int32, (Ptr{Cvoid}, Int32), ψ.h, a), ψ.ctx.h); ψ)
+compress!(ψ::GB300MPS; bond=0, maxdim=-1, threshold=-1.0) =
+    (check(ccall((:tn_mps_compress, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int64, Float64), ψ.h, bond, maxdim, threshold), ψ.ctx.h); ψ)
+
+function simple_update!(ψ::GB300MPS, G::Array{ComplexF64}, site::Integer; maxdim=-1, threshold=-1.0)
+    nsites = ndims(G) == 2 ? 1 : 2
+    check(ccall((:tn_mps_simple_update, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int32, Ptr{ComplexF64}, Int64, Float64),
+                ψ.h, nsites, site, G, maxdim, threshold), ψ.ctx.h)
+    return ψ
+end
+evolve!(ψ::GB300MPS, G::Array{ComplexF64}, site::Integer) = simple_update!(ψ, G, site)  # evolve.jl:140-143
+
+function overlap(a::GB300MPS, b::GB300MPS)
+    out = zeros(Float64, 2)
+    check(ccall((:tn_mps_overlap, libtenetgb), Int32, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Float64}), a.h, b.h, out), a.ctx.h)
+    return complex(out[1], out[2])
+end
+
+function LinearAlgebra.norm(ψ::GB300MPS)
+    out = Ref{Float64}(0.0)
+    check(ccall((:tn_mps_norm, libtenetgb), Int32, (Ptr{Cvoid}, Ref{Float64}), ψ.h, out), ψ.ctx.h)
+    return out[]
+end
+
+LinearAlgebra.normalize!(ψ::GB300MPS) = (check(ccall((:tn_mps_normalize, libtenetgb), Int32, (Ptr{Cvoid},), ψ.h), ψ.ctx.h); ψ)
+
+end # module

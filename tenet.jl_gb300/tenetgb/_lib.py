@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libtenetgb.so")
 
 TN_OK, TN_EINVAL, TN_ENOMEM, TN_ENOCONV, TN_ETIMEOUT, TN_ECUDA, TN_EUNSUPPORTED = range(7)
 TN_F32, TN_F64, TN_C32, TN_C64 = range(4)
-TN_PREC_NATIVE, TN_PREC_MIXED = 0, 1
+TN_PREC_NATIVE, TN_PREC_MIXED, TN_PREC_TF32 = 0, 1, 2
 TN_FORM_NONCANONICAL, TN_FORM_MIXED, TN_FORM_BOND = 0, 1, 2
 TN_MAX_RANK = 8
 
@@ -87,6 +87,10 @@ SIGNATURES = {
         [_vp, C.c_int, C.c_int, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp, _i64, _dbl, _vp, _vp, _vp, _pi64],
     ),
     "tn_mps_create": (_st, [_vp, _i32, _i32, _pi64, _i64, C.c_int, C.POINTER(_vp)]),
+    "tn_mps_create_batched": (_st, [_vp, _i32, _i32, _i32, _pi64, _i64, C.c_int, C.POINTER(_vp)]),
+    "tn_mps_batch_size": (_st, [_vp, _pi32]),
+    "tn_mps_set_instance_site": (_st, [_vp, _i32, _i32, _i64, _i64, _vp]),
+    "tn_mps_get_instance_site": (_st, [_vp, _i32, _i32, _vp]),
     "tn_mps_destroy": (_st, [_vp]),
     "tn_mps_copy": (_st, [_vp, C.POINTER(_vp)]),
     "tn_mps_set_site": (_st, [_vp, _i32, _i64, _i64, _vp]),
@@ -109,6 +113,23 @@ SIGNATURES = {
 }
 
 _lib = None
+_shutting_down = False
+
+
+def _mark_shutdown():
+    global _shutting_down
+    _shutting_down = True
+
+
+def shutting_down():
+    """True once the interpreter is exiting: destructors then leave device memory to
+    the process teardown instead of calling into the library."""
+    return _shutting_down
+
+
+import atexit  # noqa: E402
+
+atexit.register(_mark_shutdown)
 
 
 def load():

@@ -33,7 +33,8 @@ _DT = {
     np.dtype(np.float64): L.TN_F64,
     np.dtype(np.float32): L.TN_F32,
 }
-_PREC = {"native": L.TN_PREC_NATIVE, "fp64": L.TN_PREC_NATIVE, "mixed": L.TN_PREC_MIXED}
+_PREC = {"native": L.TN_PREC_NATIVE, "fp64": L.TN_PREC_NATIVE, "fp32": L.TN_PREC_NATIVE, "mixed": L.TN_PREC_MIXED,
+         "3xtf32": L.TN_PREC_MIXED, "tf32": L.TN_PREC_TF32}
 
 
 def precision_code(p):
@@ -62,6 +63,8 @@ class Context:
             self.h = None
 
     def __del__(self):
+        if L.shutting_down():
+            return
         try:
             self.close()
         except Exception:
@@ -148,6 +151,8 @@ class DeviceTensor:
         return _DT[self.dtype]
 
     def __del__(self):
+        if L.shutting_down():
+            return
         try:
             if self.owned and self.ptr:
                 self.ctx.free(self.ptr)

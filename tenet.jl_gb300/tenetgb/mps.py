@@ -105,10 +105,14 @@ def _sites_from_arrays(arrays, order=("l", "r", "o")):
 
 class MPS:
     """MatrixProductState on one GB300.  ``sites`` are (χl, d, χr) arrays (C-ordered
-    numpy accepted; any memory order is fine)."""
+    numpy accepted; any memory order is fine).
+
+    ``MPS.batched([sites_0, sites_1, …])`` holds B instances with equal bond dimensions
+    that every operation advances in lockstep (one batched launch per kernel); values
+    that are scalars for one MPS (overlap, norm, amplitude) become length-B arrays."""
 
     def __init__(self, sites=None, *, arrays=None, order=("l", "r", "o"), ctx: Context | None = None,
-                 max_bond=0, precision="native", _handle=None):
+                 max_bond=0, precision="native", _handle=None, _instances=None):
         self.ctx = ctx or default_context()
         self.lib = self.ctx.lib
         if _handle is not None:
@@ -116,10 +120,15 @@ class MPS:
             return
         if arrays is not None:
             sites = _sites_from_arrays(arrays, order)
-        sites = [np.asarray(s, dtype=np.complex128) for s in sites]
+        instances = _instances if _instances is not None else [sites]
+        instances = [[np.asarray(s, dtype=np.complex128) for s in inst] for inst in instances]
+        sites = instances[0]
         L_ = len(sites)
         d = sites[0].shape[1]
         bonds = [s.shape[2] for s in sites[:-1]]
+        for inst in instances:
+            if len(inst) != L_ or [s.shape for s in inst] != [s.shape for s in sites]:
+                raise ValueError("batched MPS instances must have identical shapes")
         for i in range(L_ - 1):
             if sites[i].shape[2] != sites[i + 1].shape[0]:
                 raise ValueError(f"bond {i + 1}-{i + 2}: dims differ")
@@ -127,15 +136,33 @@ class MPS:
             raise ValueError("open boundary: end sites must have a size-1 outer bond")
         h = C.c_void_p()
         b = (C.c_int64 * (L_ - 1))(*bonds)
-        self.ctx.check(self.lib.tn_mps_create(self.ctx.h, L_, d, b, int(max_bond), precision_code(precision), C.byref(h)))
+        self.ctx.check(self.lib.tn_mps_create_batched(self.ctx.h, len(instances), L_, d, b, int(max_bond),
+                                                      precision_code(precision), C.byref(h)))
         self.h = h
-        for i, s in enumerate(sites):
-            f = np.asfortranarray(s)
-            self.ctx.check(self.lib.tn_mps_set_site(self.h, i + 1, s.shape[0], s.shape[2], f.ctypes.data_as(C.c_void_p)))
+        for bi, inst in enumerate(instances):
+            for i, s in enumerate(inst):
+                f = np.asfortranarray(s)
+                self.ctx.check(self.lib.tn_mps_set_instance_site(self.h, bi, i + 1, s.shape[0], s.shape[2],
+                                                                 f.ctypes.data_as(C.c_void_p)))
         self._L, self._d = L_, d
+
+    @classmethod
+    def batched(cls, instances, **kw):
+        return cls(_instances=list(instances), **kw)
+
+    @property
+    def batch(self):
+        v = C.c_int32()
+        self._chk(self.lib.tn_mps_batch_size(self.h, C.byref(v)))
+        return v.value
+
+    def _one(self, arr):
+        return arr[0] if self.batch == 1 else arr
 
     # -- bookkeeping -----------------------------------------------------------
     def __del__(self):
+        if L.shutting_down():
+            return
         try:
             if getattr(self, "h", None):
                 self.lib.tn_mps_destroy(self.h)
@@ -189,24 +216,24 @@ class MPS:
         m._L, m._d = self._L, self._d
         return m
 
-    def site(self, i):
+    def site(self, i, instance=0):
         """Site tensor i (1-based) as a (χl, d, χr) numpy array."""
         b = [1] + self.bondsizes() + [1]
         shape = (b[i - 1], self._d, b[i])
         out = np.empty(int(np.prod(shape)), dtype=np.complex128)
-        self._chk(self.lib.tn_mps_get_site(self.h, i, out.ctypes.data_as(C.c_void_p)))
+        self._chk(self.lib.tn_mps_get_instance_site(self.h, instance, i, out.ctypes.data_as(C.c_void_p)))
         return out.reshape(shape, order="F")
 
-    def sites(self):
-        return [self.site(i) for i in range(1, self._L + 1)]
+    def sites(self, instance=0):
+        return [self.site(i, instance) for i in range(1, self._L + 1)]
 
     def lambda_(self):
-        """Λ at the bond-canonical centre (LambdaSite(bond))."""
+        """Λ at the bond-canonical centre (LambdaSite(bond)); (B, χ) when batched."""
         n = C.c_int64()
         self._chk(self.lib.tn_mps_get_lambda(self.h, None, C.byref(n)))
-        out = np.empty(n.value, dtype=np.float64)
+        out = np.empty((self.batch, n.value), dtype=np.float64)
         self._chk(self.lib.tn_mps_get_lambda(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), C.byref(n)))
-        return out
+        return self._one(out)
 
     # -- Tenet operations --------------------------------------------------------
     def canonize_(self, form):
@@ -264,9 +291,9 @@ class MPS:
 
     def norm(self):
         """norm(ψ) (norm.jl:17-37); moves the orthogonality centre like the reference."""
-        v = C.c_double()
-        self._chk(self.lib.tn_mps_norm(self.h, C.byref(v)))
-        return v.value
+        v = np.empty(self.batch, dtype=np.float64)
+        self._chk(self.lib.tn_mps_norm(self.h, v.ctypes.data_as(C.POINTER(C.c_double))))
+        return float(v[0]) if self.batch == 1 else v
 
     def normalize_(self):
         self._chk(self.lib.tn_mps_normalize(self.h))
@@ -274,9 +301,10 @@ class MPS:
 
     def overlap(self, other: "MPS"):
         """overlap(self, other) = ⟨other|self⟩ (overlap.jl:36-50)."""
-        out = (C.c_double * 2)()
-        self._chk(self.lib.tn_mps_overlap(self.h, other.h, out))
-        return complex(out[0], out[1])
+        out = np.empty(2 * self.batch, dtype=np.float64)
+        self._chk(self.lib.tn_mps_overlap(self.h, other.h, out.ctypes.data_as(C.POINTER(C.c_double))))
+        v = out[0::2] + 1j * out[1::2]
+        return complex(v[0]) if self.batch == 1 else v
 
     def amplitude(self, bits):
         """overlap(ProductState(bits), ψ) (overlap.jl:22-32); ``bits`` is a string of
@@ -286,17 +314,19 @@ class MPS:
         else:
             vecs = [np.asarray(v, dtype=np.complex128) for v in bits]
         v = np.ascontiguousarray(np.stack(vecs))
-        out = (C.c_double * 2)()
-        self._chk(self.lib.tn_mps_amplitude(self.h, v.ctypes.data_as(C.c_void_p), out))
-        return complex(out[0], out[1])
+        out = np.empty(2 * self.batch, dtype=np.float64)
+        self._chk(self.lib.tn_mps_amplitude(self.h, v.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.POINTER(C.c_double))))
+        a = out[0::2] + 1j * out[1::2]
+        return complex(a[0]) if self.batch == 1 else a
 
     def local_expectations(self, op):
         """⟨ψ|O_i|ψ⟩/⟨ψ|ψ⟩ for every site i."""
         o = np.asfortranarray(np.asarray(op, dtype=np.complex128))
-        out = np.empty(2 * self._L, dtype=np.float64)
+        out = np.empty(2 * self._L * self.batch, dtype=np.float64)
         self._chk(self.lib.tn_mps_local_expectations(self.h, o.ctypes.data_as(C.c_void_p),
                                                      out.ctypes.data_as(C.POINTER(C.c_double))))
-        return out[0::2] + 1j * out[1::2]
+        z = (out[0::2] + 1j * out[1::2]).reshape(self.batch, self._L)
+        return z[0] if self.batch == 1 else z
 
 
 def _product_vectors(bits):

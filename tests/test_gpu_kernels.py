@@ -242,3 +242,69 @@ def test_muscle_simple_update(ctx, precision):
     th = np.tensordot(a, b, axes=(2, 0))
     th_o = np.tensordot(An_o, Bn_o, axes=(2, 0))
     assert np.abs(th - th_o).max() <= 1e-12 * np.abs(th_o).max()
+
+
+@pytest.mark.parametrize("prec,tol", [("mixed", 5e-6), ("tf32", 1e-3)])
+@pytest.mark.parametrize("m,n,k", [(256, 256, 256), (130, 70, 90), (1000, 300, 520), (8, 1024, 64)])
+@pytest.mark.parametrize("opa,opb", [("T", "N"), ("N", "N"), ("C", "T")])
+def test_tensor_core_gemm_c32(ctx, prec, tol, m, n, k, opa, opb):
+    """tcgen05 TF32 / 3xTF32 GEMM (complex via the real 4M block form) against FP64."""
+    import ctypes as C
+
+    import tenetgb
+
+    rng = np.random.default_rng(11)
+    ra, ca = (m, k) if opa == "N" else (k, m)
+    rb, cb = (k, n) if opb == "N" else (n, k)
+    A = cgauss(rng, (ra, ca), np.complex64)
+    B = cgauss(rng, (rb, cb), np.complex64)
+
+    def op(X, o):
+        X = X.astype(np.complex128)
+        return X if o == "N" else (X.T if o == "T" else X.conj().T)
+
+    ref = op(A, opa) @ op(B, opb)
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, A)
+    dB = tenetgb.DeviceTensor.from_numpy(ctx, B)
+    dC = tenetgb.DeviceTensor(ctx, (m, n), np.complex64)
+    one, zero = (C.c_double * 2)(1, 0), (C.c_double * 2)(0, 0)
+    code = tenetgb.core.precision_code(prec)
+    ctx.check(ctx.lib.tn_gemm(ctx.h, 2, code, opa.encode(), opb.encode(), m, n, k, one, C.c_void_p(dA.ptr), ra, 0,
+                              C.c_void_p(dB.ptr), rb, 0, zero, C.c_void_p(dC.ptr), m, 0, 1))
+    err = np.abs(dC.numpy() - ref).max() / (np.abs(op(A, opa)).max() * np.abs(op(B, opb)).max() * np.sqrt(k))
+    assert err < tol, err
+
+
+@pytest.mark.parametrize("prec", ["mixed", "tf32"])
+def test_tensor_core_gemm_f32(ctx, prec):
+    import ctypes as C
+
+    import tenetgb
+
+    rng = np.random.default_rng(12)
+    m, n, k = 300, 200, 400
+    A = rng.standard_normal((k, m)).astype(np.float32)
+    B = rng.standard_normal((k, n)).astype(np.float32)
+    ref = A.astype(np.float64).T @ B.astype(np.float64)
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, A)
+    dB = tenetgb.DeviceTensor.from_numpy(ctx, B)
+    dC = tenetgb.DeviceTensor(ctx, (m, n), np.float32)
+    one, zero = (C.c_double * 2)(1, 0), (C.c_double * 2)(0, 0)
+    ctx.check(ctx.lib.tn_gemm(ctx.h, 0, tenetgb.core.precision_code(prec), b"T", b"N", m, n, k, one, C.c_void_p(dA.ptr),
+                              k, 0, C.c_void_p(dB.ptr), k, 0, zero, C.c_void_p(dC.ptr), m, 0, 1))
+    err = np.abs(dC.numpy() - ref).max() / (np.abs(A).max() * np.abs(B).max() * np.sqrt(k))
+    # measured on GB300: 3xTF32 ~1e-6 at K≈400 (the tensor pipe's FP32 accumulation is
+    # coarser than FMA accumulation), single-pass TF32 ~2e-4
+    assert err < (5e-6 if prec == "mixed" else 1e-3), err
+
+
+def test_contract_c32_tensor_core(ctx):
+    import tenetgb
+
+    rng = np.random.default_rng(13)
+    A, B = cgauss(rng, (16, 8, 32), np.complex64), cgauss(rng, (32, 8, 24), np.complex64)
+    ta = tenetgb.DeviceTensor.from_numpy(ctx, A, list("abc"))
+    tb = tenetgb.DeviceTensor.from_numpy(ctx, B, list("cbd"))
+    tc = tenetgb.binary_einsum(ta, tb, out_inds=list("ad"), precision="mixed")
+    ref = np.einsum("abc,cbd->ad", A.astype(np.complex128), B.astype(np.complex128))
+    assert np.abs(tc.numpy() - ref).max() <= 1e-5 * np.abs(ref).max()

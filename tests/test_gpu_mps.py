@@ -224,3 +224,56 @@ def test_plain_small_config(ctx):
     assert abs(z - z_o) <= 1e-12 * abs(ov_o)
     assert abs(psi.norm() ** 2 - ov_o.real) <= 1e-12 * ov_o.real
     assert isinstance(psi.form, tenetgb.MixedCanonical)
+
+
+@pytest.mark.parametrize("precision", ["native", "mixed"])
+def test_batched_tebd_matches_oracle_per_instance(ctx, precision):
+    """B=3 instances in lockstep: instance 0 is a product state written into χ=4 bonds
+    (its θ spectra have exact zeros, so the cutoff keeps fewer values than for the
+    random instances and the common bond is zero-padded).  Every instance must match its
+    own oracle run."""
+    import tenetgb
+    from tenetgb import workloads as W
+
+    L_, chi0 = 14, 4
+    _, layers = W.tebd_workload(L=L_, chi0=chi0, n_layers=5)
+    rand = [W.random_mps_arrays(L_, 2, chi0, seed=s) for s in (21, 22)]
+    prod = [np.zeros_like(s) for s in rand[0]]
+    for s in prod:
+        s[0, 0, 0] = 1.0
+    insts = [prod] + rand
+    psi = tenetgb.MPS.batched(insts, ctx=ctx, max_bond=32, precision=precision)
+    psi.evolve_brickwork_(layers, maxdim=32, threshold=1e-12)
+    ov = psi.overlap(psi)
+    z = psi.local_expectations(W.pauli_z())
+    nrm = psi.norm()
+    for b, sites in enumerate(insts):
+        p = O.OMPS([s.copy() for s in sites])
+        O.tebd(p, layers, maxdim=32, threshold=1e-12)
+        ov_o = O.overlap(p, p)
+        assert abs(ov[b] - ov_o) <= 1e-12 * abs(ov_o), b
+        z_o, _ = O.local_expectations(p, W.pauli_z())
+        assert np.abs(z[b] - z_o).max() <= 1e-11, b
+        assert abs(nrm[b] ** 2 - ov_o.real) <= 1e-12 * ov_o.real
+    # the product instance's true ranks are below the common (padded) bond dimension
+    p0 = O.OMPS([s.copy() for s in insts[0]])
+    O.tebd(p0, layers, maxdim=32, threshold=1e-12)
+    pb, gb = p0.bondsizes(), psi.bondsizes()
+    assert all(a <= b for a, b in zip(pb, gb)) and any(a < b for a, b in zip(pb, gb))
+
+
+def test_batched_compress_and_amplitude(ctx):
+    import tenetgb
+    from tenetgb import workloads as W
+
+    insts = [W.random_mps_arrays(10, 2, 16, seed=s, orthogonalize=False) for s in (31, 32, 33, 34)]
+    psi = tenetgb.MPS.batched(insts, ctx=ctx)
+    amp = psi.amplitude("0110100101")
+    tenetgb.compress_(psi, maxdim=6)
+    nrm = psi.norm()
+    for b, sites in enumerate(insts):
+        p = O.OMPS([s.copy() for s in sites])
+        a_o = O.amplitude(O.product_state_vectors("0110100101"), p)
+        assert abs(amp[b] - a_o) <= 1e-12 * np.sqrt(abs(O.overlap(p, p)))
+        O.compress(p, maxdim=6)
+        assert abs(nrm[b] - O.norm(p)) <= 1e-12 * O.norm(p)
