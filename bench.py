@@ -136,6 +136,7 @@ def run_ours(args):
         dist.init_process_group("gloo")
     dev = torch.device("cuda", local)
     ctx = tenetgb.Context(local)
+    ctx.set_autotune(True)  # launch shapes are tuned on first use (saturation / warm-up)
     stream = torch.cuda.Stream(device=dev)
     ctx.set_stream(stream.cuda_stream)
     l2buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
@@ -363,9 +364,10 @@ def profile_gate(args):
     from tenetgb import workloads as W
 
     ctx = tenetgb.Context(0)
-    sites = W.random_mps_arrays(20, 2, CHI_MAX, seed=7)
+    ctx.set_autotune(True)
+    insts = [W.random_mps_arrays(20, 2, CHI_MAX, seed=7 + b) for b in range(args.batch)]
     gate = W.gate_tensor(W.haar_unitary(np.random.default_rng(8), 4))
-    psi = tenetgb.MPS(sites, ctx=ctx, max_bond=CHI_MAX, precision=args.precision)
+    psi = tenetgb.MPS.batched(insts, ctx=ctx, max_bond=CHI_MAX, precision=args.precision)
     psi.canonize_([10, 11])
     for rep in range(2):
         ctx.sync()
@@ -373,12 +375,50 @@ def profile_gate(args):
         psi.simple_update_(gate, [10, 11], maxdim=CHI_MAX, threshold=CUTOFF)
         ctx.sync()
         dt = time.perf_counter() - t0
-    print(json.dumps({"profile_gate_ms": 1e3 * dt, "precision": args.precision, "bond": psi.bondsizes()[9],
-                      "launches": ctx.launches()}))
+    print(json.dumps({"profile_gate_ms": 1e3 * dt, "precision": args.precision, "batch": args.batch,
+                      "bond": psi.bondsizes()[9], "launches": ctx.launches()}))
+
+
+def run_lattice(args):
+    """Closed 8×8 lattice, bond 8, ComplexF32 (seed 4): contraction to a scalar along the
+    planner's path, in 3×TF32 (tensor pipe), TF32, FP32 (CUDA cores) and FP64; errors
+    against the FP64 run.  Prints one JSON line (a secondary workload)."""
+    import torch
+
+    import tenetgb
+    from tenetgb import network as N
+
+    ctx = tenetgb.Context(0)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    net = N.lattice_2d(8, 8, 8, seed=4)
+    path = N.greedy_path(net.labels, net.dims)
+    steps, peak = N.path_flops(net.labels, net.dims, path)
+    flops = sum(st["flops"] for st in steps)
+    res = {}
+    for mode, dt in [("fp64", np.complex128), ("3xtf32", np.complex64), ("tf32", np.complex64), ("fp32", np.complex64)]:
+        prec = {"fp64": "native", "3xtf32": "mixed", "tf32": "tf32", "fp32": "native"}[mode]
+        N.contract(net, path, precision=prec, dtype=dt, ctx=ctx)  # warm-up
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        val = N.contract(net, path, precision=prec, dtype=dt, ctx=ctx)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        res[mode] = {"ms": ms, "value": complex(val), "tflops": flops / (ms * 1e-3) / 1e12}
+    ref = res["fp64"]["value"]
+    for mode in res:
+        res[mode]["rel_err_vs_fp64"] = abs(res[mode]["value"] - ref) / abs(ref)
+        res[mode]["value"] = [res[mode]["value"].real, res[mode]["value"].imag]
+    print(json.dumps({"metric": "lattice_8x8_bond8_contraction_tflops", "value": res["3xtf32"]["tflops"],
+                      "unit": "TFLOP/s (complex-algorithmic)", "steps": len(path), "peak_elements": peak,
+                      "path_flops": flops, "modes": res, "data": "synthetic (seeded Gaussian C32, seed 4)"}))
 
 
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="tebd", choices=["tebd", "lattice"])
     ap.add_argument("--profile-gate", action="store_true", help="one saturated gate (small ncu case)")
     ap.add_argument("--precision", default="native", choices=["native", "mixed"])
     ap.add_argument("--batch", type=int, default=8, help="MPS instances advanced in lockstep")
@@ -391,6 +431,8 @@ def main():
         args.warmup = 3
     if args.profile_gate:
         profile_gate(args)
+    elif args.workload == "lattice":
+        run_lattice(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -54,7 +54,7 @@ typedef enum { TN_F32 = 0, TN_F64 = 1, TN_C32 = 2, TN_C64 = 3 } tn_dtype_t;
  * TN_PREC_TF32: C32/F32 GEMMs as single-pass TF32 tensor-core products. */
 typedef enum { TN_PREC_NATIVE = 0, TN_PREC_MIXED = 1, TN_PREC_TF32 = 2 } tn_precision_t;
 
-#define TN_MAX_RANK 8
+#define TN_MAX_RANK 16
 
 typedef struct tn_ctx tn_ctx;
 
@@ -79,6 +79,13 @@ tn_status_t tn_hbm_in_use(tn_ctx* ctx, size_t* bytes);
 tn_status_t tn_kernel_launches(tn_ctx* ctx, int64_t* count);
 const char* tn_last_error_string(tn_ctx* ctx);
 const char* tn_version(void);
+/* autotuner: with enable != 0 the first call of an unseen shape bucket times the
+ * candidate launch configurations (QR panel and slab widths) and records the fastest.
+ * tn_tuning_dump writes the table as text ("key v1 v2" lines; *needed = bytes incl. the
+ * terminator); tn_tuning_load reads such text back (a tuning cache file). */
+tn_status_t tn_set_autotune(tn_ctx* ctx, int32_t enable);
+tn_status_t tn_tuning_dump(tn_ctx* ctx, char* buf, size_t len, size_t* needed);
+tn_status_t tn_tuning_load(tn_ctx* ctx, const char* text);
 
 /* ------------------------------------------------------------------------------------
  * K1 — index permutation (replaces Julia `permutedims` inside Muscle.binary_einsum and
@@ -138,6 +145,12 @@ tn_status_t tn_svd_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int6
                         int64_t n, const void* d_A, int64_t lda, int64_t strideA, void* d_U,
                         int64_t strideU, double* d_S, int64_t strideS, void* d_Vh,
                         int64_t strideVh, int64_t batch);
+
+/* diagnostics of the last SVD on this context: Jacobi sweeps run in FP32 (mixed
+ * pre-pass) and in FP64 (-1: the one-CTA shared-memory kernel ran all sweeps), and the
+ * number of rotations applied in each sweep of the first matrix (up to n_rot) */
+tn_status_t tn_svd_last_sweeps(tn_ctx* ctx, int32_t* fp32_sweeps, int32_t* fp64_sweeps,
+                               int32_t* rotations, int32_t n_rot);
 
 /* truncation rank select: keep min(maxdim, k) values (maxdim <= 0: no cap), then those
  * with |s| > threshold (threshold <= 0: no threshold), at least one.  Mirrors

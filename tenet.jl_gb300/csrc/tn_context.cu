@@ -213,6 +213,42 @@ tn_status_t tn_kernel_launches(tn_ctx* ctx, int64_t* count) {
   return TN_OK;
 }
 
+tn_status_t tn_set_autotune(tn_ctx* ctx, int32_t enable) {
+  if (!ctx) return TN_EINVAL;
+  ctx->autotune = enable != 0;
+  return TN_OK;
+}
+
+// text form: one "key value1 value2" line per tuned shape
+tn_status_t tn_tuning_dump(tn_ctx* ctx, char* buf, size_t len, size_t* needed) {
+  if (!ctx) return TN_EINVAL;
+  std::string out;
+  for (auto& kv : ctx->tuning)
+    out += kv.first + " " + std::to_string(kv.second.first) + " " + std::to_string(kv.second.second) + "\n";
+  if (needed) *needed = out.size() + 1;
+  if (buf && len > 0) {
+    size_t c = out.size() < len - 1 ? out.size() : len - 1;
+    memcpy(buf, out.data(), c);
+    buf[c] = 0;
+  }
+  return TN_OK;
+}
+
+tn_status_t tn_tuning_load(tn_ctx* ctx, const char* text) {
+  if (!ctx || !text) return TN_EINVAL;
+  const char* p = text;
+  while (*p) {
+    char key[128];
+    int a = 0, b = 0, used = 0;
+    if (sscanf(p, "%127s %d %d%n", key, &a, &b, &used) != 3) break;
+    if (a < 1 || a > 32 || b < 1 || b > 4) return tn_set_error(ctx, TN_EINVAL, "tn_tuning_load: bad entry %s", key);
+    ctx->tuning[key] = {a, b};
+    p += used;
+    while (*p == '\n' || *p == ' ') ++p;
+  }
+  return TN_OK;
+}
+
 const char* tn_last_error_string(tn_ctx* ctx) {
   return ctx ? ctx->last_error.c_str() : g_create_error.c_str();
 }

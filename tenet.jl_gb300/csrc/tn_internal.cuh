@@ -104,6 +104,13 @@ struct tn_ctx {
   // release until the last of them is destroyed
   int refs = 0;
   bool destroy_requested = false;
+  // diagnostics of the last Jacobi SVD: sweeps per precision, rotations per sweep of
+  // the first matrix of the large-matrix path (-1: shared-memory path)
+  int last_sweeps_fp32 = 0, last_sweeps_fp64 = 0;
+  int sweep_rotations[64] = {0};
+  // autotuned launch parameters, keyed by kernel family + shape bucket
+  bool autotune = false;
+  std::unordered_map<std::string, std::pair<int, int>> tuning;
 };
 void ctx_release(tn_ctx* ctx);  // frees the context (called when refs drop to 0)
 
@@ -210,6 +217,11 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
                            int64_t sA, cxd* U, int64_t sU, double* S, int64_t sS, cxd* V,
                            int64_t sV, int64_t batch);
 
+// left vectors + values only (m >= n): U m×n, S n (no V accumulation on large matrices)
+size_t svd_left_workspace(tn_precision_t prec, int64_t m, int64_t n, int64_t batch);
+tn_status_t svd_left(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_t n, const cxd* A, int64_t lda, int64_t sA,
+                     cxd* U, int64_t sU, double* S, int64_t sS, int64_t batch);
+
 // full thin SVD for any m, n: U m×k, S k, Vh k×n (reserves its own workspace when
 // ws_managed is false)
 size_t svd_any_workspace(tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n,
@@ -243,6 +255,9 @@ tn_status_t scale_cols_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, i
 template <typename T>
 tn_status_t scale_rows_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, int64_t ld,
                             const double* S, int64_t sX = 0, int64_t sS = 0, int64_t batch = 1);
+// X_b(r, c) *= 1/sqrt(S_b[r]) (0 where S_b[r] == 0)
+tn_status_t scale_rows_invsqrt(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int64_t ld,
+                               const double* S, int64_t sX, int64_t sS, int64_t batch);
 tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out);
 tn_status_t copy_matrix_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src,
                             int64_t lds, cxd* dst, int64_t ldd, int64_t sSrc = 0,

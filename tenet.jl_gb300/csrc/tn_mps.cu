@@ -300,9 +300,12 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
                                int64_t maxdim, double threshold, int64_t batch, su_out_fn out_fn, void* out_arg,
                                double* Sout, int64_t* rank_out) {
   const int64_t m = chl * d1, n = d2 * chr, k = std::min(m, n), dd = d1 * d2;
+  // m ≥ n (the saturated TEBD case, θ square): U and S only, then
+  //   B' = √S Vh = diag(1/√s) Uᴴ θ  (one GEMM; A'B' keeps its ε‖θ‖ accuracy)
+  const bool left_only = m >= n;
   size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(batch * m * n)) + ws_round(sizeof(cxd) * (size_t)(batch * m * k)) +
                 ws_round(sizeof(double) * (size_t)(batch * k)) + ws_round(sizeof(cxd) * (size_t)(batch * k * n)) +
-                svd_any_workspace(TN_C64, prec, m, n, batch);
+                (left_only ? svd_left_workspace(prec, m, n, batch) : svd_any_workspace(TN_C64, prec, m, n, batch));
   TN_RETURN_IF(ws_reserve(ctx, need));
   cxd* th0 = ws_take<cxd>(ctx, (size_t)(batch * m * n));
   cxd* th = ws_take<cxd>(ctx, (size_t)(batch * m * n));
@@ -315,17 +318,27 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
   // which are contiguous blocks of chl·dd elements
   TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, dd, dd, kOne, th0, chl, chl * dd, dG, dd, 0, kZero, th, chl,
                                chl * dd, chr * batch));
-  TN_RETURN_IF(svd_any(ctx, TN_C64, prec, m, n, th, m, m * n, U, m * k, S, k, Vh, k * n, batch));
+  if (left_only)
+    TN_RETURN_IF(svd_left(ctx, prec, m, n, th, m, m * n, U, m * k, S, k, batch));
+  else
+    TN_RETURN_IF(svd_any(ctx, TN_C64, prec, m, n, th, m, m * n, U, m * k, S, k, Vh, k * n, batch));
   int64_t r = 0;
   TN_RETURN_IF(rank_select_batched(ctx, S, k, k, batch, maxdim, threshold, &r, nullptr));
   cxd *Aout = nullptr, *Bout = nullptr;
   int64_t sAo = 0, sBo = 0;
   TN_RETURN_IF(out_fn(out_arg, r, &Aout, &sAo, &Bout, &sBo));
-  // A' = U[:, :r] √S ; B' = √S Vh[:r, :]
+  // A' = U[:, :r] √S
   TN_RETURN_IF(copy_matrix_cxd(ctx, m * r, 1, U, m * r, Aout, m * r, m * k, sAo, batch));
   TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
-  TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
-  TN_RETURN_IF(scale_rows_sqrt<double>(ctx, Bout, r, n, r, S, sBo, k, batch));
+  if (left_only) {
+    // B' = diag(1/√s) U[:, :r]ᴴ θ
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
+    TN_RETURN_IF(scale_rows_invsqrt(ctx, Bout, r, n, r, S, sBo, k, batch));
+  } else {
+    // B' = √S Vh[:r, :]
+    TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
+    TN_RETURN_IF(scale_rows_sqrt<double>(ctx, Bout, r, n, r, S, sBo, k, batch));
+  }
   if (Sout)
     TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(Sout, sizeof(double) * r, S, sizeof(double) * k, sizeof(double) * r, batch,
                                          cudaMemcpyDeviceToDevice, ctx->stream));

@@ -219,7 +219,7 @@ extern "C" tn_status_t tn_permute(tn_ctx* ctx, tn_dtype_t dtype, int32_t rank, c
                                   const int64_t* in_strides, const int32_t* perm, const void* in,
                                   void* out, int32_t conj) {
   if (!ctx) return TN_EINVAL;
-  TN_ARG(ctx, rank >= 1 && rank <= TN_MAX_RANK, "tn_permute: rank must be in 1..8");
+  TN_ARG(ctx, rank >= 1 && rank <= TN_MAX_RANK, "tn_permute: rank must be in 1..16");
   TN_ARG(ctx, dims && perm && in && out, "tn_permute: null pointer");
   bool seen[TN_MAX_RANK] = {false};
   for (int i = 0; i < rank; ++i) {

@@ -14,18 +14,21 @@
 //    Y = Tᴴ W (or T W when forming Q), A_slab −= V Y.  Every SM works on the trailing
 //    update, which holds O(m n²) of the O(m n²) flops.
 //  * Q is formed by applying the panels in reverse to [I_k; 0] (LAPACK ungqr order).
+#include <algorithm>
+
 #include "tn_internal.cuh"
 
 namespace {
 
 constexpr int kPanelThreads = 256;
-constexpr int kSlabCols = 4;
+constexpr int kMaxPanel = 32;
 constexpr size_t kPanelSmemMax = 180 * 1024;  // + 34 KB static (Gram, T) <= 227 KB
 
+// widest panel whose m×nb block fits the panel kernel's shared memory
 template <typename T>
-int panel_width(int64_t m) {
+int panel_width_max(int64_t m) {
   int64_t cap = (int64_t)(kPanelSmemMax / (sizeof(cx<T>) * (size_t)(m > 0 ? m : 1)));
-  int nb = 32;
+  int nb = kMaxPanel;
   while (nb > 1 && nb > cap) nb >>= 1;
   return nb;
 }
@@ -156,7 +159,7 @@ __global__ void __launch_bounds__(kPanelThreads)
 // X[j0:m, c0:c1] ← (I − V T Vᴴ)^{op} X  where op = ᴴ (conjT = true, trailing update of
 // the factorisation) or identity (conjT = false, forming Q).  V is the panel stored in
 // W[j0:m, j0:j0+jb].
-template <typename T>
+template <typename T, int kSlabCols>
 __global__ void __launch_bounds__(256)
     k_apply_block_reflector(int64_t m, int64_t j0, int jb, int nb, const cx<T>* W, int64_t ldw, int64_t sW,
                             const cx<T>* Tm, int64_t sT, cx<T>* X, int64_t ldx, int64_t sX, int64_t c0,
@@ -236,28 +239,45 @@ __global__ void k_extract_r_init_q(int64_t m, int64_t n, int64_t k, const cx<T>*
 
 template <typename T>
 size_t qr_workspace(int64_t m, int64_t n, int64_t batch) {
-  int64_t k = m < n ? m : n;
-  int nb = panel_width<T>(m);
-  int64_t npan = (k + nb - 1) / nb;
+  const int64_t k = m < n ? m : n;
+  const int nb = panel_width_max<T>(m);
+  const int64_t npan = (k + nb - 1) / nb;
   size_t w = ws_round(sizeof(cx<T>) * (size_t)(m * n * batch));
   size_t tau = ws_round(sizeof(cx<T>) * (size_t)(k * batch + 1));
-  size_t tm = ws_round(sizeof(cx<T>) * (size_t)(npan * nb * nb * batch + 1));
+  // T factors: npan·nb² per matrix at the widest panel bounds every narrower choice
+  size_t tm = ws_round(sizeof(cx<T>) * (size_t)((npan + 1) * nb * nb * batch + 1));
   return w + tau + tm;
 }
 template size_t qr_workspace<double>(int64_t, int64_t, int64_t);
 template size_t qr_workspace<float>(int64_t, int64_t, int64_t);
 
+namespace {
+
 template <typename T>
-tn_status_t qr_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda, int64_t sA, cx<T>* Q,
-                  int64_t sQ, cx<T>* R, int64_t sR, int64_t batch) {
-  // workspace must have been reserved by the caller (qr_workspace) and is taken here
+tn_status_t launch_reflector(tn_ctx* ctx, int slab, dim3 grid, int64_t m, int64_t j0, int jb, int nb, const cx<T>* W,
+                             int64_t sW, const cx<T>* Tm, int64_t sT, cx<T>* X, int64_t sX, int64_t c0, int64_t c1,
+                             bool conjT) {
+  switch (slab) {
+    case 1:
+      k_apply_block_reflector<T, 1><<<grid, 256, 0, ctx->stream>>>(m, j0, jb, nb, W, m, sW, Tm, sT, X, m, sX, c0, c1, conjT);
+      break;
+    case 2:
+      k_apply_block_reflector<T, 2><<<grid, 256, 0, ctx->stream>>>(m, j0, jb, nb, W, m, sW, Tm, sT, X, m, sX, c0, c1, conjT);
+      break;
+    default:
+      k_apply_block_reflector<T, 4><<<grid, 256, 0, ctx->stream>>>(m, j0, jb, nb, W, m, sW, Tm, sT, X, m, sX, c0, c1, conjT);
+      break;
+  }
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+// one factorisation with panel width nb and block-reflector slab width `slab`
+template <typename T>
+tn_status_t qr_run(tn_ctx* ctx, int nb, int slab, int64_t m, int64_t n, const cx<T>* A, int64_t lda, int64_t sA,
+                   cx<T>* Q, int64_t sQ, cx<T>* R, int64_t sR, int64_t batch, cx<T>* W, cx<T>* tau, cx<T>* Tm) {
   const int64_t k = m < n ? m : n;
-  if (m == 0 || n == 0 || batch == 0) return TN_OK;
-  const int nb = panel_width<T>(m);
   const int64_t npan = (k + nb - 1) / nb;
-  cx<T>* W = ws_take<cx<T>>(ctx, (size_t)(m * n * batch));
-  cx<T>* tau = ws_take<cx<T>>(ctx, (size_t)(k * batch + 1));
-  cx<T>* Tm = ws_take<cx<T>>(ctx, (size_t)(npan * nb * nb * batch + 1));
   const int64_t sW = m * n, sTau = k, sT = npan * nb * nb;
   const unsigned gy = (unsigned)(batch < 65535 ? batch : 65535);
   {
@@ -266,10 +286,6 @@ tn_status_t qr_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda
     k_copy_in<T><<<dim3((unsigned)blocks, gy), 256, 0, ctx->stream>>>(m, n, A, lda, sA, W, sW, batch);
     TN_LAUNCHED(ctx);
   }
-  const size_t smem = sizeof(cx<T>) * (size_t)m * nb;
-  if (smem > kPanelSmemMax) return tn_set_error(ctx, TN_EUNSUPPORTED, "qr: m=%lld too large for the panel kernel", (long long)m);
-  TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_qr_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemMax));
-  if (batch > 2147483647) return tn_set_error(ctx, TN_EINVAL, "qr: batch too large");
   for (int64_t p = 0; p < npan; ++p) {
     const int64_t j0 = p * nb;
     const int jb = (int)(k - j0 < nb ? k - j0 : nb);
@@ -277,34 +293,82 @@ tn_status_t qr_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda
         m, j0, jb, nb, W, m, sW, tau, sTau, Tm + p * nb * nb, sT);
     TN_LAUNCHED(ctx);
     const int64_t c0 = j0 + jb;
-    if (c0 < n) {
-      dim3 grid(cdiv(n - c0, kSlabCols), gy);
-      k_apply_block_reflector<T><<<grid, 256, 0, ctx->stream>>>(m, j0, jb, nb, W, m, sW, Tm + p * nb * nb, sT, W,
-                                                                 m, sW, c0, n, true);
-      TN_LAUNCHED(ctx);
-    }
+    if (c0 < n)
+      TN_RETURN_IF(launch_reflector<T>(ctx, slab, dim3(cdiv(n - c0, slab), gy), m, j0, jb, nb, W, sW, Tm + p * nb * nb,
+                                       sT, W, sW, c0, n, true));
   }
   {
     int64_t blocks = ((m * k) + 255) / 256;
     if (blocks > 4096) blocks = 4096;
-    k_extract_r_init_q<T><<<dim3((unsigned)blocks, gy), 256, 0, ctx->stream>>>(m, n, k, W, sW, R, sR, Q, sQ,
-                                                                                batch);
+    k_extract_r_init_q<T><<<dim3((unsigned)blocks, gy), 256, 0, ctx->stream>>>(m, n, k, W, sW, R, sR, Q, sQ, batch);
     TN_LAUNCHED(ctx);
   }
   for (int64_t p = npan - 1; p >= 0; --p) {
     const int64_t j0 = p * nb;
     const int jb = (int)(k - j0 < nb ? k - j0 : nb);
-    dim3 grid(cdiv(k - j0, kSlabCols), gy);
-    k_apply_block_reflector<T><<<grid, 256, 0, ctx->stream>>>(m, j0, jb, nb, W, m, sW, Tm + p * nb * nb, sT, Q, m,
-                                                               sQ, j0, k, false);
-    TN_LAUNCHED(ctx);
+    TN_RETURN_IF(launch_reflector<T>(ctx, slab, dim3(cdiv(k - j0, slab), gy), m, j0, jb, nb, W, sW, Tm + p * nb * nb,
+                                     sT, Q, sQ, j0, k, false));
   }
   return TN_OK;
 }
-template tn_status_t qr_cx<double>(tn_ctx*, int64_t, int64_t, const cxd*, int64_t, int64_t, cxd*, int64_t,
-                                   cxd*, int64_t, int64_t);
-template tn_status_t qr_cx<float>(tn_ctx*, int64_t, int64_t, const cxf*, int64_t, int64_t, cxf*, int64_t,
-                                  cxf*, int64_t, int64_t);
+
+}  // namespace
+
+// Panel width and slab width come from the context's tuning table, keyed by the shape
+// (m, n and a batch bucket).  With autotuning on, the first call of an unseen shape
+// times every candidate (panel 4/8/16/32 that fits shared memory × slab 1/2/4) with
+// CUDA events and records the fastest; otherwise the default is panel 8, slab 2.
+template <typename T>
+tn_status_t qr_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda, int64_t sA, cx<T>* Q, int64_t sQ,
+                  cx<T>* R, int64_t sR, int64_t batch) {
+  const int64_t k = m < n ? m : n;
+  if (m == 0 || n == 0 || batch == 0) return TN_OK;
+  if (batch > 2147483647) return tn_set_error(ctx, TN_EINVAL, "qr: batch too large");
+  const int nb_max = panel_width_max<T>(m);
+  if (sizeof(cx<T>) * (size_t)m * 1 > kPanelSmemMax)
+    return tn_set_error(ctx, TN_EUNSUPPORTED, "qr: m=%lld too large for the panel kernel", (long long)m);
+  const int64_t npan_max = (k + nb_max - 1) / nb_max;
+  cx<T>* W = ws_take<cx<T>>(ctx, (size_t)(m * n * batch));
+  cx<T>* tau = ws_take<cx<T>>(ctx, (size_t)(k * batch + 1));
+  cx<T>* Tm = ws_take<cx<T>>(ctx, (size_t)((npan_max + 1) * nb_max * nb_max * batch + 1));
+  TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_qr_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPanelSmemMax));
+  const int bb = batch <= 1 ? 1 : batch <= 4 ? 4 : batch <= 16 ? 16 : 64;
+  char key[96];
+  snprintf(key, sizeof(key), "qr%zu:%lld:%lld:%d", sizeof(T), (long long)m, (long long)n, bb);
+  auto it = ctx->tuning.find(key);
+  int nb = std::min(8, nb_max), slab = 2;
+  if (it != ctx->tuning.end()) {
+    nb = std::min(it->second.first, nb_max);
+    slab = it->second.second;
+  } else if (ctx->autotune) {
+    float best = 1e30f;
+    cudaEvent_t e0, e1;
+    TN_CHECK_CUDA(ctx, cudaEventCreate(&e0));
+    TN_CHECK_CUDA(ctx, cudaEventCreate(&e1));
+    for (int cand_nb = 4; cand_nb <= nb_max; cand_nb *= 2)
+      for (int cand_slab = 1; cand_slab <= 4; cand_slab *= 2) {
+        TN_CHECK_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+        TN_RETURN_IF(qr_run<T>(ctx, cand_nb, cand_slab, m, n, A, lda, sA, Q, sQ, R, sR, batch, W, tau, Tm));
+        TN_CHECK_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+        TN_CHECK_CUDA(ctx, cudaEventSynchronize(e1));
+        float ms = 0;
+        TN_CHECK_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) {
+          best = ms;
+          nb = cand_nb;
+          slab = cand_slab;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    ctx->tuning[key] = {nb, slab};
+  }
+  return qr_run<T>(ctx, nb, slab, m, n, A, lda, sA, Q, sQ, R, sR, batch, W, tau, Tm);
+}
+template tn_status_t qr_cx<double>(tn_ctx*, int64_t, int64_t, const cxd*, int64_t, int64_t, cxd*, int64_t, cxd*,
+                                   int64_t, int64_t);
+template tn_status_t qr_cx<float>(tn_ctx*, int64_t, int64_t, const cxf*, int64_t, int64_t, cxf*, int64_t, cxf*,
+                                  int64_t, int64_t);
 
 extern "C" tn_status_t tn_qr_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int64_t m, int64_t n,
                                   const void* A, int64_t lda, int64_t strideA, void* Q, int64_t strideQ,

@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(NT)
   Rot<T> Rt = make_rot(al, be, g, tol);
   if (!Rt.apply) return;
   if (threadIdx.x == 0) {
-    rotated[b] = 1;
+    atomicAdd(&rotated[b], 1);
     nrm[b * n + i] = al - Rt.t * Rt.ag;
     nrm[b * n + j] = be + Rt.t * Rt.ag;
   }
@@ -352,6 +352,7 @@ __global__ void k_svd_gather(int64_t m, int64_t n, const cx<T>* W, int64_t sW, c
     T inv = s > 0 ? T(1.0 / s) : T(0);
     U[b * sU + t] = inv * W[b * sW + r + (int64_t)src * m];
   }
+  if (!V || !Vo) return;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * n; t += (int64_t)gridDim.x * blockDim.x) {
     int64_t r = t % n, c = t / n;
     int src = order[b * n + c];
@@ -467,6 +468,7 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       ctx->launches += N;  // norm refresh + N-1 steps
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * batch, cudaMemcpyDeviceToHost, ctx->stream));
       TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      if (sweeps < (int)(sizeof(ctx->sweep_rotations) / sizeof(int))) ctx->sweep_rotations[sweeps] = h_rot[0];
       n_active = 0;
       for (int64_t b = 0; b < batch; ++b) {
         h_act[b] = h_act[b] && h_rot[b];
@@ -478,6 +480,10 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
   }
   if (sweeps_out) *sweeps_out = sweeps;
   if (noconv_out) *noconv_out = noconv;
+  if (sizeof(T) == 4)
+    ctx->last_sweeps_fp32 = sweeps;
+  else
+    ctx->last_sweeps_fp64 = sweeps;
   return TN_OK;
 }
 
@@ -521,6 +527,7 @@ static tn_status_t svd_tall_impl(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>*
     TN_LAUNCHED(ctx);
   }
   bool noconv = false;
+  ctx->last_sweeps_fp32 = 0;
   TN_RETURN_IF(jacobi_core<T>(ctx, m, n, W, V, batch, false, active, rotated, nrm, kMaxSweeps, sweeps_out, &noconv));
   TN_RETURN_IF(jacobi_finalize<T>(ctx, m, n, W, V, order, U, sU, S, sS, Vo, sVo, vh, batch));
   if (noconv) return tn_set_error(ctx, TN_ENOCONV, "Jacobi SVD did not converge within %d sweeps", kMaxSweeps);
@@ -568,12 +575,15 @@ size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
   s += ws_round(sizeof(int) * (size_t)(n * batch));
   s += 2 * ws_round(sizeof(int) * (size_t)(batch + 1));
   s += ws_round(sizeof(double) * (size_t)(n * batch)) + ws_round(sizeof(float) * (size_t)(n * batch));
+  s += ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // V scratch when V is not wanted
   return s;
 }
 
 tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int64_t lda, int64_t sA, cxd* U,
                            int64_t sU, double* S, int64_t sS, cxd* V, int64_t sV, int64_t batch) {
+  // V == nullptr: right vectors not wanted; the FP64 sweeps then skip accumulating them
   if (m < n) return tn_set_error(ctx, TN_EINVAL, "svd_tall_mixed: m < n");
+  const bool want_v = V != nullptr;
   if (n == 0 || batch == 0) return TN_OK;
   if (batch > 65535) return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: batch > 65535");
   cxf* W32 = ws_take<cxf>(ctx, (size_t)(m * n * batch));
@@ -581,6 +591,11 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   cxd* W64 = ws_take<cxd>(ctx, (size_t)(m * n * batch));
   cxd* V64 = ws_take<cxd>(ctx, (size_t)(n * n * batch));
   cxd* G = ws_take<cxd>(ctx, (size_t)(n * n * batch));
+  cxd* Vt = want_v ? nullptr : ws_take<cxd>(ctx, (size_t)(n * n * batch));
+  if (!want_v) {
+    V = Vt;
+    sV = n * n;
+  }
   int* order = ws_take<int>(ctx, (size_t)(n * batch));
   int* active = ws_take<int>(ctx, (size_t)(batch + 1));
   int* rotated = ws_take<int>(ctx, (size_t)(batch + 1));
@@ -616,8 +631,48 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   // W = A V  (FP64)
   TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, n, mkcx(1.0, 0.0), A, lda, sA, V64, n, n * n, mkcx(0.0, 0.0), W64,
                                m, m * n, batch));
-  TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W64, V64, batch, true, active, rotated, nrm64, kMaxSweeps, nullptr, &noconv));
-  TN_RETURN_IF(jacobi_finalize<double>(ctx, m, n, W64, V64, order, U, sU, S, sS, V, sV, false, batch));
+  TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W64, want_v ? V64 : nullptr, batch, true, active, rotated, nrm64,
+                                    kMaxSweeps, nullptr, &noconv));
+  TN_RETURN_IF(jacobi_finalize<double>(ctx, m, n, W64, want_v ? V64 : nullptr, order, U, sU, S, sS, want_v ? V : nullptr,
+                                       sV, false, batch));
+  if (noconv) return tn_set_error(ctx, TN_ENOCONV, "Jacobi SVD did not converge within %d sweeps", kMaxSweeps);
+  return TN_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// left singular vectors and values only (m ≥ n): U m×n, S n.  The large-matrix path
+// skips the V accumulation (~43 % of an FP64 sweep's work at m = n); callers recover the
+// right factor they need from U and A.
+// ---------------------------------------------------------------------------------
+size_t svd_left_workspace(tn_precision_t prec, int64_t m, int64_t n, int64_t batch) {
+  return prec == TN_PREC_MIXED ? svd_mixed_workspace(m, n, batch) : svd_workspace<double>(m, n, batch);
+}
+
+tn_status_t svd_left(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_t n, const cxd* A, int64_t lda, int64_t sA,
+                     cxd* U, int64_t sU, double* S, int64_t sS, int64_t batch) {
+  if (m < n) return tn_set_error(ctx, TN_EINVAL, "svd_left: m < n");
+  if (n == 0 || batch == 0) return TN_OK;
+  if (batch > 65535) return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: batch > 65535");
+  if (prec == TN_PREC_MIXED) return svd_tall_mixed(ctx, m, n, A, lda, sA, U, sU, S, sS, nullptr, 0, batch);
+  cxd* W = ws_take<cxd>(ctx, (size_t)(m * n * batch));
+  cxd* V = ws_take<cxd>(ctx, (size_t)(n * n * batch));
+  int* order = ws_take<int>(ctx, (size_t)(n * batch));
+  int* active = ws_take<int>(ctx, (size_t)(batch + 1));
+  int* rotated = ws_take<int>(ctx, (size_t)(batch + 1));
+  double* nrm = ws_take<double>(ctx, (size_t)(n * batch));
+  {
+    int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
+    k_copy_mat<double><<<dim3((unsigned)blocks, (unsigned)batch), 256, 0, ctx->stream>>>(m, n, A, lda, sA, W, m * n,
+                                                                                         batch);
+    TN_LAUNCHED(ctx);
+  }
+  // the one-CTA shared-memory kernel needs V resident; the large path runs without it
+  const bool small = sizeof(cxd) * (size_t)(m * n + n * n) <= kSmemMax && n <= 256;
+  bool noconv = false;
+  ctx->last_sweeps_fp32 = 0;
+  TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W, small ? V : nullptr, batch, false, active, rotated, nrm, kMaxSweeps,
+                                   nullptr, &noconv));
+  TN_RETURN_IF(jacobi_finalize<double>(ctx, m, n, W, nullptr, order, U, sU, S, sS, nullptr, 0, false, batch));
   if (noconv) return tn_set_error(ctx, TN_ENOCONV, "Jacobi SVD did not converge within %d sweeps", kMaxSweeps);
   return TN_OK;
 }
@@ -669,6 +724,15 @@ tn_status_t svd_any(tn_ctx* ctx, tn_dtype_t dt, tn_precision_t prec, int64_t m, 
   if (dt == TN_C32)
     return svd_any_t<float>(ctx, prec, m, n, (const cxf*)A, lda, sA, (cxf*)U, sU, S, sS, (cxf*)Vh, sVh, batch);
   return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: only C64 and C32 are implemented");
+}
+
+extern "C" tn_status_t tn_svd_last_sweeps(tn_ctx* ctx, int32_t* fp32_sweeps, int32_t* fp64_sweeps,
+                                          int32_t* rotations, int32_t n_rot) {
+  if (!ctx) return TN_EINVAL;
+  if (fp32_sweeps) *fp32_sweeps = ctx->last_sweeps_fp32;
+  if (fp64_sweeps) *fp64_sweeps = ctx->last_sweeps_fp64;
+  for (int i = 0; rotations && i < n_rot && i < 64; ++i) rotations[i] = ctx->sweep_rotations[i];
+  return TN_OK;
 }
 
 extern "C" tn_status_t tn_svd_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int64_t m, int64_t n,

@@ -90,15 +90,15 @@ function Base.Array(a::GB300Array{T,N}) where {T,N}
 end
 
 # ---- Muscle-level entry points ---------------------------------------------------------
-# tn_tensor {int32 rank; int64 dims[8]; int32 modes[8]; void* data}
+# tn_tensor {int32 rank; int64 dims[16]; int32 modes[16]; void* data}
 struct TnTensor
     rank::Int32
-    dims::NTuple{8,Int64}
-    modes::NTuple{8,Int32}
+    dims::NTuple{16,Int64}
+    modes::NTuple{16,Int32}
     data::Ptr{Cvoid}
 end
 
-pad8(v, fill) = ntuple(i -> i <= length(v) ? v[i] : fill, 8)
+pad16(v, fill) = ntuple(i -> i <= length(v) ? v[i] : fill, 16)
 
 """
     binary_einsum(a, a_inds, b, b_inds, c_inds; precision=TN_PREC_NATIVE)
@@ -111,9 +111,9 @@ function binary_einsum(a::GB300Array{T}, ai::Vector{Int}, b::GB300Array{T}, bi::
                        precision=TN_PREC_NATIVE) where {T}
     cdims = [i in ai ? size(a, findfirst(==(i), ai)) : size(b, findfirst(==(i), bi)) for i in ci]
     c = GB300Array{T}(undef, Tuple(cdims); ctx=a.ctx)
-    ta = Ref(TnTensor(length(ai), pad8(collect(size(a)), 0), pad8(Int32.(ai), Int32(0)), a.ptr))
-    tb = Ref(TnTensor(length(bi), pad8(collect(size(b)), 0), pad8(Int32.(bi), Int32(0)), b.ptr))
-    tc = Ref(TnTensor(length(ci), pad8(cdims, 0), pad8(Int32.(ci), Int32(0)), c.ptr))
+    ta = Ref(TnTensor(length(ai), pad16(collect(size(a)), 0), pad16(Int32.(ai), Int32(0)), a.ptr))
+    tb = Ref(TnTensor(length(bi), pad16(collect(size(b)), 0), pad16(Int32.(bi), Int32(0)), b.ptr))
+    tc = Ref(TnTensor(length(ci), pad16(cdims, 0), pad16(Int32.(ci), Int32(0)), c.ptr))
     check(ccall((:tn_contract, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int32, Ref{TnTensor}, Ref{TnTensor}, Ref{TnTensor}),
                 a.ctx.h, dtype(T), precision, ta, tb, tc), a.ctx.h)
     return c

@@ -18,7 +18,7 @@ TN_OK, TN_EINVAL, TN_ENOMEM, TN_ENOCONV, TN_ETIMEOUT, TN_ECUDA, TN_EUNSUPPORTED 
 TN_F32, TN_F64, TN_C32, TN_C64 = range(4)
 TN_PREC_NATIVE, TN_PREC_MIXED, TN_PREC_TF32 = 0, 1, 2
 TN_FORM_NONCANONICAL, TN_FORM_MIXED, TN_FORM_BOND = 0, 1, 2
-TN_MAX_RANK = 8
+TN_MAX_RANK = 16
 
 
 class TenetGBError(RuntimeError):
@@ -69,6 +69,9 @@ SIGNATURES = {
     "tn_kernel_launches": (_st, [_vp, _pi64]),
     "tn_last_error_string": (C.c_char_p, [_vp]),
     "tn_version": (C.c_char_p, []),
+    "tn_set_autotune": (_st, [_vp, _i32]),
+    "tn_tuning_dump": (_st, [_vp, C.c_char_p, _sz, C.POINTER(_sz)]),
+    "tn_tuning_load": (_st, [_vp, C.c_char_p]),
     "tn_permute": (_st, [_vp, C.c_int, _i32, _pi64, _pi64, _pi32, _vp, _vp, _i32]),
     "tn_gemm": (
         _st,
@@ -78,6 +81,7 @@ SIGNATURES = {
     "tn_contract": (_st, [_vp, C.c_int, C.c_int, C.POINTER(tn_tensor), C.POINTER(tn_tensor), C.POINTER(tn_tensor)]),
     "tn_qr_thin": (_st, [_vp, C.c_int, C.c_int, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _i64]),
     "tn_svd_thin": (_st, [_vp, C.c_int, C.c_int, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64]),
+    "tn_svd_last_sweeps": (_st, [_vp, _pi32, _pi32, _pi32, _i32]),
     "tn_truncation_rank": (_st, [_vp, _vp, _i64, _i64, _dbl, _pi64]),
     "tn_hadamard": (_st, [_vp, C.c_int, _i32, _pi64, _i32, _vp, _vp, _vp]),
     "tn_norm2": (_st, [_vp, C.c_int, _i64, _vp, _pdbl]),

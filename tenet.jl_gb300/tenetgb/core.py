@@ -107,6 +107,26 @@ class Context:
         self.check(self.lib.tn_hbm_in_use(self.h, C.byref(v)))
         return v.value
 
+    def set_autotune(self, enable=True):
+        """Time candidate launch configurations on the first call of each new shape and
+        keep the fastest (per context)."""
+        self.check(self.lib.tn_set_autotune(self.h, int(bool(enable))))
+
+    def tuning(self):
+        """The autotuner's table as text (one "key v1 v2" line per shape)."""
+        n = C.c_size_t()
+        self.check(self.lib.tn_tuning_dump(self.h, None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        self.check(self.lib.tn_tuning_dump(self.h, buf, n.value, None))
+        return buf.value.decode()
+
+    def load_tuning(self, text):
+        self.check(self.lib.tn_tuning_load(self.h, text.encode()))
+
+    def save_tuning(self, path):
+        with open(path, "w") as f:
+            f.write(self.tuning())
+
     def launches(self):
         v = C.c_int64()
         self.check(self.lib.tn_kernel_launches(self.h, C.byref(v)))
