@@ -20,6 +20,7 @@
 // t = sgn(ζ)/(|ζ|+√(1+ζ²)), c = 1/√(1+t²), s = c·t:
 //   w_i' = c·w_i − s·e^{−iφ}·w_j,   w_j' = s·e^{iφ}·w_i + c·w_j.
 #include <algorithm>
+#include <mutex>
 
 #include "tn_internal.cuh"
 
@@ -724,6 +725,142 @@ tn_status_t svd_any(tn_ctx* ctx, tn_dtype_t dt, tn_precision_t prec, int64_t m, 
   if (dt == TN_C32)
     return svd_any_t<float>(ctx, prec, m, n, (const cxf*)A, lda, sA, (cxf*)U, sU, S, sS, (cxf*)Vh, sVh, batch);
   return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: only C64 and C32 are implemented");
+}
+
+// ---------------------------------------------------------------------------------
+// Allocation-free thin SVD.
+//
+// Some callers cannot allocate device memory at the point where they need an SVD: code
+// that runs while a CUDA graph is being captured by someone else, real-time loops whose
+// memory was fixed up front, or hosts that hand the library a stream but no allocator.
+// tn_svd_thin_noalloc serves them: it takes only the caller's input and output buffers
+// and keeps its scratch (W, V, column norms, the sort order and two flag words) in one
+// file-scope device array of kNoAllocScratchBytes.  Every GPU that loads the library
+// holds that array until the process exits.
+// ---------------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB per device
+__device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+constexpr int kNoAllocMaxDevices = 64;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {nullptr};
+
+// The host-side name g_noalloc_scratch is only a stand-in for the device array; its
+// device address is looked up once per device (with that device current) and cached.
+tn_status_t noalloc_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return tn_set_error(nullptr, TN_ECUDA, "tn_svd_thin_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return tn_set_error(nullptr, TN_EUNSUPPORTED, "tn_svd_thin_noalloc: device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return tn_set_error(nullptr, TN_ECUDA, "tn_svd_thin_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    g_noalloc_addr[dev] = p;
+  }
+  *out = g_noalloc_addr[dev];
+  return TN_OK;
+}
+
+__global__ void k_noalloc_flags(int* active, int* rotated) {
+  if (threadIdx.x == 0) {
+    *active = 1;
+    *rotated = 0;
+  }
+}
+
+inline size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+}  // namespace
+
+extern "C" tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, const void* d_A, int64_t lda,
+                                          void* d_U, double* d_S, void* d_Vh) {
+  if (m < 1 || n < 1 || m < n)
+    return tn_set_error(nullptr, TN_EINVAL, "tn_svd_thin_noalloc: need m >= n >= 1 (pass the adjoint for m < n)");
+  if (lda < m) return tn_set_error(nullptr, TN_EINVAL, "tn_svd_thin_noalloc: lda < m");
+  if (!d_A || !d_U || !d_S || !d_Vh) return tn_set_error(nullptr, TN_EINVAL, "tn_svd_thin_noalloc: null pointer");
+  // scratch layout: W (m×n) | V (n×n) | column norms (n) | order (n) | active | rotated
+  const size_t oW = 0, oV = oW + al256(sizeof(cxd) * (size_t)(m * n)), oN = oV + al256(sizeof(cxd) * (size_t)(n * n)),
+               oO = oN + al256(sizeof(double) * (size_t)n), oF = oO + al256(sizeof(int) * (size_t)n),
+               total = oF + 256;
+  if (total > kNoAllocScratchBytes)
+    return tn_set_error(nullptr, TN_EINVAL,
+                        "tn_svd_thin_noalloc: %lld x %lld needs %zu bytes of scratch; the limit is %zu "
+                        "((m*n + n*n)*16 + n*12 + ~1 KiB <= 16 MiB, e.g. 1024 x 512)",
+                        (long long)m, (long long)n, total, kNoAllocScratchBytes);
+  void* base = nullptr;
+  TN_RETURN_IF(noalloc_scratch(&base));
+  char* sc = static_cast<char*>(base);
+  cxd* W = reinterpret_cast<cxd*>(sc + oW);
+  cxd* V = reinterpret_cast<cxd*>(sc + oV);
+  double* nrm = reinterpret_cast<double*>(sc + oN);
+  int* order = reinterpret_cast<int*>(sc + oO);
+  int* active = reinterpret_cast<int*>(sc + oF);
+  int* rotated = active + 1;
+  cudaStream_t st = (cudaStream_t)stream;
+#define NA_CHECK(call)                                                                                      \
+  do {                                                                                                      \
+    cudaError_t _e = (call);                                                                                \
+    if (_e != cudaSuccess)                                                                                  \
+      return tn_set_error(nullptr, TN_ECUDA, "tn_svd_thin_noalloc: %s: %s", #call, cudaGetErrorString(_e)); \
+  } while (0)
+  // the array keeps the previous call's contents: everything read below is written first
+  k_copy_mat<double><<<(unsigned)std::min<int64_t>((m * n + 255) / 256, 2048), 256, 0, st>>>(
+      m, n, (const cxd*)d_A, lda, 0, W, m * n, 1);
+  NA_CHECK(cudaGetLastError());
+  k_identity<double><<<(unsigned)std::min<int64_t>((n * n + 255) / 256, 2048), 256, 0, st>>>(n, V, n * n, 1);
+  NA_CHECK(cudaGetLastError());
+  k_noalloc_flags<<<1, 32, 0, st>>>(active, rotated);
+  NA_CHECK(cudaGetLastError());
+  const double tol = jacobi_tol<double>(m);
+  const int N = (int)(n + (n & 1));
+  const dim3 grid(N / 2, 1);
+  bool converged = false;
+  for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
+    NA_CHECK(cudaMemsetAsync(rotated, 0, sizeof(int), st));
+    k_col_norms<double><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, 1216)), 256, 0, st>>>(
+        m, n, W, m * n, nrm, 1);
+    NA_CHECK(cudaGetLastError());
+    for (int r = 0; r < N - 1; ++r) {
+      if (m <= 512)
+        k_jacobi_step_reg<double, 128, 4, false><<<grid, 128, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
+                                                                        rotated, tol);
+      else if (m <= 1024)
+        k_jacobi_step_reg<double, 256, 4, false><<<grid, 256, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
+                                                                        rotated, tol);
+      else if (m <= 2048)
+        k_jacobi_step_reg<double, 256, 8, false><<<grid, 256, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
+                                                                        rotated, tol);
+      else
+        k_jacobi_step_reg<double, 256, 16, false><<<grid, 256, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
+                                                                         rotated, tol);
+      NA_CHECK(cudaGetLastError());
+    }
+    int h_rot = 0;  // host stack word: no allocation
+    NA_CHECK(cudaMemcpyAsync(&h_rot, rotated, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NA_CHECK(cudaStreamSynchronize(st));
+    converged = h_rot == 0;
+  }
+  int P2 = 1;
+  while (P2 < n) P2 <<= 1;
+  const size_t smem = (sizeof(double) + sizeof(int)) * (size_t)P2;
+  if (smem > 48 * 1024)
+    NA_CHECK(cudaFuncSetAttribute(k_svd_order<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+  k_svd_order<double><<<1, 512, smem, st>>>(m, n, W, m * n, d_S, 0, order);
+  NA_CHECK(cudaGetLastError());
+  k_svd_gather<double><<<dim3((unsigned)std::min<int64_t>((m * n + 255) / 256, 1024), 1), 256, 0, st>>>(
+      m, n, W, m * n, V, n * n, d_S, 0, order, (cxd*)d_U, 0, (cxd*)d_Vh, 0, true, 1);
+  NA_CHECK(cudaGetLastError());
+  NA_CHECK(cudaStreamSynchronize(st));
+#undef NA_CHECK
+  if (!converged)
+    return tn_set_error(nullptr, TN_ENOCONV, "tn_svd_thin_noalloc: no convergence within %d sweeps", kMaxSweeps);
+  return TN_OK;
 }
 
 extern "C" tn_status_t tn_svd_last_sweeps(tn_ctx* ctx, int32_t* fp32_sweeps, int32_t* fp64_sweeps,

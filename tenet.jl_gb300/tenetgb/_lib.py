@@ -82,6 +82,7 @@ SIGNATURES = {
     "tn_qr_thin": (_st, [_vp, C.c_int, C.c_int, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _i64]),
     "tn_svd_thin": (_st, [_vp, C.c_int, C.c_int, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64]),
     "tn_svd_last_sweeps": (_st, [_vp, _pi32, _pi32, _pi32, _i32]),
+    "tn_svd_thin_noalloc": (_st, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _vp]),
     "tn_truncation_rank": (_st, [_vp, _vp, _i64, _i64, _dbl, _pi64]),
     "tn_hadamard": (_st, [_vp, C.c_int, _i32, _pi64, _i32, _vp, _vp, _vp]),
     "tn_norm2": (_st, [_vp, C.c_int, _i64, _vp, _pdbl]),
