@@ -219,9 +219,15 @@ tn_status_t gemm_mixed_c64(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n
 
 static bool valid_op(char c) { return c == 'N' || c == 'T' || c == 'C'; }
 
+// The tensor path pays an operand-preparation pass (split + 4M expansion) and 128×128
+// tiles; skinny GEMMs (any of m, n < 64 or k < 32) are HBM-bound and stay on the FP32
+// CUDA cores, which are also the more accurate choice.
+static bool use_tensor_path(tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n, int64_t k) {
+  return (dt == TN_C32 || dt == TN_F32) && prec != TN_PREC_NATIVE && m >= 64 && n >= 64 && k >= 32;
+}
+
 size_t gemm_any_workspace(tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t n, int64_t k) {
-  if ((dt == TN_C32 || dt == TN_F32) && prec != TN_PREC_NATIVE)
-    return tc_gemm_workspace(dt == TN_C32, prec == TN_PREC_TF32 ? 1 : 3, m, n, k);
+  if (use_tensor_path(dt, prec, m, n, k)) return tc_gemm_workspace(dt == TN_C32, prec == TN_PREC_TF32 ? 1 : 3, m, n, k);
   return 0;
 }
 
@@ -229,7 +235,7 @@ tn_status_t gemm_any(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, char op
                      int64_t k, const double* alpha, const void* A, int64_t lda, int64_t strideA, const void* B,
                      int64_t ldb, int64_t strideB, const double* beta, void* C, int64_t ldc, int64_t strideC,
                      int64_t batch) {
-  const bool tc = (dtype == TN_C32 || dtype == TN_F32) && prec != TN_PREC_NATIVE;
+  const bool tc = use_tensor_path(dtype, prec, m, n, k);
   if (tc) {
     if (dtype == TN_C32 && (alpha[1] != 0.0 || beta[1] != 0.0))
       return tn_set_error(ctx, TN_EUNSUPPORTED, "tensor-core GEMM: complex alpha/beta not supported");

@@ -301,8 +301,16 @@ unsigned blocks_for(tn_ctx* ctx, int64_t n) {
 }  // namespace
 
 // Workspace (bytes) for tc_gemm on the given shape.
+// K-major operands are stored with K padded to a multiple of 4 floats (the 16-byte TMA
+// pitch rule) and at least one 32-float box; the last box reads past K as zeros.
+static inline int64_t padded_k(bool complex_in, int64_t k) {
+  int64_t kk = complex_in ? 2 * k : k;
+  kk = (kk + 3) / 4 * 4;
+  return kk < 32 ? 32 : kk;
+}
+
 size_t tc_gemm_workspace(bool complex_in, int passes, int64_t m, int64_t n, int64_t k) {
-  const int64_t Kp = ((complex_in ? 2 * k : k) + 31) / 32 * 32;
+  const int64_t Kp = padded_k(complex_in, k);
   const int64_t Ma = complex_in ? 2 * m : m;
   const int copies = passes > 1 ? 2 : 1;
   return copies * (ws_round(4 * (size_t)(Ma * Kp)) + ws_round(4 * (size_t)(n * Kp))) + ws_round(sizeof(int) * 4);
@@ -314,7 +322,7 @@ size_t tc_gemm_workspace(bool complex_in, int passes, int64_t m, int64_t n, int6
 tn_status_t tc_gemm(tn_ctx* ctx, bool complex_in, int passes, char opa, char opb, int64_t m, int64_t n, int64_t k,
                     float alpha, const void* A, int64_t lda, const void* B, int64_t ldb, float beta, void* C, int64_t ldc) {
   if (m == 0 || n == 0) return TN_OK;
-  const int64_t Kp = ((complex_in ? 2 * k : k) + 31) / 32 * 32;
+  const int64_t Kp = padded_k(complex_in, k);
   const int64_t Ma = complex_in ? 2 * m : m;
   if (Ma > (1ll << 31) - 128 || n > (1ll << 31) - 128) return tn_set_error(ctx, TN_EUNSUPPORTED, "tc_gemm: too large");
   const bool split = passes > 1;

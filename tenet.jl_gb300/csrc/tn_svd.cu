@@ -153,6 +153,11 @@ __global__ void __launch_bounds__(NT)
     be = nrm[b * n + j];
   }
   Rot<T> Rt = make_rot(al, be, g, tol);
+  if (threadIdx.x == 0 && al > T(0) && be > T(0)) {
+    // largest off-diagonal ratio of the sweep (positive floats order like their bits)
+    const float ratio = (float)(sqrt(abs2(g)) / sqrt(al * be));
+    atomicMax(&rotated[gridDim.y + b], __float_as_int(ratio));
+  }
   if (!Rt.apply) return;
   if (threadIdx.x == 0) {
     atomicAdd(&rotated[b], 1);
@@ -370,8 +375,8 @@ __global__ void k_svd_gather(int64_t m, int64_t n, const cx<T>* W, int64_t sW, c
 template <typename T>
 size_t svd_workspace(int64_t m, int64_t n, int64_t batch) {
   return ws_round(sizeof(cx<T>) * (size_t)(m * n * batch)) + ws_round(sizeof(cx<T>) * (size_t)(n * n * batch)) +
-         ws_round(sizeof(int) * (size_t)(n * batch)) + 2 * ws_round(sizeof(int) * (size_t)(batch + 1)) +
-         ws_round(sizeof(T) * (size_t)(n * batch));
+         ws_round(sizeof(int) * (size_t)(n * batch)) + ws_round(sizeof(int) * (size_t)(batch + 1)) +
+         ws_round(sizeof(int) * (size_t)(2 * batch + 2)) + ws_round(sizeof(T) * (size_t)(n * batch));
 }
 template size_t svd_workspace<double>(int64_t, int64_t, int64_t);
 template size_t svd_workspace<float>(int64_t, int64_t, int64_t);
@@ -428,9 +433,13 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       k_identity<T><<<dim3((unsigned)blocks, gy), 256, 0, ctx->stream>>>(n, V, n * n, batch);
       TN_LAUNCHED(ctx);
     }
-    std::vector<int> h_act(batch, 1), h_rot(batch);
+    std::vector<int> h_act(batch, 1), h_rot(2 * batch);
     TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
     const int N = (int)(n + (n & 1));
+    // A sweep whose largest off-diagonal ratio is ρ leaves ~ρ² for the next one
+    // (one-sided Jacobi converges quadratically); when ρ² is far below tol the next
+    // sweep would rotate nothing and is skipped.
+    const double stop_ratio = sqrt((double)tol * 1e-2);
     // graph for one sweep
     char key[256];
     snprintf(key, sizeof(key), "jac%zu:%lld:%lld:%lld:%p:%p:%p:%p:%p", sizeof(T), (long long)m, (long long)n,
@@ -446,7 +455,7 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       }
       cudaGraph_t g = nullptr;
       TN_CHECK_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      cudaMemsetAsync(rotated, 0, sizeof(int) * batch, ctx->stream);
+      cudaMemsetAsync(rotated, 0, sizeof(int) * 2 * batch, ctx->stream);
       int64_t nb = std::min<int64_t>((n * batch * 32 + 255) / 256, (int64_t)ctx->num_sms * 8);
       k_col_norms<T><<<(unsigned)std::max<int64_t>(nb, 1), 256, 0, ctx->stream>>>(m, n, W, m * n, nrm, batch);
       tn_status_t st = TN_OK;
@@ -467,12 +476,15 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
     for (sweeps = 0; sweeps < max_sweeps && n_active > 0; ++sweeps) {
       TN_CHECK_CUDA(ctx, cudaGraphLaunch(ge, ctx->stream));
       ctx->launches += N;  // norm refresh + N-1 steps
-      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * batch, cudaMemcpyDeviceToHost, ctx->stream));
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * 2 * batch, cudaMemcpyDeviceToHost,
+                                         ctx->stream));
       TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
       if (sweeps < (int)(sizeof(ctx->sweep_rotations) / sizeof(int))) ctx->sweep_rotations[sweeps] = h_rot[0];
       n_active = 0;
       for (int64_t b = 0; b < batch; ++b) {
-        h_act[b] = h_act[b] && h_rot[b];
+        float ratio;
+        memcpy(&ratio, &h_rot[batch + b], sizeof(float));
+        h_act[b] = h_act[b] && h_rot[b] && ratio > stop_ratio;
         n_active += h_act[b];
       }
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
@@ -520,7 +532,7 @@ static tn_status_t svd_tall_impl(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>*
   cx<T>* V = ws_take<cx<T>>(ctx, (size_t)(n * n * batch));
   int* order = ws_take<int>(ctx, (size_t)(n * batch));
   int* active = ws_take<int>(ctx, (size_t)(batch + 1));
-  int* rotated = ws_take<int>(ctx, (size_t)(batch + 1));
+  int* rotated = ws_take<int>(ctx, (size_t)(2 * batch + 2));
   T* nrm = ws_take<T>(ctx, (size_t)(n * batch));
   {
     int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
@@ -548,9 +560,9 @@ template tn_status_t svd_tall_cx<float>(tn_ctx*, int64_t, int64_t, const cxf*, i
 // ---------------------------------------------------------------------------------
 // mixed precision (C64 data): the Jacobi sweeps run first in FP32 — on GB300 the FP32
 // pipe is ~64× the FP64 pipe — until the columns are orthogonal to FP32 accuracy.  The
-// FP32 rotations V32 are lifted to FP64, re-orthonormalised by two Newton–Schulz steps
-// V ← V (3I − VᴴV)/2, and W = A·V is formed in FP64; the FP64 Jacobi sweeps then only
-// remove the O(1e-6) residual (quadratic convergence: 2–3 sweeps instead of ~9).
+// FP32 rotations V32 are lifted to FP64, re-orthonormalised by one series step
+// V ← V (I − E/2 + 3E²/8 − 5E³/16), E = VᴴV − I, and W = A·V is formed in FP64; the FP64 Jacobi
+// sweeps then only remove the O(1e-5) residual (quadratic convergence: two sweeps).
 // Rotations, σ and the truncation decision stay FP64.
 // ---------------------------------------------------------------------------------
 __global__ void k_d2f(int64_t count, const cxd* __restrict__ a, int64_t lda, int64_t rows, cxf* __restrict__ b) {
@@ -567,6 +579,29 @@ __global__ void k_f2d(int64_t count, const cxf* __restrict__ a, cxd* __restrict_
   }
 }
 
+// E = G − I as complex float (G = VᴴV, n×n per matrix, dense; E at batch stride sE)
+__global__ void k_gram_minus_identity_f32(int64_t n, int64_t batch, const cxd* G, cxf* E, int64_t sE) {
+  const int64_t total = n * n * batch;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / (n * n), w = t % (n * n), r = w % n, c = w / n;
+    cxd g = G[t];
+    E[b * sE + w] = mkcx<float>((float)(g.x - (r == c ? 1.0 : 0.0)), (float)g.y);
+  }
+}
+// G ← I − E/2 + 3E²/8 − 5E³/16 with E = G − I (FP64), E² (stride n²) and E³ (stride sE3)
+// in FP32
+__global__ void k_ortho_poly(int64_t n, int64_t batch, cxd* G, const cxf* E2, const cxf* E3, int64_t sE3) {
+  const int64_t total = n * n * batch;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / (n * n), w = t % (n * n), r = w % n, c = w / n;
+    const double id = r == c ? 1.0 : 0.0;
+    const cxd g = G[t];
+    const cxf e2 = E2[t], e3 = E3[b * sE3 + w];
+    G[t] = mkcx<double>(id - 0.5 * (g.x - id) + 0.375 * (double)e2.x - 0.3125 * (double)e3.x,
+                        -0.5 * g.y + 0.375 * (double)e2.y - 0.3125 * (double)e3.y);
+  }
+}
+
 size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
   size_t s = 0;
   s += ws_round(sizeof(cxf) * (size_t)(m * n * batch));      // W32
@@ -574,9 +609,10 @@ size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
   s += ws_round(sizeof(cxd) * (size_t)(m * n * batch));      // W64
   s += 2 * ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // V64, G
   s += ws_round(sizeof(int) * (size_t)(n * batch));
-  s += 2 * ws_round(sizeof(int) * (size_t)(batch + 1));
+  s += ws_round(sizeof(int) * (size_t)(batch + 1)) + ws_round(sizeof(int) * (size_t)(2 * batch + 2));
   s += ws_round(sizeof(double) * (size_t)(n * batch)) + ws_round(sizeof(float) * (size_t)(n * batch));
   s += ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // V scratch when V is not wanted
+  s += ws_round(sizeof(cxf) * (size_t)(n * n * batch));  // E³ when W32 has no room for it
   return s;
 }
 
@@ -592,6 +628,7 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   cxd* W64 = ws_take<cxd>(ctx, (size_t)(m * n * batch));
   cxd* V64 = ws_take<cxd>(ctx, (size_t)(n * n * batch));
   cxd* G = ws_take<cxd>(ctx, (size_t)(n * n * batch));
+  cxf* G3 = ws_take<cxf>(ctx, (size_t)(n * n * batch));
   cxd* Vt = want_v ? nullptr : ws_take<cxd>(ctx, (size_t)(n * n * batch));
   if (!want_v) {
     V = Vt;
@@ -599,7 +636,7 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   }
   int* order = ws_take<int>(ctx, (size_t)(n * batch));
   int* active = ws_take<int>(ctx, (size_t)(batch + 1));
-  int* rotated = ws_take<int>(ctx, (size_t)(batch + 1));
+  int* rotated = ws_take<int>(ctx, (size_t)(2 * batch + 2));
   double* nrm64 = ws_take<double>(ctx, (size_t)(n * batch));
   float* nrm32 = ws_take<float>(ctx, (size_t)(n * batch));
   for (int64_t b = 0; b < batch; ++b) {
@@ -615,20 +652,37 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
     k_f2d<<<(unsigned)blocks, 256, 0, ctx->stream>>>(cnt, V32, V64);
     TN_LAUNCHED(ctx);
   }
-  // Two Newton–Schulz steps  G = VᴴV ; V ← 1.5 V − 0.5 V G  (unitarity error e → 1.5e²:
-  // FP32's ~1e-5 reaches the FP64 floor after two), ping-ponging between V64 and V
-  for (int it = 0; it < 2; ++it) {
-    cxd* src = it == 0 ? V64 : V;
-    cxd* dst = it == 0 ? V : V64;
-    const int64_t s_src = it == 0 ? n * n : sV, s_dst = it == 0 ? sV : n * n;
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', n, n, n, mkcx(1.0, 0.0), src, n, s_src, src, n, s_src, mkcx(0.0, 0.0),
-                                 G, n, n * n, batch));
-    for (int64_t b = 0; b < batch; ++b)
-      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(dst + b * s_dst, src + b * s_src, sizeof(cxd) * n * n,
-                                         cudaMemcpyDeviceToDevice, ctx->stream));
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', n, n, n, mkcx(-0.5, 0.0), src, n, s_src, G, n, n * n, mkcx(1.5, 0.0),
-                                 dst, n, s_dst, batch));
+  // One orthonormalisation step: with E = VᴴV − I (FP64 GEMM),
+  //   V ← V (I − E/2 + 3E²/8 − 5E³/16)   (the (I + E)^{-1/2} series; residual ~ (35/128)E⁴)
+  // FP32 rotation accumulation leaves |E| ~ 1e-4, so E² and E³ need only ~1e-4 relative
+  // accuracy: both are FP32 GEMMs.
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', n, n, n, mkcx(1.0, 0.0), V64, n, n * n, V64, n, n * n, mkcx(0.0, 0.0), G,
+                               n, n * n, batch));
+  {
+    const int64_t cnt = n * n * batch;
+    const unsigned blocks = (unsigned)std::min<int64_t>((cnt + 255) / 256, 4096);
+    // E (as FP32, in the W32 scratch: m ≥ n) and E² (in V32, no longer needed)
+    // E in W32[0 : n²], E² in V32, E³ in W32[n² : 2n²] (W32 holds m·n ≥ n² per matrix; the
+    // second half is used only when m ≥ 2n, otherwise E³ goes to a slot after E²)
+    cxf* E = W32;
+    cxf* E2 = V32;
+    cxf* E3 = (m >= 2 * n) ? W32 + n * n : nullptr;
+    const int64_t sE = m * n;
+    k_gram_minus_identity_f32<<<blocks, 256, 0, ctx->stream>>>(n, batch, G, E, sE);
+    TN_LAUNCHED(ctx);
+    TN_RETURN_IF(gemm_cx<float>(ctx, 'N', 'N', n, n, n, mkcx(1.0f, 0.0f), E, n, sE, E, n, sE, mkcx(0.0f, 0.0f), E2, n,
+                                n * n, batch));
+    if (!E3) E3 = G3;
+    TN_RETURN_IF(gemm_cx<float>(ctx, 'N', 'N', n, n, n, mkcx(1.0f, 0.0f), E2, n, n * n, E, n, sE, mkcx(0.0f, 0.0f), E3,
+                                n, (E3 == W32 + n * n) ? sE : n * n, batch));
+    k_ortho_poly<<<blocks, 256, 0, ctx->stream>>>(n, batch, G, E2, E3, (E3 == W32 + n * n) ? sE : n * n);
+    TN_LAUNCHED(ctx);
   }
+  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', n, n, n, mkcx(1.0, 0.0), V64, n, n * n, G, n, n * n, mkcx(0.0, 0.0), V,
+                               n, sV, batch));
+  for (int64_t b = 0; b < batch; ++b)
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(V64 + b * n * n, V + b * sV, sizeof(cxd) * n * n, cudaMemcpyDeviceToDevice,
+                                       ctx->stream));
   // W = A V  (FP64)
   TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, n, mkcx(1.0, 0.0), A, lda, sA, V64, n, n * n, mkcx(0.0, 0.0), W64,
                                m, m * n, batch));
@@ -659,7 +713,7 @@ tn_status_t svd_left(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_t n, con
   cxd* V = ws_take<cxd>(ctx, (size_t)(n * n * batch));
   int* order = ws_take<int>(ctx, (size_t)(n * batch));
   int* active = ws_take<int>(ctx, (size_t)(batch + 1));
-  int* rotated = ws_take<int>(ctx, (size_t)(batch + 1));
+  int* rotated = ws_take<int>(ctx, (size_t)(2 * batch + 2));
   double* nrm = ws_take<double>(ctx, (size_t)(n * batch));
   {
     int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
@@ -822,7 +876,7 @@ extern "C" tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, c
   const dim3 grid(N / 2, 1);
   bool converged = false;
   for (int sweep = 0; sweep < kMaxSweeps && !converged; ++sweep) {
-    NA_CHECK(cudaMemsetAsync(rotated, 0, sizeof(int), st));
+    NA_CHECK(cudaMemsetAsync(rotated, 0, 2 * sizeof(int), st));
     k_col_norms<double><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, 1216)), 256, 0, st>>>(
         m, n, W, m * n, nrm, 1);
     NA_CHECK(cudaGetLastError());

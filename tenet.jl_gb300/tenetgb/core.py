@@ -313,6 +313,12 @@ def norm(t: DeviceTensor):
     return v.value
 
 
+def scale(t: DeviceTensor, s):
+    """t ← s·t in place (real s)."""
+    t.ctx.check(t.ctx.lib.tn_scale(t.ctx.h, t.code, t.size, C.c_void_p(t.ptr), float(s)))
+    return t
+
+
 def simple_update(A: DeviceTensor, ia, B: DeviceTensor, ib, bond, op: DeviceTensor, oa, ob, maxdim=None,
                   threshold=None, precision="native"):
     """Muscle.simple_update(A, ia, B, ib, bond, op, oa, ob; maxdim, absorb=AbsorbEqually()).

@@ -17,7 +17,8 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .core import Context, DeviceTensor, binary_einsum, default_context
+from .core import Context, DeviceTensor, binary_einsum, default_context, scale
+from .core import norm as tensor_norm
 
 
 @dataclass
@@ -190,11 +191,14 @@ def path_flops(labels_list, dims, path):
 
 
 def contract(net: Network, path=None, precision="mixed", dtype=None, ctx: Context | None = None,
-             max_size=2**28, timing=False):
+             max_size=2**28, timing=False, rescale=True):
     """Contract ``net`` to a scalar on the GPU along ``path`` (greedy by default).
 
-    ``dtype`` overrides the storage type (e.g. complex128 for the FP64 run).  Returns the
-    scalar, or (scalar, stats) with ``timing``."""
+    ``dtype`` overrides the storage type (e.g. complex128 for the FP64 run).  With
+    ``rescale`` every intermediate is divided by its norm (an FP64 reduction) and the log
+    of the scale is carried in FP64: a closed 8×8 network of unit-norm tensors has a
+    value near 1e-51, below the FP32 range, so unscaled FP32 intermediates underflow.
+    Returns the scalar (complex128), or (scalar, stats) with ``timing``."""
     ctx = ctx or default_context()
     if path is None:
         path = greedy_path(net.labels, net.dims, max_size)
@@ -207,6 +211,7 @@ def contract(net: Network, path=None, precision="mixed", dtype=None, ctx: Contex
         for lab in labs:
             counts[lab] = counts.get(lab, 0) + 1
     nxt = len(net.arrays)
+    log_scale = 0.0
     t0 = time.perf_counter()
     for a, b in path:
         ta, tb = live.pop(a), live.pop(b)
@@ -215,11 +220,19 @@ def contract(net: Network, path=None, precision="mixed", dtype=None, ctx: Contex
         contracted = [x for x in shared if x not in out]
         for x in contracted:
             counts[x] -= 2
-        live[nxt] = binary_einsum(ta, tb, dims=contracted, out_inds=out, precision=precision)
+        res = binary_einsum(ta, tb, dims=contracted, out_inds=out, precision=precision)
+        if rescale:
+            nrm = tensor_norm(res)
+            if nrm > 0 and np.isfinite(nrm):
+                scale(res, 1.0 / nrm)
+                log_scale += math.log(nrm)
+        live[nxt] = res
         del ta, tb
         nxt += 1
     (res,) = live.values()
-    val = complex(res.numpy().reshape(-1)[0]) if res.size == 1 else res.numpy()
+    val = res.numpy().astype(np.complex128)
+    val = complex(val.reshape(-1)[0]) if res.size == 1 else val
+    val = val * math.exp(log_scale) if log_scale > -700 else complex(np.float64(val) * np.exp(np.float64(log_scale)))
     if not timing:
         return val
     ctx.sync()
