@@ -421,6 +421,194 @@ def run_lattice(args):
                       "path_flops": flops, "modes": res, "data": "synthetic (seeded Gaussian C32, seed 4)"}))
 
 
+def run_kernels(args):
+    """Kernel rooflines outside the TEBD step: the permutation kernel on 1 GiB ComplexF64
+    tensors (bytes = 2·numel·16, against the measured HBM copy rate) and the contraction
+    GEMMs at 4096³ (C32 on the tcgen05 tensor pipe in TF32 and 3×TF32, counted as real
+    tensor-core flops 2·(2m)·n·(2k) per pass against half the measured BF16 rate, the
+    dense TF32 rate; C64 on the FP64 pipe).  Each figure is the best of 5 launches timed
+    with CUDA events.  Prints one JSON line (a secondary workload)."""
+    import ctypes as C
+
+    import torch
+
+    import tenetgb
+
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+    hbm, tf32 = peaks["hbm_gbs"], peaks["bf16_tflops"] / 2
+    ctx = tenetgb.Context(0)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def best(fn, reps=5):
+        fn()
+        ctx.sync()
+        ts = []
+        for _ in range(reps):
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return min(ts)
+
+    out = {"permute": [], "gemm": []}
+    for dims, perm in [((1024, 1024, 64), (2, 0, 1)), ((1024, 1024, 64), (1, 0, 2)), ((64, 2, 1024, 2, 256), (2, 0, 4, 1, 3)),
+                       ((512, 512, 256), (0, 2, 1))]:
+        numel = int(np.prod(dims))
+        src = ctx.alloc(numel * 16)
+        dst = ctx.alloc(numel * 16)
+        rank = len(dims)
+        cd = (C.c_int64 * rank)(*dims)
+        st = [1]
+        for x in dims[:-1]:
+            st.append(st[-1] * x)
+        cs = (C.c_int64 * rank)(*st)
+        cp = (C.c_int32 * rank)(*perm)
+
+        def f():
+            ctx.check(ctx.lib.tn_permute(ctx.h, 3, rank, cd, cs, cp, C.c_void_p(src), C.c_void_p(dst), 0))
+
+        ms = best(f)
+        gbs = 2 * numel * 16 / (ms * 1e-3) / 1e9
+        out["permute"].append({"dims": list(dims), "perm": list(perm), "ms": ms, "GB/s": gbs, "frac_hbm": gbs / hbm})
+        ctx.free(src)
+        ctx.free(dst)
+    N = 4096
+    one, zero = (C.c_double * 2)(1, 0), (C.c_double * 2)(0, 0)
+    for dt, prec, label, passes in [(2, 2, "c32_tf32", 1), (2, 1, "c32_3xtf32", 3), (2, 0, "c32_fp32_cuda_cores", 0),
+                                    (3, 0, "c64_fp64", 0)]:
+        n = N if dt == 2 else 2048
+        tdt = torch.complex64 if dt == 2 else torch.complex128
+        A = torch.randn(n, n, dtype=tdt, device="cuda")
+        B = torch.randn(n, n, dtype=tdt, device="cuda")
+        Cc = torch.empty(n, n, dtype=tdt, device="cuda")
+        torch.cuda.synchronize()
+
+        def g():
+            ctx.check(ctx.lib.tn_gemm(ctx.h, dt, prec, b"N", b"N", n, n, n, one, C.c_void_p(A.data_ptr()), n, 0,
+                                      C.c_void_p(B.data_ptr()), n, 0, zero, C.c_void_p(Cc.data_ptr()), n, 0, 1))
+
+        ms = best(g)
+        cplx = 8 * n**3 / (ms * 1e-3) / 1e12
+        e = {"kind": label, "n": n, "ms": ms, "complex_algorithmic_tflops": cplx}
+        if passes:
+            real = passes * 2 * (2 * n) * n * (2 * n) / (ms * 1e-3) / 1e12
+            e.update({"tensor_tflops": real, "frac_tf32_peak": real / tf32})
+        out["gemm"].append(e)
+        del A, B, Cc
+    print(json.dumps({"metric": "kernel_rooflines", "hbm_peak_gbs": hbm, "tf32_dense_peak_tflops": tf32,
+                      "peak_source": "MEASURED_PEAKS.json (TF32 dense = BF16 / 2)", **out}))
+
+
+def batched_flops(Ls, chis, maxdims, d=2):
+    """Algorithmic flops of canonize!(ψ, L) → compress!(ψ; maxdim) for the given shapes
+    (complex: QR 4(2mn² − ⅔n³) ×2 with Q; SVD 4(4m²n + 8mn² + 9n³); GEMM 8mnk)."""
+    from tenetgb import workloads as W
+
+    def qr(m, n):
+        return 2 * 4 * (2 * m * n * n - 2 * n**3 / 3)
+
+    def svd(m, n):
+        m, n = max(m, n), min(m, n)
+        return 4 * (4 * m * m * n + 8 * m * n * n + 9 * n**3)
+
+    tot = 0.0
+    for L, chi, md in zip(Ls, chis, maxdims):
+        b = [1] + W.clamped_bonds(L, d, chi) + [1]
+        for k in range(1, L):  # QR sweep: A_k (b[k-1] d × b[k]), R·A_{k+1}
+            tot += qr(b[k - 1] * d, b[k]) + 8 * b[k] * b[k] * d * b[k + 1]
+        for i in range(L, 1, -1):  # LQ sweep
+            tot += qr(d * b[i], b[i - 1]) + 8 * b[i - 2] * d * b[i - 1] * b[i - 1]
+        prev = 1
+        for k in range(1, L):  # SVD sweep with truncation
+            m, n = prev * d, b[k]
+            r = min(md, m, n)
+            tot += svd(m, n) + 8 * r * n * m + 8 * r * n * d * b[k + 1]
+            prev = r
+    return tot
+
+
+def run_batched(args):
+    """Config 4: ragged batch of random MPS (L uniform in [16, 128], χ log-uniform in
+    [16, 512], d=2, seed 5; the first --batched-sample of the 512-MPS population), each
+    canonize!(ψ, MixedCanonical(L)) → compress!(ψ; maxdim = χ÷2) → norm(ψ), FP64.  The
+    grouped path (one launch per kernel per sweep step over all instances) against the
+    per-instance device loop on the same data.  Prints one JSON line (a secondary
+    workload)."""
+    import torch
+
+    import tenetgb
+    from tenetgb import workloads as W
+    from tenetgb.group import MPSGroup
+
+    Ls_all, chis_all = W.batched_population()
+    n = args.batched_sample
+    Ls, chis = Ls_all[:n], chis_all[:n]
+    maxdim = [max(1, c // 2) for c in chis]
+    ctx = tenetgb.Context(0)
+    ctx.set_autotune(True)
+    g = MPSGroup.random(Ls, chis, seed=5, ctx=ctx)
+    ctx.sync()
+    init = [g.sites(b) for b in range(n)]
+    flops = batched_flops(Ls, chis, maxdim)
+    sampler = ClockSampler(0)
+    times_g, times_p = [], []
+    with sampler:
+        for rep in range(2):  # warm-up, timed
+            ctx.check(ctx.lib.tn_group_fill_random(g.h, 5))
+            ctx.sync()
+            t0 = time.perf_counter()
+            norms_g = g.canonize_compress_norm(maxdim)
+            times_g.append(time.perf_counter() - t0)
+        for rep in range(2):
+            psis = [tenetgb.MPS([a.copy() for a in init[b]], ctx=ctx) for b in range(n)]
+            ctx.sync()
+            t0 = time.perf_counter()
+            norms_p = []
+            for b, psi in enumerate(psis):
+                psi.canonize_(tenetgb.MixedCanonical(Ls[b]))
+                psi.compress_(maxdim=maxdim[b])
+                norms_p.append(psi.norm())
+            times_p.append(time.perf_counter() - t0)
+            del psis
+    tg, tp = times_g[-1], times_p[-1]
+    norms_p = np.array(norms_p)
+    # CPU oracle on the smallest instances of the sample, ~20 s
+    from oracle import tenet_oracle as O
+
+    order = np.argsort([L * c**3 for L, c in zip(Ls, chis)])
+    done, spent, fl_cpu = 0, 0.0, 0.0
+    for b in order:
+        psi = O.OMPS([a.copy() for a in init[b]])
+        t0 = time.perf_counter()
+        O.canonize(psi, O.MixedCanonical(Ls[b]))
+        O.compress(psi, maxdim=maxdim[b])
+        O.norm(psi)
+        spent += time.perf_counter() - t0
+        done += 1
+        fl_cpu += batched_flops([Ls[b]], [chis[b]], [maxdim[b]])
+        if spent > 20:
+            break
+    print(json.dumps({
+        "metric": "batched_canonize_compress_norm_mps_per_s", "value": n / tg, "unit": "MPS/s",
+        "higher_is_better": True, "dtype": "c128 (FP64)",
+        "data": "synthetic (seeded Gaussian MPS generated on the device, seed 5)",
+        "config": {"workload": "ragged_mps_L16to128_chi16to512_canonize_compress_half_norm",
+                   "population": 512, "sample": n, "Ls": Ls, "chis": chis, "maxdim": "chi // 2"},
+        "grouped": {"s": tg, "mps_per_s": n / tg, "tflops_algorithmic": flops / tg / 1e12},
+        "per_instance_loop": {"s": tp, "mps_per_s": n / tp, "tflops_algorithmic": flops / tp / 1e12},
+        "speedup_grouped_vs_loop": tp / tg,
+        "norm_max_rel_diff_grouped_vs_loop": float(np.max(np.abs(norms_g - norms_p) / norms_p)),
+        "algorithmic_flops": flops, "clocks": sampler.summary(),
+        "cpu_baseline": {"value": fl_cpu / spent / 1e12, "unit": "TFLOP/s (algorithmic)", "cores": os.cpu_count(),
+                         "kind": "port", "sample": f"{done} smallest MPS of the sample through the oracle, "
+                                                   f"{spent:.1f} s"},
+    }))
+
+
 SERVING_RATES = (100, 300, 1000, 3000, 5000)
 
 
@@ -531,7 +719,8 @@ def run_serving(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tebd", choices=["tebd", "lattice", "serving"])
+    ap.add_argument("--workload", default="tebd", choices=["tebd", "lattice", "serving", "kernels", "batched"])
+    ap.add_argument("--batched-sample", type=int, default=32, help="instances of the 512-MPS population (batched)")
     ap.add_argument("--queries", type=int, default=200, help="queries per arrival rate (serving)")
     ap.add_argument("--serve-budget-gb", type=float, default=200.0, help="HBM budget of the server (serving)")
     ap.add_argument("--profile-gate", action="store_true", help="one saturated gate (small ncu case)")
@@ -550,6 +739,10 @@ def main():
         run_lattice(args)
     elif args.workload == "serving":
         run_serving(args)
+    elif args.workload == "kernels":
+        run_kernels(args)
+    elif args.workload == "batched":
+        run_batched(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

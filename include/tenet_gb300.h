@@ -264,6 +264,79 @@ tn_status_t tn_mps_amplitude(const tn_mps* mps, const void* h_vectors, double* h
 /* ⟨ψ|O_i|ψ⟩/⟨ψ|ψ⟩ for every site i, O a host d×d C64; h_out is B×L×(re,im) */
 tn_status_t tn_mps_local_expectations(const tn_mps* mps, const void* h_op, double* h_out);
 
+/* ---------------------------------------------------------------------------------
+ * Query server: a device-resident pool of MPS answering amplitude, local expectation
+ * value and overlap queries with continuous batching (src/Operations/overlap.jl:22-50).
+ * The server owns its context, a worker thread, one high-priority stream for amplitude
+ * and expectation batches, four overlap streams, and a workspace arena of work_bytes
+ * carved per job.  A pool MPS holds its sites A_i and the environment-dressed sites
+ * X_i = Lf_{i-1} A_i R_{i+1} (2× the site bytes); pool and arena together stay under
+ * hbm_budget (0 = unlimited).  Queries wait until a job slot and workspace are free.
+ * All arithmetic is FP64.
+ * --------------------------------------------------------------------------------- */
+typedef struct tn_server tn_server;
+
+#define TN_Q_AMPLITUDE 0   /* ⟨bits|ψ⟩: data = L×d C64 product vectors, site-major, not conjugated */
+#define TN_Q_EXPECTATION 1 /* ⟨ψ|O_site|ψ⟩/⟨ψ|ψ⟩: data = d×d C64 operator (column-major), site 1-based */
+#define TN_Q_OVERLAP 2     /* ⟨ψ_{mps_b}|ψ_{mps}⟩: both MPS of equal L and d */
+
+typedef struct {
+  int32_t kind;
+  int32_t mps;   /* pool id (the ket) */
+  int32_t mps_b; /* overlap: pool id of the bra */
+  int32_t site;  /* expectation value: operator site */
+  const void* data;
+} tn_query;
+
+tn_status_t tn_serve_create(int32_t device, size_t hbm_budget, size_t work_bytes, int32_t max_batch,
+                            tn_server** out);
+/* waits for every submitted query, then frees the pool and the device */
+tn_status_t tn_serve_destroy(tn_server* srv);
+/* host sites (column-major (χl, d, χr) C64) → pool; TN_ENOMEM past the budget */
+tn_status_t tn_serve_add_mps(tn_server* srv, int32_t L, int32_t d, const int64_t* bond_dims /* L-1 */,
+                             const void* const* h_sites, int32_t* id);
+/* seeded Gaussian MPS generated on the device, bonds min(chi, d^min(i, L-i)), entries of
+ * variance 1/(d χ_{i-1}) */
+tn_status_t tn_serve_add_random_mps(tn_server* srv, int32_t L, int32_t d, int64_t chi, uint64_t seed, int32_t* id);
+tn_status_t tn_serve_remove_mps(tn_server* srv, int32_t id);
+tn_status_t tn_serve_mps_info(tn_server* srv, int32_t id, int32_t* L, int32_t* d, int64_t* bond_dims,
+                              double* norm2);
+tn_status_t tn_serve_get_site(tn_server* srv, int32_t id, int32_t site, void* h_data);
+/* thread-safe; returns at once with a ticket */
+tn_status_t tn_serve_submit(tn_server* srv, const tn_query* q, int64_t* ticket);
+/* blocks until the ticket's result is ready (TN_ETIMEOUT after timeout_s); value =
+ * (re, im); latency = submit → result on the host, seconds */
+tn_status_t tn_serve_wait(tn_server* srv, int64_t ticket, double timeout_s, double* h_value, double* latency_s);
+/* completed, short jobs, overlap jobs, largest batch, deferrals for memory, pool bytes,
+ * pending, jobs in flight */
+tn_status_t tn_serve_stats(tn_server* srv, int64_t* h_stats /* 8 */);
+/* message of the last failed tn_serve_* call on this thread */
+const char* tn_serve_last_error(void);
+
+/* ---------------------------------------------------------------------------------
+ * Grouped MPS batches: B independent MPS of different lengths L_b and bond dimensions
+ * (physical dimension d shared), stored on the device and processed in lockstep by
+ * grouped launches (each launch covers every instance with a site at that step, shapes
+ * from a per-step descriptor table).  Sites are column-major (χ_{i-1}, d, χ_i) C64.
+ * --------------------------------------------------------------------------------- */
+typedef struct tn_group tn_group;
+/* bonds: the L_b − 1 inner bond dimensions of every instance, concatenated */
+tn_status_t tn_group_create(tn_ctx* ctx, int32_t B, const int32_t* L, int32_t d, const int64_t* bonds,
+                            tn_group** out);
+tn_status_t tn_group_destroy(tn_group* g);
+/* seeded Gaussian sites generated on the device, entries of variance 1/(d χ_{i-1}) */
+tn_status_t tn_group_fill_random(tn_group* g, uint64_t seed);
+tn_status_t tn_group_set_site(tn_group* g, int32_t b, int32_t site, const void* h_data);
+tn_status_t tn_group_get_site(const tn_group* g, int32_t b, int32_t site, void* h_data);
+tn_status_t tn_group_bond_dims(const tn_group* g, int32_t b, int64_t* h_bonds /* L_b - 1 */);
+/* for every instance b: canonize!(ψ_b, MixedCanonical(L_b)); compress!(ψ_b;
+ * maxdim = maxdim[b]); h_norms[b] = norm(ψ_b) = ‖Λ_{L_b-1}‖ (canonize.jl:121-252,
+ * compress.jl:21-69, norm.jl:31-34).  Afterwards sites 1..L_b-1 are left-isometric and
+ * site L_b holds Λ_{L_b-1} absorbed; Λ_{L_b-1} is returned by tn_group_lambda.  The
+ * initial bonds must satisfy χ_{i-1}·d ≥ χ_i and χ_{i}·d ≥ χ_{i-1} (rand(MPS) clamping). */
+tn_status_t tn_group_canonize_compress_norm(tn_group* g, const int64_t* maxdim, double* h_norms);
+tn_status_t tn_group_lambda(const tn_group* g, int32_t b, double* h_lambda, int64_t* len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -521,6 +521,15 @@ def local_expectations(psi: OMPS, op):
     return out / nrm, nrm
 
 
+def expectation(psi: OMPS, site: int, op):
+    """⟨ψ|O_site|ψ⟩ / ⟨ψ|ψ⟩ computed the reference's way: overlap(ψ, O_site ψ) /
+    overlap(ψ, ψ), two environment sweeps (overlap.jl:36-50); ``site`` is 1-based."""
+    opsi = psi.copy()
+    A = psi.site(site)
+    opsi.set_site(site, np.einsum("ab,lbr->lar", op, A))
+    return overlap(opsi, psi) / overlap(psi, psi)
+
+
 def contract_state(psi: OMPS):
     """Full state vector (small L only): the ``contract(ψ)`` of the reference tests,
     with Λ absorbed when the MPS is bond-canonical."""

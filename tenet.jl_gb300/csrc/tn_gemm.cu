@@ -128,6 +128,12 @@ tn_status_t gemm_cx(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64
   if (k == 0) {
     // C = beta C: run the kernel with an empty reduction
   }
+  // a few rows against wide operands (batched amplitudes, environment rows): row tiles
+  // of 8 / 16 so the DFMA work is not spent on padding
+  if (m <= 8 && n >= 64)
+    return launch<T, 8, 32, 8, 1, 1>(ctx, opa, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch);
+  if (m <= 16 && n >= 64)
+    return launch<T, 16, 32, 8, 2, 1>(ctx, opa, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch);
   int64_t tiles64 = (int64_t)cdiv(m, 64) * cdiv(n, 64) * batch;
   if (tiles64 >= ctx->num_sms)
     return launch<T, 64, 64, 8, 4, 4>(ctx, opa, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,

@@ -211,16 +211,19 @@ tn_status_t svd_tall_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64
                         int64_t sA, cx<T>* U, int64_t sU, double* S, int64_t sS, cx<T>* V,
                         int64_t sV, int64_t batch, int* sweeps_out);
 
-// mixed precision SVD (C64 data): FP32 Jacobi pre-pass + FP64 polish
+// mixed precision SVD (C64 data): FP32 Jacobi pre-pass + FP64 polish.  keep > 0 (V null
+// only): only the `keep` largest triplets are wanted; the rest of U and S is approximate.
 size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch);
 tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int64_t lda,
                            int64_t sA, cxd* U, int64_t sU, double* S, int64_t sS, cxd* V,
-                           int64_t sV, int64_t batch);
+                           int64_t sV, int64_t batch, int64_t keep);
 
-// left vectors + values only (m >= n): U m×n, S n (no V accumulation on large matrices)
+// left vectors + values only (m >= n): U m×n, S n (no V accumulation on large matrices).
+// keep > 0: a truncation to at most `keep` values follows (the mixed path then skips the
+// work that only the discarded tail would need; plain FP64 ignores it).
 size_t svd_left_workspace(tn_precision_t prec, int64_t m, int64_t n, int64_t batch);
 tn_status_t svd_left(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_t n, const cxd* A, int64_t lda, int64_t sA,
-                     cxd* U, int64_t sU, double* S, int64_t sS, int64_t batch);
+                     cxd* U, int64_t sU, double* S, int64_t sS, int64_t batch, int64_t keep = 0);
 
 // full thin SVD for any m, n: U m×k, S k, Vh k×n (reserves its own workspace when
 // ws_managed is false)

@@ -318,8 +318,8 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
   // which are contiguous blocks of chl·dd elements
   TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, dd, dd, kOne, th0, chl, chl * dd, dG, dd, 0, kZero, th, chl,
                                chl * dd, chr * batch));
-  if (left_only)
-    TN_RETURN_IF(svd_left(ctx, prec, m, n, th, m, m * n, U, m * k, S, k, batch));
+  if (left_only)  // at most maxdim values survive the truncation below
+    TN_RETURN_IF(svd_left(ctx, prec, m, n, th, m, m * n, U, m * k, S, k, batch, maxdim > 0 && maxdim < n ? maxdim : 0));
   else
     TN_RETURN_IF(svd_any(ctx, TN_C64, prec, m, n, th, m, m * n, U, m * k, S, k, Vh, k * n, batch));
   int64_t r = 0;

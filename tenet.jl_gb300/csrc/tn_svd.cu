@@ -51,40 +51,51 @@ __device__ __forceinline__ void rr_pair(int N, int r, int k, int& i, int& j) {
   }
 }
 
+// Jacobi rotation of the pair (w_i, w_j) with α = ‖w_i‖², β = ‖w_j‖², γ = w_iᴴw_j:
+// ζ = (β − α)/(2|γ|), t = sign(ζ)/(|ζ| + √(1+ζ²)), c = 1/√(1+t²), s = c·t, e^{iφ} = γ/|γ|.
+// Square roots and divisions are the correctly rounded ones (an approximate reciprocal
+// square root makes every rotation shrink the columns by an ulp, which adds up over
+// thousands of rotations).  The apply test compares squares.  A rotation that rounds to
+// the identity (t = 0 when ζ² overflows) is not applied, so the sweep can end.
 template <typename T>
-struct Rot {
-  T c, s, t, ag;
-  cx<T> e;  // e^{iφ}
-  bool apply;
+struct RotC {
+  T c, tag;     // tag = t·|γ|: the exact change of the two squared column norms
+  cx<T> se;     // s·e^{iφ}
+  float ratio;  // |γ| / √(αβ), for the convergence monitor
+  int apply;
 };
 
 template <typename T>
-__device__ __forceinline__ Rot<T> make_rot(T alpha, T beta, cx<T> g, T tol) {
-  Rot<T> R;
-  T ag = sqrt(abs2(g));
-  R.apply = ag > tol * sqrt(alpha * beta) && ag > T(0);
-  if (!R.apply) {
-    R.c = 1;
-    R.s = 0;
-    R.e = mkcx<T>(1, 0);
+__device__ __forceinline__ RotC<T> make_rot_c(T alpha, T beta, cx<T> g, T tol) {
+  RotC<T> R;
+  const T ag2 = abs2(g);
+  const T ab = alpha * beta;
+  R.apply = ag2 > tol * tol * ab && ag2 > T(0);
+  R.ratio = ab > T(0) ? sqrtf((float)(ag2 / ab)) : 0.f;
+  R.c = T(1);
+  R.tag = T(0);
+  R.se = mkcx<T>(0, 0);
+  if (!R.apply) return R;
+  const T ag = sqrt(ag2);
+  const T zeta = (beta - alpha) / (T(2) * ag);
+  const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+  if (t == T(0)) {
+    R.apply = 0;
     return R;
   }
-  T zeta = (beta - alpha) / (T(2) * ag);
-  T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-  R.c = T(1) / sqrt(T(1) + t * t);
-  R.s = R.c * t;
-  R.t = t;
-  R.ag = ag;
-  R.e = mkcx<T>(g.x / ag, g.y / ag);
+  const T c = T(1) / sqrt(T(1) + t * t);
+  const T s = c * t;
+  R.c = c;
+  R.tag = t * ag;
+  R.se = mkcx<T>(s * (g.x / ag), s * (g.y / ag));
   return R;
 }
 
 template <typename T>
-__device__ __forceinline__ void rot_apply(const Rot<T>& R, cx<T>& wi, cx<T>& wj) {
-  // wi' = c wi − s conj(e) wj ; wj' = s e wi + c wj
-  cx<T> se = mkcx<T>(R.s * R.e.x, R.s * R.e.y);
-  cx<T> a = R.c * wi - conjg(se) * wj;
-  cx<T> b = se * wi + R.c * wj;
+__device__ __forceinline__ void rot_apply_c(T c, cx<T> se, cx<T>& wi, cx<T>& wj) {
+  // wi' = c wi − conj(se) wj ; wj' = se wi + c wj
+  const cx<T> a = c * wi - conjg(se) * wj;
+  const cx<T> b = se * wi + c * wj;
   wi = a;
   wj = b;
 }
@@ -98,12 +109,14 @@ __device__ __forceinline__ void rot_apply(const Rot<T>& R, cx<T>& wi, cx<T>& wj)
 template <typename T, int NT, int R, bool EXACT>
 __global__ void __launch_bounds__(NT)
     k_jacobi_step_reg(int64_t m, int64_t n, int N, int r, cx<T>* W, int64_t sW, cx<T>* V, int64_t sV, T* nrm,
-                      const int* active, int* rotated, T tol) {
+                      const int* active, int* rotated, T tol, const unsigned char* __restrict__ tail) {
   const int64_t b = blockIdx.y;
   if (!active[b]) return;
   int i, j;
   rr_pair(N, r, blockIdx.x, i, j);
   if (j >= n) return;
+  // both columns ranked below the kept set: their mutual orthogonality is never used
+  if (tail && tail[b * n + i] && tail[b * n + j]) return;
   cx<T>* wi = W + b * sW + (int64_t)i * m;
   cx<T>* wj = W + b * sW + (int64_t)j * m;
   constexpr int NW = NT / 32;
@@ -138,37 +151,49 @@ __global__ void __launch_bounds__(NT)
     red[warp][3] = be;
   }
   __syncthreads();
-  g = mkcx<T>(0, 0);
-  al = 0;
-  be = 0;
-#pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    g.x += red[w][0];
-    g.y += red[w][1];
-    al += red[w][2];
-    be += red[w][3];
-  }
-  if (!EXACT) {
-    al = nrm[b * n + i];
-    be = nrm[b * n + j];
-  }
-  Rot<T> Rt = make_rot(al, be, g, tol);
-  if (threadIdx.x == 0 && al > T(0) && be > T(0)) {
-    // largest off-diagonal ratio of the sweep (positive floats order like their bits)
-    const float ratio = (float)(sqrt(abs2(g)) / sqrt(al * be));
-    atomicMax(&rotated[gridDim.y + b], __float_as_int(ratio));
-  }
-  if (!Rt.apply) return;
+  // one thread forms the rotation (FP64 square roots and divisions are scarce on this
+  // part) and hands (c, s·e^{iφ}) to the block through shared memory
+  __shared__ T s_rot[3];
+  __shared__ int s_apply;
   if (threadIdx.x == 0) {
-    atomicAdd(&rotated[b], 1);
-    nrm[b * n + i] = al - Rt.t * Rt.ag;
-    nrm[b * n + j] = be + Rt.t * Rt.ag;
+    g = mkcx<T>(0, 0);
+    al = 0;
+    be = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      g.x += red[w][0];
+      g.y += red[w][1];
+      al += red[w][2];
+      be += red[w][3];
+    }
+    if (!EXACT) {
+      al = nrm[b * n + i];
+      be = nrm[b * n + j];
+    }
+    const RotC<T> Rt = make_rot_c(al, be, g, tol);
+    if (al > T(0) && be > T(0)) {
+      // largest off-diagonal ratio of the sweep (positive floats order like their bits)
+      atomicMax(&rotated[gridDim.y + b], __float_as_int(Rt.ratio));
+    }
+    s_apply = Rt.apply;
+    if (Rt.apply) {
+      atomicAdd(&rotated[b], 1);
+      nrm[b * n + i] = al - Rt.tag;
+      nrm[b * n + j] = be + Rt.tag;
+      s_rot[0] = Rt.c;
+      s_rot[1] = Rt.se.x;
+      s_rot[2] = Rt.se.y;
+    }
   }
+  __syncthreads();
+  if (!s_apply) return;
+  const T c = s_rot[0];
+  const cx<T> se = mkcx<T>(s_rot[1], s_rot[2]);
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     const int64_t t = threadIdx.x + (int64_t)q * NT;
     if (t < m) {
-      rot_apply(Rt, x[q], y[q]);
+      rot_apply_c(c, se, x[q], y[q]);
       wi[t] = x[q];
       wj[t] = y[q];
     }
@@ -177,10 +202,10 @@ __global__ void __launch_bounds__(NT)
     cx<T>* vi = V + b * sV + (int64_t)i * n;
     cx<T>* vj = V + b * sV + (int64_t)j * n;
     for (int64_t t = threadIdx.x; t < n; t += NT) {
-      cx<T> a = vi[t], c = vj[t];
-      rot_apply(Rt, a, c);
+      cx<T> a = vi[t], e = vj[t];
+      rot_apply_c(c, se, a, e);
       vi[t] = a;
-      vj[t] = c;
+      vj[t] = e;
     }
   }
 }
@@ -244,12 +269,12 @@ __global__ void __launch_bounds__(512)
         be = warp_sum(be);
         g.x = warp_sum(g.x);
         g.y = warp_sum(g.y);
-        Rot<T> R = make_rot(al, be, g, tol);
+        const RotC<T> R = make_rot_c(al, be, g, tol);
         if (!R.apply) continue;
         if (lane == 0) s_rot = 1;
         for (int64_t t = lane; t < m; t += 32) {
           cx<T> x = wi[t], y = wj[t];
-          rot_apply(R, x, y);
+          rot_apply_c(R.c, R.se, x, y);
           wi[t] = x;
           wj[t] = y;
         }
@@ -257,7 +282,7 @@ __global__ void __launch_bounds__(512)
         cx<T>* vj = sv + (int64_t)j * n;
         for (int64_t t = lane; t < n; t += 32) {
           cx<T> x = vi[t], y = vj[t];
-          rot_apply(R, x, y);
+          rot_apply_c(R.c, R.se, x, y);
           vi[t] = x;
           vj[t] = y;
         }
@@ -382,20 +407,62 @@ template size_t svd_workspace<double>(int64_t, int64_t, int64_t);
 template size_t svd_workspace<float>(int64_t, int64_t, int64_t);
 
 // one round-robin step of the register kernel, instantiated by row count
+// flags[b][j] = 1 for the columns of matrix b outside its `keep` largest norms (ties
+// kept): one CTA per matrix, bitonic sort of a copy of the norms in shared memory.
+template <typename T>
+__global__ void __launch_bounds__(512) k_tail_flags(int64_t n, const T* __restrict__ nrm, int64_t keep,
+                                                    unsigned char* __restrict__ flags) {
+  extern __shared__ unsigned char smem_raw[];
+  T* v = reinterpret_cast<T*>(smem_raw);
+  const int64_t b = blockIdx.x;
+  int64_t P2 = 1;
+  while (P2 < n) P2 <<= 1;
+  for (int64_t t = threadIdx.x; t < P2; t += blockDim.x) v[t] = t < n ? nrm[b * n + t] : T(-1);
+  __syncthreads();
+  for (int64_t k = 2; k <= P2; k <<= 1)
+    for (int64_t jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int64_t t = threadIdx.x; t < P2; t += blockDim.x) {
+        const int64_t u = t ^ jj;
+        if (u > t) {
+          const bool desc = (t & k) == 0;
+          const T x = v[t], y = v[u];
+          if (desc ? (x < y) : (x > y)) {
+            v[t] = y;
+            v[u] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  const T thr = v[keep - 1];
+  for (int64_t t = threadIdx.x; t < n; t += blockDim.x) flags[b * n + t] = nrm[b * n + t] < thr ? 1 : 0;
+}
+
+template <typename T>
+static tn_status_t update_tail_flags(tn_ctx* ctx, int64_t n, int64_t batch, const T* nrm, int64_t keep,
+                                     unsigned char* flags) {
+  int64_t P2 = 1;
+  while (P2 < n) P2 <<= 1;
+  k_tail_flags<T><<<(unsigned)batch, 512, sizeof(T) * (size_t)P2, ctx->stream>>>(n, nrm, keep, flags);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
 template <typename T>
 static tn_status_t launch_step(tn_ctx* ctx, int64_t m, int64_t n, int N, int r, cx<T>* W, cx<T>* V, T* nrm,
-                               const int* active, int* rotated, T tol, unsigned gy) {
+                               const int* active, int* rotated, T tol, unsigned gy,
+                               const unsigned char* tail) {
   constexpr bool EX = sizeof(T) == 4;
   const dim3 grid(N / 2, gy);
   const int64_t sW = m * n, sV = n * n;
   if (m <= 512)
-    k_jacobi_step_reg<T, 128, 4, EX><<<grid, 128, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol);
+    k_jacobi_step_reg<T, 128, 4, EX><<<grid, 128, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol, tail);
   else if (m <= 1024)
-    k_jacobi_step_reg<T, 256, 4, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol);
+    k_jacobi_step_reg<T, 256, 4, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol, tail);
   else if (m <= 2048)
-    k_jacobi_step_reg<T, 256, 8, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol);
+    k_jacobi_step_reg<T, 256, 8, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol, tail);
   else if (m <= 4096)
-    k_jacobi_step_reg<T, 256, 16, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol);
+    k_jacobi_step_reg<T, 256, 16, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol, tail);
   else
     return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: more than 4096 rows");
   TN_LAUNCHED(ctx);
@@ -409,8 +476,21 @@ static tn_status_t launch_step(tn_ctx* ctx, int64_t m, int64_t n, int N, int r, 
 // buffer addresses, and replayed per sweep; the host reads one flag word per matrix
 // after each sweep to stop converged matrices.
 template <typename T>
+//   tail / keep: truncation-aware mode (keep > 0, n ≤ 4096): only the `keep`
+//     largest columns are wanted.  tail[b][j] flags the columns ranked below them;
+//     rotations between two flagged columns are skipped.  The flags are refreshed from
+//     the running column norms after each sweep that rotated fewer than half of its
+//     pairs (always, when the flags were set by an earlier phase: tail_preset).
+//   min_rot_frac: the sweeps of matrix b also stop once a sweep rotates no more than this
+//     fraction of the pairs (a pre-pass whose residue a later phase removes).
 static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T>* V, int64_t batch, bool v_given,
-                               int* active, int* rotated, T* nrm, int max_sweeps, int* sweeps_out, bool* noconv_out) {
+                               int* active, int* rotated, T* nrm, int max_sweeps, int* sweeps_out, bool* noconv_out,
+                               unsigned char* tail = nullptr, int64_t keep = 0, bool tail_preset = false,
+                               double min_rot_frac = 0.0) {
+  if (!(tail && keep > 0 && keep < n && n <= 4096)) {
+    tail = nullptr;
+    keep = 0;
+  }
   const unsigned gy = (unsigned)batch;
   const T tol = jacobi_tol<T>(m);
   int sweeps = 0;
@@ -442,8 +522,8 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
     const double stop_ratio = sqrt((double)tol * 1e-2);
     // graph for one sweep
     char key[256];
-    snprintf(key, sizeof(key), "jac%zu:%lld:%lld:%lld:%p:%p:%p:%p:%p", sizeof(T), (long long)m, (long long)n,
-             (long long)batch, (void*)W, (void*)V, (void*)nrm, (void*)active, (void*)rotated);
+    snprintf(key, sizeof(key), "jac%zu:%lld:%lld:%lld:%p:%p:%p:%p:%p:%p", sizeof(T), (long long)m, (long long)n,
+             (long long)batch, (void*)W, (void*)V, (void*)nrm, (void*)active, (void*)rotated, (void*)tail);
     cudaGraphExec_t ge = nullptr;
     auto it = ctx->graphs.find(key);
     if (it != ctx->graphs.end()) {
@@ -459,7 +539,8 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       int64_t nb = std::min<int64_t>((n * batch * 32 + 255) / 256, (int64_t)ctx->num_sms * 8);
       k_col_norms<T><<<(unsigned)std::max<int64_t>(nb, 1), 256, 0, ctx->stream>>>(m, n, W, m * n, nrm, batch);
       tn_status_t st = TN_OK;
-      for (int r = 0; r < N - 1 && st == TN_OK; ++r) st = launch_step<T>(ctx, m, n, N, r, W, V, nrm, active, rotated, tol, gy);
+      for (int r = 0; r < N - 1 && st == TN_OK; ++r)
+        st = launch_step<T>(ctx, m, n, N, r, W, V, nrm, active, rotated, tol, gy, tail);
       cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
       if (st != TN_OK) {
         if (g) cudaGraphDestroy(g);
@@ -472,6 +553,9 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       ctx->graphs[key] = ge;
       ctx->launches -= (N - 1);  // counted again per replay below
     }
+    if (tail && !tail_preset) TN_CHECK_CUDA(ctx, cudaMemsetAsync(tail, 0, (size_t)(n * batch), ctx->stream));
+    const int64_t pairs = n * (n - 1) / 2;
+    const int64_t min_rot = (int64_t)(min_rot_frac * (double)pairs);
     int n_active = (int)batch;
     for (sweeps = 0; sweeps < max_sweeps && n_active > 0; ++sweeps) {
       TN_CHECK_CUDA(ctx, cudaGraphLaunch(ge, ctx->stream));
@@ -481,12 +565,16 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
       if (sweeps < (int)(sizeof(ctx->sweep_rotations) / sizeof(int))) ctx->sweep_rotations[sweeps] = h_rot[0];
       n_active = 0;
+      int64_t max_rot = 0;
       for (int64_t b = 0; b < batch; ++b) {
         float ratio;
         memcpy(&ratio, &h_rot[batch + b], sizeof(float));
-        h_act[b] = h_act[b] && h_rot[b] && ratio > stop_ratio;
+        if (h_act[b]) max_rot = std::max<int64_t>(max_rot, h_rot[b]);
+        h_act[b] = h_act[b] && h_rot[b] && ratio > stop_ratio && h_rot[b] > min_rot;
         n_active += h_act[b];
       }
+      if (tail && n_active > 0 && (tail_preset || 2 * max_rot < pairs))
+        TN_RETURN_IF(update_tail_flags<T>(ctx, n, batch, nrm, keep, tail));
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
     }
     noconv = n_active > 0;
@@ -613,12 +701,18 @@ size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
   s += ws_round(sizeof(double) * (size_t)(n * batch)) + ws_round(sizeof(float) * (size_t)(n * batch));
   s += ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // V scratch when V is not wanted
   s += ws_round(sizeof(cxf) * (size_t)(n * n * batch));  // E³ when W32 has no room for it
+  s += ws_round((size_t)(n * batch));                     // tail flags
   return s;
 }
 
 tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int64_t lda, int64_t sA, cxd* U,
-                           int64_t sU, double* S, int64_t sS, cxd* V, int64_t sV, int64_t batch) {
-  // V == nullptr: right vectors not wanted; the FP64 sweeps then skip accumulating them
+                           int64_t sU, double* S, int64_t sS, cxd* V, int64_t sV, int64_t batch, int64_t keep) {
+  // V == nullptr: right vectors not wanted; the FP64 sweeps then skip accumulating them.
+  // keep > 0 (only with V == nullptr): only the `keep` largest singular triplets are
+  // wanted (a truncation to maxdim follows).  Columns ranked below keep + margin by the
+  // running norms are the tail; rotations between two tail columns are skipped in both
+  // phases, so the kept columns are exact to FP64 and the tail entries of U and S are
+  // approximate (never used by the caller).
   if (m < n) return tn_set_error(ctx, TN_EINVAL, "svd_tall_mixed: m < n");
   const bool want_v = V != nullptr;
   if (n == 0 || batch == 0) return TN_OK;
@@ -639,13 +733,25 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   int* rotated = ws_take<int>(ctx, (size_t)(2 * batch + 2));
   double* nrm64 = ws_take<double>(ctx, (size_t)(n * batch));
   float* nrm32 = ws_take<float>(ctx, (size_t)(n * batch));
+  unsigned char* tail = ws_take<unsigned char>(ctx, (size_t)(n * batch));
+  const int64_t keep_m = (!want_v && keep > 0) ? keep + std::max<int64_t>(16, keep / 8) : 0;
   for (int64_t b = 0; b < batch; ++b) {
     int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
     k_d2f<<<(unsigned)blocks, 256, 0, ctx->stream>>>(m * n, A + b * sA, lda, m, W32 + b * m * n);
     TN_LAUNCHED(ctx);
   }
   bool noconv = false;
-  TN_RETURN_IF(jacobi_core<float>(ctx, m, n, W32, V32, batch, false, active, rotated, nrm32, kMaxSweeps, nullptr, &noconv));
+  // FP32 pre-pass, stopped once a sweep rotates ≤ 1 % of the pairs (the FP64 phase removes
+  // the residue)
+  TN_RETURN_IF(jacobi_core<float>(ctx, m, n, W32, V32, batch, false, active, rotated, nrm32, kMaxSweeps, nullptr, &noconv,
+                                  (keep_m > 0 && keep_m < n) ? tail : nullptr, keep_m, false, 0.01));
+  if (keep_m > 0 && keep_m < n) {
+    // rank the columns by their FP32 norms (the pre-pass left them nearly orthogonal)
+    int64_t nb = std::min<int64_t>((n * batch * 32 + 255) / 256, (int64_t)ctx->num_sms * 8);
+    k_col_norms<float><<<(unsigned)std::max<int64_t>(nb, 1), 256, 0, ctx->stream>>>(m, n, W32, m * n, nrm32, batch);
+    TN_LAUNCHED(ctx);
+    TN_RETURN_IF(update_tail_flags<float>(ctx, n, batch, nrm32, keep_m, tail));
+  }
   {
     int64_t cnt = n * n * batch;
     int64_t blocks = std::min<int64_t>((cnt + 255) / 256, 4096);
@@ -687,7 +793,8 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, n, mkcx(1.0, 0.0), A, lda, sA, V64, n, n * n, mkcx(0.0, 0.0), W64,
                                m, m * n, batch));
   TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W64, want_v ? V64 : nullptr, batch, true, active, rotated, nrm64,
-                                    kMaxSweeps, nullptr, &noconv));
+                                    kMaxSweeps, nullptr, &noconv, (keep_m > 0 && keep_m < n) ? tail : nullptr, keep_m,
+                                    true));
   TN_RETURN_IF(jacobi_finalize<double>(ctx, m, n, W64, want_v ? V64 : nullptr, order, U, sU, S, sS, want_v ? V : nullptr,
                                        sV, false, batch));
   if (noconv) return tn_set_error(ctx, TN_ENOCONV, "Jacobi SVD did not converge within %d sweeps", kMaxSweeps);
@@ -704,11 +811,11 @@ size_t svd_left_workspace(tn_precision_t prec, int64_t m, int64_t n, int64_t bat
 }
 
 tn_status_t svd_left(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_t n, const cxd* A, int64_t lda, int64_t sA,
-                     cxd* U, int64_t sU, double* S, int64_t sS, int64_t batch) {
+                     cxd* U, int64_t sU, double* S, int64_t sS, int64_t batch, int64_t keep) {
   if (m < n) return tn_set_error(ctx, TN_EINVAL, "svd_left: m < n");
   if (n == 0 || batch == 0) return TN_OK;
   if (batch > 65535) return tn_set_error(ctx, TN_EUNSUPPORTED, "svd: batch > 65535");
-  if (prec == TN_PREC_MIXED) return svd_tall_mixed(ctx, m, n, A, lda, sA, U, sU, S, sS, nullptr, 0, batch);
+  if (prec == TN_PREC_MIXED) return svd_tall_mixed(ctx, m, n, A, lda, sA, U, sU, S, sS, nullptr, 0, batch, keep);
   cxd* W = ws_take<cxd>(ctx, (size_t)(m * n * batch));
   cxd* V = ws_take<cxd>(ctx, (size_t)(n * n * batch));
   int* order = ws_take<int>(ctx, (size_t)(n * batch));
@@ -754,7 +861,7 @@ static tn_status_t svd_any_t(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_
     if (mixed) {
       // V (n×n) into Vh then conjugate-transpose in place via a temporary
       cx<T>* Vt = ws_take<cx<T>>(ctx, (size_t)(n * n * batch));
-      TN_RETURN_IF(svd_tall_mixed(ctx, m, n, (const cxd*)A, lda, sA, (cxd*)U, sU, S, sS, (cxd*)Vt, n * n, batch));
+      TN_RETURN_IF(svd_tall_mixed(ctx, m, n, (const cxd*)A, lda, sA, (cxd*)U, sU, S, sS, (cxd*)Vt, n * n, batch, 0));
       return transpose_cx<T>(ctx, n, n, Vt, n, n * n, Vh, n, sVh, batch, true);
     }
     return svd_tall_impl<T>(ctx, m, n, A, lda, sA, U, sU, S, sS, Vh, sVh, true, batch, nullptr);
@@ -764,7 +871,7 @@ static tn_status_t svd_any_t(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_
   TN_RETURN_IF(transpose_cx<T>(ctx, m, n, A, lda, sA, B, n, m * n, batch, true));
   cx<T>* Up = ws_take<cx<T>>(ctx, (size_t)(n * m * batch));  // U' (n×m)
   if (mixed) {
-    TN_RETURN_IF(svd_tall_mixed(ctx, n, m, (const cxd*)B, n, m * n, (cxd*)Up, n * m, S, sS, (cxd*)U, sU, batch));
+    TN_RETURN_IF(svd_tall_mixed(ctx, n, m, (const cxd*)B, n, m * n, (cxd*)Up, n * m, S, sS, (cxd*)U, sU, batch, 0));
   } else {
     TN_RETURN_IF(svd_tall_impl<T>(ctx, n, m, B, n, m * n, Up, n * m, S, sS, U, sU, false, batch, nullptr));
   }
@@ -883,16 +990,16 @@ extern "C" tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, c
     for (int r = 0; r < N - 1; ++r) {
       if (m <= 512)
         k_jacobi_step_reg<double, 128, 4, false><<<grid, 128, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
-                                                                        rotated, tol);
+                                                                        rotated, tol, nullptr);
       else if (m <= 1024)
         k_jacobi_step_reg<double, 256, 4, false><<<grid, 256, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
-                                                                        rotated, tol);
+                                                                        rotated, tol, nullptr);
       else if (m <= 2048)
         k_jacobi_step_reg<double, 256, 8, false><<<grid, 256, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
-                                                                        rotated, tol);
+                                                                        rotated, tol, nullptr);
       else
         k_jacobi_step_reg<double, 256, 16, false><<<grid, 256, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
-                                                                         rotated, tol);
+                                                                         rotated, tol, nullptr);
       NA_CHECK(cudaGetLastError());
     }
     int h_rot = 0;  // host stack word: no allocation

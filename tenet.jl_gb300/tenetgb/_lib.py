@@ -33,6 +33,19 @@ class DeviceTimeoutError(TenetGBError):
     pass
 
 
+class tn_query(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int32),
+        ("mps", C.c_int32),
+        ("mps_b", C.c_int32),
+        ("site", C.c_int32),
+        ("data", C.c_void_p),
+    ]
+
+
+TN_Q_AMPLITUDE, TN_Q_EXPECTATION, TN_Q_OVERLAP = 0, 1, 2
+
+
 class tn_tensor(C.Structure):
     _fields_ = [
         ("rank", C.c_int32),
@@ -115,6 +128,27 @@ SIGNATURES = {
     "tn_mps_normalize": (_st, [_vp]),
     "tn_mps_amplitude": (_st, [_vp, _vp, _pdbl]),
     "tn_mps_local_expectations": (_st, [_vp, _vp, _pdbl]),
+    # query server
+    "tn_serve_create": (_st, [_i32, _sz, _sz, _i32, C.POINTER(_vp)]),
+    "tn_serve_destroy": (_st, [_vp]),
+    "tn_serve_add_mps": (_st, [_vp, _i32, _i32, _pi64, C.POINTER(_vp), _pi32]),
+    "tn_serve_add_random_mps": (_st, [_vp, _i32, _i32, _i64, C.c_uint64, _pi32]),
+    "tn_serve_remove_mps": (_st, [_vp, _i32]),
+    "tn_serve_mps_info": (_st, [_vp, _i32, _pi32, _pi32, _pi64, _pdbl]),
+    "tn_serve_get_site": (_st, [_vp, _i32, _i32, _vp]),
+    "tn_serve_submit": (_st, [_vp, _vp, _pi64]),
+    "tn_serve_wait": (_st, [_vp, _i64, _dbl, _pdbl, _pdbl]),
+    "tn_serve_stats": (_st, [_vp, _pi64]),
+    "tn_serve_last_error": (C.c_char_p, []),
+    # grouped (ragged) MPS batches
+    "tn_group_create": (_st, [_vp, _i32, _pi32, _i32, _pi64, C.POINTER(_vp)]),
+    "tn_group_destroy": (_st, [_vp]),
+    "tn_group_fill_random": (_st, [_vp, C.c_uint64]),
+    "tn_group_set_site": (_st, [_vp, _i32, _i32, _vp]),
+    "tn_group_get_site": (_st, [_vp, _i32, _i32, _vp]),
+    "tn_group_bond_dims": (_st, [_vp, _i32, _pi64]),
+    "tn_group_canonize_compress_norm": (_st, [_vp, _pi64, _pdbl]),
+    "tn_group_lambda": (_st, [_vp, _i32, _pdbl, _pi64]),
 }
 
 _lib = None

@@ -108,3 +108,61 @@ def batched_workload(n=512, seed=5, L_range=(16, 128), chi_range=(16, 512)):
 
 def pauli_z():
     return np.array([[1, 0], [0, -1]], dtype=np.complex128)
+
+
+# ----------------------------------------------------------------------------------
+# query serving: device-resident pool + Poisson query trace
+# ----------------------------------------------------------------------------------
+SERVING_CHIS = (32, 64, 128, 256, 512, 1024)
+
+
+def serving_pool(n_pairs=8, seed=6):
+    """Pool of 2·n_pairs random MPS, d=2: L uniform in [8, 256], χ uniform in
+    {32, …, 1024}, bonds clamped.  MPS come in pairs of equal L (χ drawn independently)
+    so that overlap queries always have a partner.  Returns [(L, χ, seed)]."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_pairs):
+        L = int(rng.integers(8, 257))
+        ca, cb = (int(c) for c in rng.choice(SERVING_CHIS, 2))
+        out.append((L, ca, 1000 * seed + 2 * k))
+        out.append((L, cb, 1000 * seed + 2 * k + 1))
+    return out
+
+
+def serving_trace(pool_L, rate, n, seed=7, d=2):
+    """n queries with exponential inter-arrival times at ``rate`` per second: 60 %
+    amplitudes of uniform random bit strings on a uniform random pool MPS, 30 % ⟨O_i⟩
+    with O = (X + X†)/2 (X complex Gaussian 2×2) at a uniform site, 10 % overlaps of the
+    two MPS of a uniform random pair.  ``pool_L``: L of each pool entry (pairs adjacent).
+    Returns [(t_arrival, kind, mps, arg)] with kind in {"amp", "exp", "ovl"}."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    t -= t[0]
+    out = []
+    npool = len(pool_L)
+    for k in range(n):
+        u = rng.random()
+        if u < 0.6:
+            m = int(rng.integers(npool))
+            out.append((float(t[k]), "amp", m, rng.integers(0, d, pool_L[m])))
+        elif u < 0.9:
+            m = int(rng.integers(npool))
+            X = complex_gaussian(rng, (d, d))
+            out.append((float(t[k]), "exp", m, (int(rng.integers(1, pool_L[m] + 1)), (X + X.conj().T) / 2)))
+        else:
+            p = int(rng.integers(npool // 2))
+            out.append((float(t[k]), "ovl", 2 * p, 2 * p + 1))
+    return out
+
+
+# ----------------------------------------------------------------------------------
+# batched (ragged) population
+# ----------------------------------------------------------------------------------
+def batched_population(n=512, seed=5, Lmin=16, Lmax=128, chimin=16, chimax=512):
+    """n independent MPS shapes: L uniform in [Lmin, Lmax], χ = round(exp(U[ln χmin,
+    ln χmax])).  Returns (Ls, chis)."""
+    rng = np.random.default_rng(seed)
+    Ls = [int(x) for x in rng.integers(Lmin, Lmax + 1, n)]
+    chis = [int(round(float(np.exp(u)))) for u in rng.uniform(np.log(chimin), np.log(chimax), n)]
+    return Ls, chis

@@ -218,3 +218,22 @@ def test_tebd_small_unitary_invariants():
             a = start + 2 * j - 1
             v = np.moveaxis(np.tensordot(G, v, axes=([2, 3], [a, a + 1])), [0, 1], [a, a + 1])
     assert np.allclose(O.contract_state(psi), v.reshape(-1), atol=1e-12)
+
+
+def test_expectation_two_overlaps_matches_environment_sweep():
+    """The serving queries' ⟨O_i⟩ (overlap(ψ, O_i ψ)/overlap(ψ, ψ), the reference's
+    form) equals the left/right-environment evaluation for every site."""
+    rng = np.random.default_rng(11)
+    sites = []
+    bonds = [1, 2, 4, 5, 3, 2, 1]
+    for i in range(6):
+        sites.append((rng.standard_normal((bonds[i], 2, bonds[i + 1])) +
+                      1j * rng.standard_normal((bonds[i], 2, bonds[i + 1]))) / np.sqrt(2))
+    psi = O.OMPS(sites)
+    X = rng.standard_normal((2, 2)) + 1j * rng.standard_normal((2, 2))
+    op = (X + X.conj().T) / 2
+    ref, _ = O.local_expectations(psi, op)
+    for i in range(1, 7):
+        e = O.expectation(psi, i, op)
+        assert abs(e - ref[i - 1]) <= 1e-13 * np.linalg.norm(op)
+        assert abs(e.imag) <= 1e-13 * np.linalg.norm(op)  # Hermitian O
