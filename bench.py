@@ -725,7 +725,7 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=200.0, help="HBM budget of the server (serving)")
     ap.add_argument("--profile-gate", action="store_true", help="one saturated gate (small ncu case)")
     ap.add_argument("--precision", default="native", choices=["native", "mixed"])
-    ap.add_argument("--batch", type=int, default=8, help="MPS instances advanced in lockstep")
+    ap.add_argument("--batch", type=int, default=16, help="MPS instances advanced in lockstep")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)

@@ -324,7 +324,8 @@ typedef struct tn_group tn_group;
 tn_status_t tn_group_create(tn_ctx* ctx, int32_t B, const int32_t* L, int32_t d, const int64_t* bonds,
                             tn_group** out);
 tn_status_t tn_group_destroy(tn_group* g);
-/* seeded Gaussian sites generated on the device, entries of variance 1/(d χ_{i-1}) */
+/* seeded Gaussian sites generated on the device, entries of variance 1/(d χ_{i-1}),
+ * with the bond dimensions given at creation (also after a compress) */
 tn_status_t tn_group_fill_random(tn_group* g, uint64_t seed);
 tn_status_t tn_group_set_site(tn_group* g, int32_t b, int32_t site, const void* h_data);
 tn_status_t tn_group_get_site(const tn_group* g, int32_t b, int32_t site, void* h_data);

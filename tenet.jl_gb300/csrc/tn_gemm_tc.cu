@@ -13,11 +13,12 @@
 // built by a prep kernel that also does the hi/lo split, with an epilogue that writes the
 // two row blocks back as interleaved complex.
 //
-// CTA (128 threads) per 128×128 output tile.  Thread 0 issues TMA loads (128-byte
-// swizzle, 4-stage ring with full/empty mbarriers), thread 32 issues tcgen05.mma
-// (M=128, N=128, K=8 per instruction) and commits each stage back to its empty barrier;
-// all four warps then drain TMEM with tcgen05.ld (warp w owns accumulator rows
-// 32w…32w+31).  Every mbarrier wait is bounded: on timeout the kernel records an error
+// CTA (128 threads) per 128×256 output tile, tiles visited in bands of 8 row tiles so
+// the resident CTAs share their operand panels in L2.  Thread 0 issues TMA loads
+// (128-byte swizzle, 4-stage ring of 48 KB stages with full/empty mbarriers), thread 32
+// issues tcgen05.mma (M=128, N=256, K=8 per instruction; accumulator = 256 TMEM
+// columns) and commits each stage back to its empty barrier; all four warps then drain
+// TMEM with tcgen05.ld (warp w owns accumulator rows 32w…32w+31).  Every mbarrier wait is bounded: on timeout the kernel records an error
 // word, skips the remaining work, and still releases its TMEM.
 #include <cuda.h>
 
@@ -27,11 +28,12 @@
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BKB = 128;  // tile: 128×128 outputs, 128 bytes of K
+constexpr int BM = 128, BN = 256, BKB = 128;  // tile: 128×256 outputs, 128 bytes of K
 constexpr int STAGES = 4;
 constexpr int A_BYTES = BM * BKB, B_BYTES = BN * BKB;
 constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024 /*align*/ + 256 /*barriers*/;
 constexpr long long kSpinLimit = 1ll << 28;
+constexpr int kGroupM = 8;
 
 struct Maps {
   CUtensorMap a[2];  // A_hi, A_lo
@@ -111,7 +113,14 @@ __global__ void __launch_bounds__(128, 1)
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  // grouped tile order: consecutive CTAs sweep the N tiles of a band of kGroupM row tiles,
+  // so the CTAs resident at one time share their A and B panels in L2
+  const int tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
+  const int per_group = kGroupM * tiles_n;
+  const int grp = (int)blockIdx.x / per_group, first_m = grp * kGroupM;
+  const int gsize = min(kGroupM, tiles_m - first_m);
+  const int in_grp = (int)blockIdx.x % per_group;
+  const int m0 = (first_m + in_grp % gsize) * BM, n0 = (in_grp / gsize) * BN;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(BN)
                  : "memory");
@@ -277,13 +286,13 @@ EncodeTiledFn encode_fn(tn_ctx* ctx) {
   return fn;
 }
 
-// K-major operand: rows × Kp floats, row pitch Kp·4 bytes; box 32 × 128
-tn_status_t make_map(tn_ctx* ctx, CUtensorMap* map, const float* base, int64_t rows, int64_t Kp) {
+// K-major operand: rows × Kp floats, row pitch Kp·4 bytes; box 32 floats × box_rows
+tn_status_t make_map(tn_ctx* ctx, CUtensorMap* map, const float* base, int64_t rows, int64_t Kp, uint32_t box_rows) {
   EncodeTiledFn fn = encode_fn(ctx);
   if (!fn) return TN_ECUDA;
   cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)(Kp * 4)};
-  cuuint32_t box[2] = {32, 128};
+  cuuint32_t box[2] = {32, box_rows};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -346,17 +355,18 @@ tn_status_t tc_gemm(tn_ctx* ctx, bool complex_in, int passes, char opa, char opb
   }
   Maps maps;
   memset(&maps, 0, sizeof(maps));
-  TN_RETURN_IF(make_map(ctx, &maps.a[0], Ahi, Ma, Kp));
-  TN_RETURN_IF(make_map(ctx, &maps.b[0], Bhi, n, Kp));
+  TN_RETURN_IF(make_map(ctx, &maps.a[0], Ahi, Ma, Kp, BM));
+  TN_RETURN_IF(make_map(ctx, &maps.b[0], Bhi, n, Kp, BN));
   if (split) {
-    TN_RETURN_IF(make_map(ctx, &maps.a[1], Alo, Ma, Kp));
-    TN_RETURN_IF(make_map(ctx, &maps.b[1], Blo, n, Kp));
+    TN_RETURN_IF(make_map(ctx, &maps.a[1], Alo, Ma, Kp, BM));
+    TN_RETURN_IF(make_map(ctx, &maps.b[1], Blo, n, Kp, BN));
   } else {
     maps.a[1] = maps.a[0];
     maps.b[1] = maps.b[0];
   }
-  dim3 grid(cdiv(Ma, BM), cdiv(n, BN));
-  if (grid.y > 65535) return tn_set_error(ctx, TN_EUNSUPPORTED, "tc_gemm: n too large");
+  const int64_t tiles = (int64_t)cdiv(Ma, BM) * cdiv(n, BN);
+  if (tiles > 0x7fffffffll) return tn_set_error(ctx, TN_EUNSUPPORTED, "tc_gemm: too many tiles");
+  const dim3 grid((unsigned)tiles);
   if (complex_in) {
     TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_gemm_tf32<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     k_gemm_tf32<1><<<grid, 128, SMEM_BYTES, ctx->stream>>>(maps, passes, (int)Ma, (int)n, (int)Kp, (float*)C, ldc,

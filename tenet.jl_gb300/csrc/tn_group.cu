@@ -526,7 +526,8 @@ struct tn_group {
   tn_ctx* ctx = nullptr;
   int B = 0, d = 2;
   std::vector<int> L;
-  std::vector<std::vector<int64_t>> bond;  // [b][0..L]
+  std::vector<std::vector<int64_t>> bond;   // [b][0..L] current
+  std::vector<std::vector<int64_t>> bond0;  // [b][0..L] at creation (the site capacities)
   std::vector<std::vector<int64_t>> cap;   // [b][1..L] elements
   std::vector<std::vector<cxd*>> site;     // [b][1..L]
   std::vector<std::vector<double>> lambda;  // Λ_{L−1} after compress
@@ -728,6 +729,7 @@ tn_status_t tn_group_create(tn_ctx* ctx, int32_t B, const int32_t* L, int32_t d,
       g->bond[b][i] = x;
     }
     off += L[b] - 1;
+    g->bond0.push_back(g->bond[b]);
     g->cap[b].assign(L[b] + 1, 0);
     for (int i = 1; i <= L[b]; ++i) {
       g->cap[b][i] = g->bond[b][i - 1] * d * g->bond[b][i];
@@ -766,6 +768,8 @@ tn_status_t tn_group_destroy(tn_group* g) {
 tn_status_t tn_group_fill_random(tn_group* g, uint64_t seed) {
   if (!g) return TN_EINVAL;
   tn_ctx* ctx = g->ctx;
+  g->bond = g->bond0;  // a fresh MPS of the creation shape
+  for (auto& l : g->lambda) l.clear();
   for (int b = 0; b < g->B; ++b)
     for (int i = 1; i <= g->L[b]; ++i) {
       const int64_t e = g->bond[b][i - 1] * g->d * g->bond[b][i];

@@ -61,9 +61,9 @@ def test_group_matches_oracle_per_instance(data):
         got = contract(g.sites(b))
         ref = O.contract_state(psi)
         assert np.linalg.norm(got - ref) <= 1e-11 * np.linalg.norm(ref)
-        # sites 1..L−1 are left isometries after the sweep
+        # sites 1..L−1 are left isometries after the sweep (Σ over (χl, d) of A*A = I)
         for A in g.sites(b)[:-1]:
-            assert O.isisometry(A, 0)
+            assert O.isisometry(A, 2)
 
 
 def test_group_matches_per_instance_device_path(data):
@@ -104,3 +104,20 @@ def test_group_rejects_bad_maxdim(data):
     g = MPSGroup.from_arrays(data[:2])
     with pytest.raises(ValueError):
         g.canonize_compress_norm([0, 3])
+
+
+def test_group_refill_restores_the_creation_shape():
+    from tenetgb import workloads as W
+    from tenetgb.group import MPSGroup
+
+    Ls, chis = [10, 14], [8, 12]
+    g = MPSGroup.random(Ls, chis, seed=4)
+    first = [g.sites(b) for b in range(2)]
+    n1 = g.canonize_compress_norm([2, 3])
+    g.ctx.check(g.lib.tn_group_fill_random(g.h, 4))
+    for b in range(2):
+        assert g.bond_dims(b) == W.clamped_bonds(Ls[b], 2, chis[b])
+        for x, y in zip(g.sites(b), first[b]):
+            np.testing.assert_array_equal(x, y)
+    n2 = g.canonize_compress_norm([2, 3])
+    np.testing.assert_allclose(n1, n2, rtol=1e-14)
