@@ -655,7 +655,8 @@ def run_serving(args):
     from tenetgb import workloads as W
 
     spec = W.serving_pool()
-    srv = serve.Server(hbm_budget=int(args.serve_budget_gb * 1e9), work_bytes=16 << 30, max_batch=64)
+    srv = serve.Server(hbm_budget=int(args.serve_budget_gb * 1e9), work_bytes=16 << 30, max_batch=64,
+                       precision=args.serve_precision)
     t0 = time.perf_counter()
     ids = [srv.add_random_mps(L, chi, seed=s) for (L, chi, s) in spec]
     reg_s = time.perf_counter() - t0
@@ -705,7 +706,9 @@ def run_serving(args):
     best = max(per_rate, key=lambda e: e["qps"])
     print(json.dumps({
         "metric": "serving_queries_per_s", "value": best["qps"], "unit": "queries/s", "higher_is_better": True,
-        "dtype": "c128 (FP64)", "data": "synthetic (seeded Gaussian MPS generated on the device, seed 6)",
+        "dtype": "c128 (FP64)" if args.serve_precision == "native" else
+                 "c128 data; FP32 amplitude/overlap sweeps, FP64 <O_i> and results",
+        "data": "synthetic (seeded Gaussian MPS generated on the device, seed 6)",
         "config": {"workload": "serving_pool16_L8to256_chi32to1024_mix60amp30exp10ovl", "pool": spec,
                    "pool_bytes": pool_bytes, "registration_s": reg_s, "queries_per_rate": args.queries,
                    "max_batch": 64, "work_bytes": 16 << 30},
@@ -723,6 +726,7 @@ def main():
     ap.add_argument("--batched-sample", type=int, default=32, help="instances of the 512-MPS population (batched)")
     ap.add_argument("--queries", type=int, default=200, help="queries per arrival rate (serving)")
     ap.add_argument("--serve-budget-gb", type=float, default=200.0, help="HBM budget of the server (serving)")
+    ap.add_argument("--serve-precision", default="native", choices=["native", "mixed"], help="serving arithmetic")
     ap.add_argument("--profile-gate", action="store_true", help="one saturated gate (small ncu case)")
     ap.add_argument("--precision", default="native", choices=["native", "mixed"])
     ap.add_argument("--batch", type=int, default=16, help="MPS instances advanced in lockstep")

@@ -167,6 +167,9 @@ tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, const void* 
  * number of rotations applied in each sweep of the first matrix (up to n_rot) */
 tn_status_t tn_svd_last_sweeps(tn_ctx* ctx, int32_t* fp32_sweeps, int32_t* fp64_sweeps,
                                int32_t* rotations, int32_t n_rot);
+/* the largest off-diagonal ratio |w_iᴴw_j| / (‖w_i‖‖w_j‖) seen in each sweep of the
+ * first matrix of the last multi-launch Jacobi phase (up to n values) */
+tn_status_t tn_svd_last_ratios(tn_ctx* ctx, float* ratios, int32_t n);
 
 /* truncation rank select: keep min(maxdim, k) values (maxdim <= 0: no cap), then those
  * with |s| > threshold (threshold <= 0: no threshold), at least one.  Mirrors
@@ -263,6 +266,18 @@ tn_status_t tn_mps_normalize(tn_mps* mps);
 tn_status_t tn_mps_amplitude(const tn_mps* mps, const void* h_vectors, double* h_out);
 /* ⟨ψ|O_i|ψ⟩/⟨ψ|ψ⟩ for every site i, O a host d×d C64; h_out is B×L×(re,im) */
 tn_status_t tn_mps_local_expectations(const tn_mps* mps, const void* h_op, double* h_out);
+/* sample(ψ, nshots) (src/Operations/sample.jl:20-72) of one instance: h_uniforms holds
+ * nshots × L uniforms in [0, 1) (row-major; the caller's RNG replaces Julia's), h_out
+ * receives nshots × L outcomes, 1-based like the reference's samples.  Moves the
+ * orthogonality centre of `mps` to site 1 (the state is unchanged). */
+tn_status_t tn_mps_sample(tn_mps* mps, int32_t instance, int64_t nshots, const double* h_uniforms, int32_t* h_out);
+/* evolve!(ψ, MPO) (src/Operations/evolve.jl:19-137).  MPO site i is a host array,
+ * column-major (w_{i-1}, d, d, w_i) = (left bond, output, input, right bond) C64, with
+ * w_0 = w_L = 1; mpo_bonds holds w_1..w_{L-1}.  algorithm 0: direct contraction (every
+ * instance; bonds become χ_i·w_i, form MixedCanonical(all)); 1: zip-up with truncation
+ * (maxdim > 0 and/or threshold > 0; single-instance MPS). */
+tn_status_t tn_mps_evolve_mpo(tn_mps* mps, const void* const* h_mpo_sites, const int64_t* mpo_bonds, int32_t algorithm,
+                              int64_t maxdim, double threshold);
 
 /* ---------------------------------------------------------------------------------
  * Query server: a device-resident pool of MPS answering amplitude, local expectation
@@ -272,7 +287,6 @@ tn_status_t tn_mps_local_expectations(const tn_mps* mps, const void* h_op, doubl
  * carved per job.  A pool MPS holds its sites A_i and the environment-dressed sites
  * X_i = Lf_{i-1} A_i R_{i+1} (2× the site bytes); pool and arena together stay under
  * hbm_budget (0 = unlimited).  Queries wait until a job slot and workspace are free.
- * All arithmetic is FP64.
  * --------------------------------------------------------------------------------- */
 typedef struct tn_server tn_server;
 
@@ -288,8 +302,11 @@ typedef struct {
   const void* data;
 } tn_query;
 
+/* precision: TN_PREC_NATIVE (FP64 throughout) or TN_PREC_MIXED (pool MPS also keep FP32
+ * copies of their sites; amplitude batches and overlap sweeps run as FP32 GEMMs with the
+ * result returned in FP64, relative error ~1e-6; ⟨O_i⟩ stays FP64) */
 tn_status_t tn_serve_create(int32_t device, size_t hbm_budget, size_t work_bytes, int32_t max_batch,
-                            tn_server** out);
+                            tn_precision_t precision, tn_server** out);
 /* waits for every submitted query, then frees the pool and the device */
 tn_status_t tn_serve_destroy(tn_server* srv);
 /* host sites (column-major (χl, d, χr) C64) → pool; TN_ENOMEM past the budget */

@@ -530,6 +530,91 @@ def expectation(psi: OMPS, site: int, op):
     return overlap(opsi, psi) / overlap(psi, psi)
 
 
+def sample(psi: OMPS, uniforms):
+    """sample(ψ, nsamples) (sample.jl:20-72) with explicit uniforms (nsamples × L in
+    [0, 1)) in place of Julia's RNG: canonize a copy to MixedCanonical(1); for each site
+    the marginals p_s = Σ_r |t[s, r]|² of the projected site t = proj · A_i, outcome by
+    inverse CDF of u·Σp, proj ← t[s, :] / √p_s.  Returns 1-based outcomes."""
+    phi = psi.copy()
+    canonize(phi, MixedCanonical(1))
+    u = np.asarray(uniforms, dtype=np.float64)
+    out = np.zeros(u.shape, dtype=np.int64)
+    for q in range(u.shape[0]):
+        proj = np.ones((1,), dtype=np.complex128)
+        for i, A in enumerate(phi.sites):
+            t = np.tensordot(proj, A, axes=(0, 0))  # (d, χr)
+            p = np.sum(np.abs(t) ** 2, axis=1)
+            target = u[q, i] * p.sum()
+            c = np.cumsum(p)
+            ch = int(np.searchsorted(c, target, side="right"))
+            ch = min(ch, len(p) - 1)
+            while ch > 0 and p[ch] == 0.0:
+                ch -= 1
+            out[q, i] = ch + 1
+            proj = t[ch] / np.sqrt(p[ch])
+    return out
+
+
+def evolve_mpo_direct(psi: OMPS, mpo):
+    """evolve!(ψ::MPS, op::MPO) (evolve.jl:131-137): generic_evolve_mps_mpo_direct!
+    (evolve.jl:19-46) — per site c = A·W over the physical index, the MPS and MPO bonds
+    fused on both sides — then canonize!(ψ, MixedCanonical(all sites)).  MPO sites are
+    (w_l, d_out, d_in, w_r)."""
+    if len(mpo) != psi.L:
+        raise ValueError("MPS and MPO must have the same number of sites")
+    sites = []
+    for A, W in zip(psi.sites, mpo):
+        c = np.einsum("lsr,aosb->laorb", A, W)
+        l, a, o, r, b = c.shape
+        sites.append(c.reshape(l * a, o, r * b))
+    psi.sites = sites
+    psi.lam = {}
+    psi.form = MixedCanonical(range(1, psi.L + 1))
+    return psi
+
+
+def _truncate(U, S, V, maxdim, threshold):
+    keep = np.arange(S.size)
+    if maxdim is not None:
+        keep = keep[: min(maxdim, S.size)]
+    if threshold is not None:
+        keep = keep[np.abs(S[keep]) > threshold]
+    return U[:, keep], S[keep], V[keep, :]
+
+
+def evolve_mpo_zipup(psi: OMPS, mpo, maxdim=None, threshold=None):
+    """generic_evolve_mps_mpo_zipup! (evolve.jl:49-129): C₁ = A₁·W₁ split by a thin SVD
+    with the physical index on the U side, truncated (maxdim, then |s| > threshold),
+    R = S·V carried right: R ← (R·A_i)·W_i, split with (left bond, physical) on the U
+    side; the last site takes R·A_L·W_L.  The form is left as the reference leaves it."""
+    if len(mpo) != psi.L:
+        raise ValueError("MPS and MPO must have the same number of sites")
+    if maxdim is None and threshold is None:
+        raise ValueError("Either `maxdim` or `threhold` must be specified")
+    L = psi.L
+    sites = []
+    # site 1: c[o, r, b] (A: 1 × s × r, W: 1 × o × s × b)
+    c = np.einsum("lsr,aosb->orb", psi.sites[0], mpo[0])
+    o, r, b = c.shape
+    U, S, V = svd_thin(c.reshape(o, r * b))
+    U, S, V = _truncate(U, S, V, maxdim, threshold)
+    sites.append(U.reshape(1, o, -1))
+    R = (S[:, None] * V).reshape(-1, r, b)  # (k, χ, w)
+    for i in range(1, L - 1):
+        A, W = psi.sites[i], mpo[i]
+        t = np.einsum("kcw,csr,wosb->korb", R, A, W)
+        k, o, r, b = t.shape
+        U, S, V = svd_thin(t.reshape(k * o, r * b))
+        U, S, V = _truncate(U, S, V, maxdim, threshold)
+        sites.append(U.reshape(k, o, -1))
+        R = (S[:, None] * V).reshape(-1, r, b)
+    t = np.einsum("kcw,csr,wosb->kor", R, psi.sites[L - 1], mpo[L - 1])
+    sites.append(t)
+    psi.sites = sites
+    psi.lam = {}
+    return psi
+
+
 def contract_state(psi: OMPS):
     """Full state vector (small L only): the ``contract(ψ)`` of the reference tests,
     with Λ absorbed when the MPS is bond-canonical."""

@@ -27,7 +27,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
     k_gemm_cx(char opa, char opb, int64_t m, int64_t n, int64_t k, cx<T> alpha,
               const cx<T>* __restrict__ A, int64_t lda, int64_t sA, const cx<T>* __restrict__ B,
               int64_t ldb, int64_t sB, cx<T> beta, cx<T>* __restrict__ C, int64_t ldc, int64_t sC,
-              int64_t batch) {
+              int64_t batch, bool upper) {
   constexpr int NT = (BM / TM) * (BN / TN);
   constexpr int RX = BN / TN;  // threads along n
   constexpr int RY = BM / TM;  // threads along m
@@ -37,6 +37,7 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
   const int tx = tid % RX, ty = tid / RX;
   const int64_t i0 = (int64_t)blockIdx.x * BM;
   const int64_t j0 = (int64_t)blockIdx.y * BN;
+  if (upper && i0 >= j0 + BN) return;  // Hermitian product: tiles below the diagonal are mirrored
   for (int64_t bz = blockIdx.z; bz < batch; bz += gridDim.z) {
     const cx<T>* Ab = A + bz * sA;
     const cx<T>* Bb = B + bz * sB;
@@ -109,13 +110,24 @@ __global__ void __launch_bounds__((BM / TM) * (BN / TN))
 template <typename T, int BM, int BN, int BK, int TM, int TN>
 tn_status_t launch(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64_t k, cx<T> alpha,
                    const cx<T>* A, int64_t lda, int64_t sA, const cx<T>* B, int64_t ldb, int64_t sB,
-                   cx<T> beta, cx<T>* C, int64_t ldc, int64_t sC, int64_t batch) {
+                   cx<T> beta, cx<T>* C, int64_t ldc, int64_t sC, int64_t batch, bool upper = false) {
   dim3 grid(cdiv(m, BM), cdiv(n, BN), (unsigned)(batch < 65535 ? batch : 65535));
   if (grid.x > 0x7fffffffu || grid.y > 65535u) return tn_set_error(ctx, TN_EINVAL, "gemm: grid too large");
   k_gemm_cx<T, BM, BN, BK, TM, TN><<<grid, (BM / TM) * (BN / TN), 0, ctx->stream>>>(
-      opa, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch);
+      opa, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, upper);
   TN_LAUNCHED(ctx);
   return TN_OK;
+}
+
+// C(i, j) = conj(C(j, i)) for i > j (n × n, batched)
+template <typename T>
+__global__ void k_mirror_lower(int64_t n, cx<T>* C, int64_t ldc, int64_t sC, int64_t batch) {
+  const int64_t total = n * n;
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t i = t % n, j = t / n;
+      if (i > j) C[b * sC + i + j * ldc] = conjg(C[b * sC + j + i * ldc]);
+    }
 }
 
 }  // namespace
@@ -141,6 +153,29 @@ tn_status_t gemm_cx(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64
   return launch<T, 32, 32, 8, 2, 2>(ctx, opa, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C,
                                     ldc, sC, batch);
 }
+
+// C = Aᴴ A (k × n input, n × n Hermitian output, batched): the tiles on and above the
+// diagonal by the GEMM kernel, the rest mirrored
+template <typename T>
+tn_status_t herk_cx(tn_ctx* ctx, int64_t n, int64_t k, const cx<T>* A, int64_t lda, int64_t sA, cx<T>* C, int64_t ldc,
+                    int64_t sC, int64_t batch) {
+  if (n == 0 || batch == 0) return TN_OK;
+  const cx<T> one = mkcx<T>(1, 0), zero = mkcx<T>(0, 0);
+  const int64_t tiles64 = (int64_t)cdiv(n, 64) * cdiv(n, 64) * batch;
+  if (tiles64 >= 2 * ctx->num_sms)
+    TN_RETURN_IF((launch<T, 64, 64, 8, 4, 4>(ctx, 'C', 'N', n, n, k, one, A, lda, sA, A, lda, sA, zero, C, ldc, sC,
+                                              batch, true)));
+  else
+    TN_RETURN_IF((launch<T, 32, 32, 8, 2, 2>(ctx, 'C', 'N', n, n, k, one, A, lda, sA, A, lda, sA, zero, C, ldc, sC,
+                                              batch, true)));
+  const int64_t blocks = std::min<int64_t>((n * n + 255) / 256, 2048);
+  k_mirror_lower<T><<<dim3((unsigned)blocks, (unsigned)(batch < 65535 ? batch : 65535)), 256, 0, ctx->stream>>>(
+      n, C, ldc, sC, batch);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+template tn_status_t herk_cx<double>(tn_ctx*, int64_t, int64_t, const cxd*, int64_t, int64_t, cxd*, int64_t, int64_t,
+                                     int64_t);
 
 template tn_status_t gemm_cx<double>(tn_ctx*, char, char, int64_t, int64_t, int64_t, cxd,
                                      const cxd*, int64_t, int64_t, const cxd*, int64_t, int64_t,

@@ -239,6 +239,42 @@ __global__ void k_prep_a_cx(int64_t M, int64_t K, int64_t Kp, const cxf* A, int6
     if (lo) lo[t] = v - h;
   }
 }
+// A' for op(A) = A (M-major source): 32×32 tiles of A staged through shared memory so
+// that both the reads (along i) and the K-major writes (along k) are coalesced; the four
+// quadrants [Ar, −Ai; Ai, Ar] of the tile are written from the staged tile.  Columns
+// kp ≥ 2K of A' (the padding) are written by k_prep_a_pad.
+__global__ void __launch_bounds__(256) k_prep_a_cx_n(int64_t M, int64_t K, int64_t Kp, const cxf* __restrict__ A,
+                                                     int64_t lda, float* __restrict__ hi, float* __restrict__ lo) {
+  __shared__ cxf tile[32][33];
+  const int64_t i0 = (int64_t)blockIdx.x * 32, k0 = (int64_t)blockIdx.y * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 × 8
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t i = i0 + tx, k = k0 + r;
+    tile[r][tx] = (i < M && k < K) ? A[i + k * lda] : mkcx(0.f, 0.f);
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int64_t i = i0 + r, k = k0 + tx;
+    if (i >= M || k >= K) continue;
+    const cxf a = tile[tx][r];
+    const float q[4] = {a.x, -a.y, a.y, a.x};  // (top,left) (top,right) (bottom,left) (bottom,right)
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t ip = i + (u >= 2 ? M : 0), kp = k + ((u & 1) ? K : 0);
+      const float v = q[u], h = tf32_hi(v);
+      hi[ip * Kp + kp] = h;
+      if (lo) lo[ip * Kp + kp] = v - h;
+    }
+  }
+}
+__global__ void k_prep_a_pad(int64_t M2, int64_t K2, int64_t Kp, float* hi, float* lo) {
+  const int64_t w = Kp - K2, total = M2 * w;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ip = t / w, kp = K2 + t % w;
+    hi[ip * Kp + kp] = 0.f;
+    if (lo) lo[ip * Kp + kp] = 0.f;
+  }
+}
 // B' (columns j < N, K-major, pitch Kp): [Br; Bi]
 __global__ void k_prep_b_cx(int64_t N, int64_t K, int64_t Kp, const cxf* B, int64_t ldb, char op, float* hi, float* lo) {
   const int64_t total = N * Kp;
@@ -342,8 +378,17 @@ tn_status_t tc_gemm(tn_ctx* ctx, bool complex_in, int passes, char opa, char opb
   int* err = ws_take<int>(ctx, 4);
   TN_CHECK_CUDA(ctx, cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
   if (complex_in) {
-    k_prep_a_cx<<<blocks_for(ctx, Ma * Kp), 256, 0, ctx->stream>>>(m, k, Kp, (const cxf*)A, lda, opa, Ahi, Alo);
-    TN_LAUNCHED(ctx);
+    if (opa == 'N') {
+      k_prep_a_cx_n<<<dim3(cdiv(m, 32), cdiv(k, 32)), 256, 0, ctx->stream>>>(m, k, Kp, (const cxf*)A, lda, Ahi, Alo);
+      TN_LAUNCHED(ctx);
+      if (Kp > 2 * k) {
+        k_prep_a_pad<<<blocks_for(ctx, Ma * (Kp - 2 * k)), 256, 0, ctx->stream>>>(Ma, 2 * k, Kp, Ahi, Alo);
+        TN_LAUNCHED(ctx);
+      }
+    } else {
+      k_prep_a_cx<<<blocks_for(ctx, Ma * Kp), 256, 0, ctx->stream>>>(m, k, Kp, (const cxf*)A, lda, opa, Ahi, Alo);
+      TN_LAUNCHED(ctx);
+    }
     k_prep_b_cx<<<blocks_for(ctx, n * Kp), 256, 0, ctx->stream>>>(n, k, Kp, (const cxf*)B, ldb, opb, Bhi, Blo);
     TN_LAUNCHED(ctx);
   } else {

@@ -108,6 +108,7 @@ struct tn_ctx {
   // the first matrix of the large-matrix path (-1: shared-memory path)
   int last_sweeps_fp32 = 0, last_sweeps_fp64 = 0;
   int sweep_rotations[64] = {0};
+  float sweep_ratio[64] = {0};  // largest off-diagonal ratio of each sweep (first matrix)
   // autotuned launch parameters, keyed by kernel family + shape bucket
   bool autotune = false;
   std::unordered_map<std::string, std::pair<int, int>> tuning;
@@ -185,6 +186,11 @@ tn_status_t gemm_cx(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64
                     cx<T> alpha, const cx<T>* A, int64_t lda, int64_t sA, const cx<T>* B,
                     int64_t ldb, int64_t sB, cx<T> beta, cx<T>* C, int64_t ldc, int64_t sC,
                     int64_t batch);
+
+// C = Aᴴ A (A k × n, C n × n Hermitian), batched
+template <typename T>
+tn_status_t herk_cx(tn_ctx* ctx, int64_t n, int64_t k, const cx<T>* A, int64_t lda, int64_t sA, cx<T>* C, int64_t ldc,
+                    int64_t sC, int64_t batch);
 
 template <typename T>
 tn_status_t permute_t(tn_ctx* ctx, int rank, const int64_t* dims, const int64_t* in_strides,

@@ -432,6 +432,55 @@ tn_status_t overlap_impl(const tn_mps* a, const tn_mps* b, double* h_out) {
   return TN_OK;
 }
 
+// Sampling step at one site for every shot q (one block per shot): marginals
+// p_s = Σ_r |T[q, s, r]|² of the projected site T = P·A (the sites to the right are right
+// isometries), outcome s by inverse CDF of the caller's uniform u (scaled by Σ_s p_s),
+// new projector row P[q, :] = T[q, s, :] / √p_s (sample.jl:34-70).  d ≤ 32.
+__global__ void __launch_bounds__(128) k_sample_site(int64_t ns, int d, int64_t chr, const cxd* __restrict__ T,
+                                                     const double* __restrict__ u, int64_t L, int site,
+                                                     cxd* __restrict__ P, int32_t* __restrict__ out, int last) {
+  __shared__ double red[4][32];
+  __shared__ double p[32];
+  __shared__ int s_choice;
+  const int64_t q = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int s = 0; s < d; ++s) {
+    double acc = 0;
+    for (int64_t r = threadIdx.x; r < chr; r += blockDim.x) acc += abs2(T[q + ((int64_t)s + (int64_t)d * r) * ns]);
+    acc = warp_sum(acc);
+    if (lane == 0) red[warp][s] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double tot = 0;
+    for (int s = 0; s < d; ++s) {
+      p[s] = red[0][s] + red[1][s] + red[2][s] + red[3][s];
+      tot += p[s];
+    }
+    const double target = u[q * L + site] * tot;
+    double c = 0;
+    int ch = d - 1;
+    for (int s = 0; s < d; ++s) {
+      c += p[s];
+      if (target < c) {
+        ch = s;
+        break;
+      }
+    }
+    while (ch > 0 && p[ch] == 0.0) --ch;  // never pick an outcome of probability zero
+    s_choice = ch;
+    out[q * L + site] = ch + 1;  // 1-based, as the reference's samples
+  }
+  __syncthreads();
+  if (last) return;
+  const int ch = s_choice;
+  const double sc = p[ch] > 0 ? 1.0 / sqrt(p[ch]) : 0.0;
+  for (int64_t r = threadIdx.x; r < chr; r += blockDim.x) {
+    const cxd t = T[q + ((int64_t)ch + (int64_t)d * r) * ns];
+    P[q + r * ns] = mkcx(t.x * sc, t.y * sc);
+  }
+}
+
 tn_status_t check_site_arg(const tn_mps* p, int32_t b, int32_t i) {
   if (b < 0 || b >= p->B) return tn_set_error(p->ctx, TN_EINVAL, "instance %d out of range (B=%d)", b, p->B);
   if (i < 1 || i > p->L) return tn_set_error(p->ctx, TN_EINVAL, "site %d out of range", i);
@@ -845,6 +894,229 @@ tn_status_t tn_mps_local_expectations(const tn_mps* p, const void* h_op, double*
     }
   }
   return TN_OK;
+}
+
+// sample(ψ, nsamples) (src/Operations/sample.jl:20-72) for one instance, with the
+// caller's uniforms (nshots × L, row-major) in place of the reference's RNG: moves the
+// orthogonality centre to site 1 (canonize!(ψ, MixedCanonical(1)), as the reference does
+// on a copy), then sweeps the sites once with all shots batched (one GEMM per site).
+tn_status_t tn_mps_sample(tn_mps* p, int32_t instance, int64_t nshots, const double* h_uniforms, int32_t* h_out) {
+  if (!p || !h_uniforms || !h_out) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_ARG(ctx, instance >= 0 && instance < p->B, "sample: instance out of range");
+  TN_ARG(ctx, nshots >= 1, "sample: nshots must be positive");
+  TN_ARG(ctx, p->d <= 32, "sample: physical dimension above 32");
+  TN_RETURN_IF(tn_mps_canonize_mixed(p, 1, 1));
+  const int L = p->L, d = p->d;
+  int64_t mx = 1;
+  for (int i = 0; i <= L; ++i) mx = std::max(mx, p->bond[i]);
+  const size_t need = ws_round(sizeof(cxd) * (size_t)(nshots * mx)) + ws_round(sizeof(cxd) * (size_t)(nshots * d * mx)) +
+                      ws_round(sizeof(double) * (size_t)(nshots * L)) + ws_round(sizeof(int32_t) * (size_t)(nshots * L));
+  TN_RETURN_IF(ws_reserve(ctx, need));
+  cxd* P = ws_take<cxd>(ctx, (size_t)(nshots * mx));
+  cxd* T = ws_take<cxd>(ctx, (size_t)(nshots * d * mx));
+  double* U = ws_take<double>(ctx, (size_t)(nshots * L));
+  int32_t* O = ws_take<int32_t>(ctx, (size_t)(nshots * L));
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(U, h_uniforms, sizeof(double) * nshots * L, cudaMemcpyHostToDevice, ctx->stream));
+  TN_RETURN_IF(set_one(ctx, P, 1, nshots));
+  for (int i = 1; i <= L; ++i) {
+    const int64_t xl = p->bond[i - 1], xr = p->bond[i];
+    const cxd* A = p->site[i] + (size_t)instance * p->cap[i];
+    // T (nshots × d xr) = P (nshots × xl) · A (xl × d xr)
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', nshots, d * xr, xl, kOne, P, nshots, 0, A, xl, 0, kZero, T, nshots, 0, 1));
+    k_sample_site<<<(unsigned)nshots, 128, 0, ctx->stream>>>(nshots, d, xr, T, U, L, i - 1, P, O, i == L ? 1 : 0);
+    TN_LAUNCHED(ctx);
+  }
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_out, O, sizeof(int32_t) * nshots * L, cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TN_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// MPO × MPS evolution (src/Operations/evolve.jl:19-137).  MPO site i is column-major
+// (w_{i-1}, d_out, d_in, w_i) C64, w_0 = w_L = 1, d_out = d_in = d.
+// ---------------------------------------------------------------------------------
+namespace {
+
+typedef double2 pd2;  // permute_t element for ComplexF64
+
+// direct method (evolve.jl:19-46) for every instance: new site i = A_i · W_i over the
+// physical index with (χ, w) fused on both bonds, χ fastest; then MixedCanonical(all)
+tn_status_t evolve_mpo_direct(tn_mps* p, const std::vector<const cxd*>& hW, const std::vector<int64_t>& w) {
+  tn_ctx* ctx = p->ctx;
+  const int L = p->L, d = p->d, B = p->B;
+  std::vector<cxd*> nsite(L + 1, nullptr);
+  std::vector<size_t> ncap(L + 1, 0);
+  for (int i = 1; i <= L; ++i) {
+    const int64_t l = p->bond[i - 1], r = p->bond[i], a = w[i - 1], b = w[i];
+    const int64_t nel = l * a * d * r * b;
+    const size_t need = ws_round(sizeof(cxd) * (size_t)(a * d * d * b)) * 2 +
+                        ws_round(sizeof(cxd) * (size_t)(l * r * d * B)) + 2 * ws_round(sizeof(cxd) * (size_t)(nel * B));
+    tn_status_t st = ws_reserve(ctx, need);
+    void* np = nullptr;
+    if (st == TN_OK) st = tn_dev_alloc(ctx, sizeof(cxd) * (size_t)nel * B, &np);
+    if (st != TN_OK) {
+      for (int j = 1; j < i; ++j) tn_dev_free(ctx, nsite[j]);
+      return st;
+    }
+    nsite[i] = (cxd*)np;
+    ncap[i] = (size_t)nel;
+    cxd* W0 = ws_take<cxd>(ctx, (size_t)(a * d * d * b));
+    cxd* W1 = ws_take<cxd>(ctx, (size_t)(a * d * d * b));
+    cxd* A1 = ws_take<cxd>(ctx, (size_t)(l * r * d * B));
+    cxd* C1 = ws_take<cxd>(ctx, (size_t)(nel * B));
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(W0, hW[i - 1], sizeof(cxd) * a * d * d * b, cudaMemcpyHostToDevice, ctx->stream));
+    // A' (l, r, s) per instance: dims (l, s, r, B), instance stride = capacity
+    {
+      const int64_t dims[4] = {l, d, r, B};
+      const int64_t str[4] = {1, l, l * d, (int64_t)p->cap[i]};
+      const int32_t perm[4] = {0, 2, 1, 3};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 4, dims, str, perm, (const pd2*)p->site[i], (pd2*)A1, false));
+    }
+    // W' (s, a, o, b) from W (a, o, s, b)
+    {
+      const int64_t dims[4] = {a, d, d, b};
+      const int32_t perm[4] = {2, 0, 1, 3};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 4, dims, nullptr, perm, (const pd2*)W0, (pd2*)W1, false));
+    }
+    // C' ((l r) × (a o b)) = A' ((l r) × s) · W' (s × (a o b)), batched over instances
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', l * r, a * d * b, d, kOne, A1, l * r, l * r * d, W1, d, 0, kZero, C1,
+                                 l * r, nel, B));
+    // new site (l, a, o, r, b) from C' (l, r, a, o, b)
+    {
+      const int64_t dims[6] = {l, r, a, d, b, B};
+      const int32_t perm[6] = {0, 2, 3, 1, 4, 5};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 6, dims, nullptr, perm, (const pd2*)C1, (pd2*)nsite[i], false));
+    }
+    TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // W0 came from pageable host memory
+  }
+  for (int i = 1; i <= L; ++i) {
+    TN_RETURN_IF(tn_dev_free(ctx, p->site[i]));
+    p->site[i] = nsite[i];
+    p->cap[i] = ncap[i];
+  }
+  for (int i = 1; i < L; ++i) {
+    p->bond[i] *= w[i];
+    p->cap_bond[i] = std::max(p->cap_bond[i], p->bond[i]);
+  }
+  p->kind = TN_FORM_MIXED;  // canonize!(ψ, MixedCanonical(sites(ψ))): no arithmetic
+  p->lo = 1;
+  p->hi = L;
+  p->lam_len = 0;
+  return TN_OK;
+}
+
+// zip-up (evolve.jl:49-129), one instance
+tn_status_t evolve_mpo_zipup(tn_mps* p, const std::vector<const cxd*>& hW, const std::vector<int64_t>& w,
+                             int64_t maxdim, double threshold) {
+  tn_ctx* ctx = p->ctx;
+  const int L = p->L, d = p->d;
+  std::vector<int64_t> ob(p->bond);  // bonds before the sweep
+  int64_t mx = 1, wm = 1;
+  for (int i = 0; i <= L; ++i) {
+    mx = std::max(mx, ob[i]);
+    wm = std::max(wm, w[i]);
+  }
+  const int64_t km = std::max<int64_t>(d * mx * wm, 1);  // largest carried bond before truncation
+  const int64_t big = km * d * mx * wm;                   // largest (k o) × (r b) block
+  const int64_t rows = km * d, cols = mx * wm, kk = std::min(rows, cols);
+  const size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(wm * d * d * wm)) + 5 * ws_round(sizeof(cxd) * (size_t)big) +
+                      ws_round(sizeof(cxd) * (size_t)(rows * kk)) + ws_round(sizeof(double) * (size_t)kk) +
+                      ws_round(sizeof(cxd) * (size_t)(kk * cols)) + svd_any_workspace(TN_C64, p->prec, rows, cols, 1);
+  TN_RETURN_IF(ws_reserve(ctx, need));
+  cxd* W0 = ws_take<cxd>(ctx, (size_t)(wm * d * d * wm));
+  cxd* W1 = ws_take<cxd>(ctx, (size_t)(wm * d * d * wm));
+  cxd* R = ws_take<cxd>(ctx, (size_t)big);
+  cxd* X = ws_take<cxd>(ctx, (size_t)big);
+  cxd* Y = ws_take<cxd>(ctx, (size_t)big);
+  cxd* T = ws_take<cxd>(ctx, (size_t)big);
+  cxd* Tm = ws_take<cxd>(ctx, (size_t)big);
+  cxd* U = ws_take<cxd>(ctx, (size_t)(rows * kk));
+  double* S = ws_take<double>(ctx, (size_t)kk);
+  cxd* Vh = ws_take<cxd>(ctx, (size_t)(kk * cols));
+  set_one(ctx, R, 1, 1);  // the carried block before site 1: (k = 1, χ_0 = 1, w_0 = 1)
+  int64_t k = 1;
+  for (int i = 1; i <= L; ++i) {
+    const int64_t c = ob[i - 1], r = ob[i], a = w[i - 1], b = w[i];
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(W0, hW[i - 1], sizeof(cxd) * a * d * d * b, cudaMemcpyHostToDevice, ctx->stream));
+    // R (k, c, a) → (k, a, c);  X ((k a) × (s r)) = R' ((k a) × c) · A (c × (s r))
+    {
+      const int64_t dims[3] = {k, c, a};
+      const int32_t perm[3] = {0, 2, 1};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 3, dims, nullptr, perm, (const pd2*)R, (pd2*)Y, false));
+    }
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k * a, d * r, c, kOne, Y, k * a, 0, p->site[i], c, 0, kZero, X, k * a, 0, 1));
+    // X (k, a, s, r) → (k, r, a, s);  W (a, o, s, b) → (a, s, o, b)
+    {
+      const int64_t dims[4] = {k, a, d, r};
+      const int32_t perm[4] = {0, 3, 1, 2};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 4, dims, nullptr, perm, (const pd2*)X, (pd2*)Y, false));
+      const int64_t wd[4] = {a, d, d, b};
+      const int32_t wp[4] = {0, 2, 1, 3};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 4, wd, nullptr, wp, (const pd2*)W0, (pd2*)W1, false));
+    }
+    // T ((k r) × (o b)) = Y ((k r) × (a s)) · W' ((a s) × (o b))
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k * r, d * b, a * d, kOne, Y, k * r, 0, W1, a * d, 0, kZero, T, k * r, 0, 1));
+    // T (k, r, o, b) → (k, o, r, b): the matrix ((k o) × (r b))
+    {
+      const int64_t dims[4] = {k, r, d, b};
+      const int32_t perm[4] = {0, 2, 1, 3};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 4, dims, nullptr, perm, (const pd2*)T, (pd2*)Tm, false));
+    }
+    const int64_t m = k * d, n = r * b;
+    if (i == L) {  // last site: (k, o, 1)
+      TN_RETURN_IF(ensure_site(p, i, (size_t)(k * d)));
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], Tm, sizeof(cxd) * k * d, cudaMemcpyDeviceToDevice, ctx->stream));
+      p->bond[i - 1] = k;
+      break;
+    }
+    const int64_t kmin = std::min(m, n);
+    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, Tm, m, 0, U, 0, S, 0, Vh, 0, 1));
+    int64_t rk = 0;
+    TN_RETURN_IF(rank_select(ctx, S, kmin, maxdim, threshold, &rk));
+    // site i = U[:, :rk] as (k, o, rk);  R = diag(S[:rk]) Vh[:rk, :] as (rk, r, b)
+    TN_RETURN_IF(ensure_site(p, i, (size_t)(m * rk)));
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], U, sizeof(cxd) * m * rk, cudaMemcpyDeviceToDevice, ctx->stream));
+    TN_RETURN_IF(copy_matrix_cxd(ctx, rk, n, Vh, kmin, R, rk));
+    TN_RETURN_IF(scale_rows_sqrt<double>(ctx, R, rk, n, rk, S));  // √S …
+    TN_RETURN_IF(scale_rows_sqrt<double>(ctx, R, rk, n, rk, S));  // … twice: S
+    p->bond[i - 1] = k;
+    k = rk;
+    TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // W0 came from pageable host memory
+  }
+  for (int i = 1; i < L; ++i) p->cap_bond[i] = std::max(p->cap_bond[i], p->bond[i]);
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  p->lam_len = 0;  // the reference leaves the form as it was set before the sweep
+  return TN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+tn_status_t tn_mps_evolve_mpo(tn_mps* p, const void* const* h_mpo_sites, const int64_t* mpo_bonds, int32_t algorithm,
+                              int64_t maxdim, double threshold) {
+  if (!p || !h_mpo_sites) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  const int L = p->L;
+  std::vector<int64_t> w(L + 1, 1);
+  for (int i = 1; i < L; ++i) {
+    TN_ARG(ctx, mpo_bonds && mpo_bonds[i - 1] >= 1, "evolve: MPO bond dimensions must be positive");
+    w[i] = mpo_bonds[i - 1];
+  }
+  std::vector<const cxd*> hW(L);
+  for (int i = 0; i < L; ++i) {
+    TN_ARG(ctx, h_mpo_sites[i] != nullptr, "evolve: null MPO site");
+    hW[i] = (const cxd*)h_mpo_sites[i];
+  }
+  if (algorithm == 0) return evolve_mpo_direct(p, hW, w);
+  TN_ARG(ctx, algorithm == 1, "evolve: algorithm must be 0 (direct) or 1 (zip-up)");
+  TN_ARG(ctx, maxdim > 0 || threshold > 0, "Either `maxdim` or `threhold` must be specified");
+  TN_ARG(ctx, p->B == 1, "evolve: the zip-up runs on single-instance MPS");
+  if (p->kind == TN_FORM_BOND) TN_RETURN_IF(tn_mps_canonize_mixed(p, p->lo, p->lo));  // absorb Λ
+  return evolve_mpo_zipup(p, hW, w, maxdim, threshold);
 }
 
 }  // extern "C"

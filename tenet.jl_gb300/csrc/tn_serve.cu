@@ -22,8 +22,10 @@
 // waits until running jobs return their blocks.  The arena and the pool together are
 // capped by the HBM budget.  Within a short job, amplitudes of one MPS are computed
 // together: per site one GEMM E (nq × χl) · A (χl × d χr) and a selection of the
-// physical component by each query's product vector.  All arithmetic is FP64; every
-// query's numbers are computed by the same sequence of operations alone or in a batch.
+// physical component by each query's product vector.  Every query's numbers are computed
+// by the same sequence of operations alone or in a batch.  Precision: FP64 throughout, or
+// (mixed servers) amplitude chains and overlap sweeps as FP32 GEMMs over FP32 copies of
+// the sites, the scalar result returned in FP64; ⟨O_i⟩ always FP64.
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -66,21 +68,35 @@ unsigned nblk(int64_t n, int cap = 4096) {
 // ---------------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------------
-__global__ void k_fill_one(cxd* x, int64_t stride, int64_t n) {
+template <typename T>
+__global__ void k_fill_one(cx<T>* x, int64_t stride, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    x[i * stride].x = 1.0;
-    x[i * stride].y = 0.0;
+    x[i * stride].x = T(1);
+    x[i * stride].y = T(0);
   }
+}
+// precision conversions: FP32 copies of the pool sites; FP32 results back to FP64
+__global__ void k_d2f_cx(int64_t n, const cxd* __restrict__ a, cxf* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = mkcx((float)a[i].x, (float)a[i].y);
+}
+__global__ void k_f2d_cx(int64_t n, const cxf* __restrict__ a, cxd* __restrict__ b) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = mkcx((double)a[i].x, (double)a[i].y);
 }
 
 // E'[q, r] = Σ_s v_q[site, s] · P[q, s + d r]   (P: nq × d χr, E': nq × χr, both ld nq)
-__global__ void k_amp_select(int64_t nq, int64_t chr, int d, const cxd* __restrict__ P, const cxd* __restrict__ vec,
-                             int64_t vstride, int64_t voff, cxd* __restrict__ E) {
+template <typename T>
+__global__ void k_amp_select(int64_t nq, int64_t chr, int d, const cx<T>* __restrict__ P, const cxd* __restrict__ vec,
+                             int64_t vstride, int64_t voff, cx<T>* __restrict__ E) {
   const int64_t total = nq * chr;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t q = t % nq, r = t / nq;
-    cxd acc = {0, 0};
-    for (int s = 0; s < d; ++s) cfma(acc, vec[q * vstride + voff + s], P[q + (s + (int64_t)d * r) * nq]);
+    cx<T> acc = mkcx(T(0), T(0));
+    for (int s = 0; s < d; ++s) {
+      const cxd v = vec[q * vstride + voff + s];
+      cfma(acc, mkcx((T)v.x, (T)v.y), P[q + (s + (int64_t)d * r) * nq]);
+    }
     E[q + r * nq] = acc;
   }
 }
@@ -169,6 +185,7 @@ struct PoolMPS {
   std::vector<int64_t> bond;  // 0..L
   std::vector<cxd*> site;     // 1..L
   std::vector<cxd*> dressed;  // 1..L   X_i = Lf_{i-1} A_i R_{i+1}: χ_{i-1} × d × χ_i
+  std::vector<cxf*> site32;   // 1..L   FP32 copies of A_i (mixed-precision servers)
   void* block = nullptr;
   size_t bytes = 0;
   int64_t maxbond = 1;
@@ -259,6 +276,7 @@ struct PinnedSlot {
 
 struct tn_server {
   tn_ctx* ctx = nullptr;
+  tn_precision_t prec = TN_PREC_NATIVE;
   int device = 0;
   cudaStream_t s_main = nullptr, s_reg = nullptr, s_ovl[kOvlStreams] = {};
   int ovl_rr = 0;
@@ -350,16 +368,23 @@ int free_slot(tn_server* S) {
 }
 
 // ⟨b|a⟩ environment sweep on ctx->stream; returns the device location of the scalar
-tn_status_t overlap_sweep(tn_ctx* ctx, const PoolMPS& a, const PoolMPS& b, cxd* F, cxd* F2, cxd* T, cxd** res) {
+// sites in the sweep's precision: the FP64 sites, or their FP32 copies
+inline const cxd* site_of(const PoolMPS& p, int i, cxd*) { return p.site[i]; }
+inline const cxf* site_of(const PoolMPS& p, int i, cxf*) { return p.site32[i]; }
+
+template <typename T>
+tn_status_t overlap_sweep(tn_ctx* ctx, const PoolMPS& a, const PoolMPS& b, cx<T>* F, cx<T>* F2, cx<T>* Tm, cx<T>** res) {
   const int d = a.d;
-  k_fill_one<<<1, 32, 0, ctx->stream>>>(F, 1, 1);
+  const cx<T> one = mkcx(T(1), T(0)), zero = mkcx(T(0), T(0));
+  k_fill_one<T><<<1, 32, 0, ctx->stream>>>(F, 1, 1);
   TN_LAUNCHED(ctx);
   for (int i = 1; i <= a.L; ++i) {
     const int64_t xa = a.bond[i - 1], xa2 = a.bond[i], yb = b.bond[i - 1], yb2 = b.bond[i];
     // T (yb × d xa2) = F (yb × xa) · A (xa × d xa2);  F2 (yb2 × xa2) = B_matᴴ · T
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', yb, d * xa2, xa, kOne, F, yb, 0, a.site[i], xa, 0, kZero, T, yb, 0, 1));
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', yb2, xa2, yb * d, kOne, b.site[i], yb * d, 0, T, yb * d, 0, kZero, F2,
-                                 yb2, 0, 1));
+    TN_RETURN_IF(gemm_cx<T>(ctx, 'N', 'N', yb, d * xa2, xa, one, F, yb, 0, site_of(a, i, (cx<T>*)nullptr), xa, 0, zero,
+                            Tm, yb, 0, 1));
+    TN_RETURN_IF(gemm_cx<T>(ctx, 'C', 'N', yb2, xa2, yb * d, one, site_of(b, i, (cx<T>*)nullptr), yb * d, 0, Tm, yb * d,
+                            0, zero, F2, yb2, 0, 1));
     std::swap(F, F2);
   }
   *res = F;
@@ -425,15 +450,33 @@ tn_status_t launch_short(tn_server* S, Job* job, std::vector<Query>& qs) {
     o += cxb(nq * p.maxbond);
     cxd* P = (cxd*)(dev + o);
     o += cxb(nq * d * p.maxbond);
-    k_fill_one<<<nblk(nq), 256, 0, ctx->stream>>>(E, 1, nq);
-    TN_LAUNCHED(ctx);
-    for (int i = 1; i <= p.L; ++i) {
-      const int64_t xl = p.bond[i - 1], xr = p.bond[i];
-      TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', nq, d * xr, xl, kOne, E, nq, 0, p.site[i], xl, 0, kZero, P, nq, 0, 1));
-      k_amp_select<<<nblk(nq * xr), 256, 0, ctx->stream>>>(nq, xr, (int)d, P, dV[g], p.L * d, (int64_t)(i - 1) * d, E);
+    if (S->prec == TN_PREC_MIXED) {  // FP32 chain over the FP32 site copies (the buffers fit twice)
+      cxf* E32 = (cxf*)E;
+      cxf* P32 = (cxf*)P;
+      const cxf one = mkcx(1.f, 0.f), zero = mkcx(0.f, 0.f);
+      k_fill_one<float><<<nblk(nq), 256, 0, ctx->stream>>>(E32, 1, nq);
       TN_LAUNCHED(ctx);
+      for (int i = 1; i <= p.L; ++i) {
+        const int64_t xl = p.bond[i - 1], xr = p.bond[i];
+        TN_RETURN_IF(gemm_cx<float>(ctx, 'N', 'N', nq, d * xr, xl, one, E32, nq, 0, p.site32[i], xl, 0, zero, P32, nq, 0, 1));
+        k_amp_select<float><<<nblk(nq * xr), 256, 0, ctx->stream>>>(nq, xr, (int)d, P32, dV[g], p.L * d,
+                                                                     (int64_t)(i - 1) * d, E32);
+        TN_LAUNCHED(ctx);
+      }
+      k_f2d_cx<<<nblk(nq), 256, 0, ctx->stream>>>(nq, E32, results + slot);
+      TN_LAUNCHED(ctx);
+    } else {
+      k_fill_one<double><<<nblk(nq), 256, 0, ctx->stream>>>(E, 1, nq);
+      TN_LAUNCHED(ctx);
+      for (int i = 1; i <= p.L; ++i) {
+        const int64_t xl = p.bond[i - 1], xr = p.bond[i];
+        TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', nq, d * xr, xl, kOne, E, nq, 0, p.site[i], xl, 0, kZero, P, nq, 0, 1));
+        k_amp_select<double><<<nblk(nq * xr), 256, 0, ctx->stream>>>(nq, xr, (int)d, P, dV[g], p.L * d,
+                                                                      (int64_t)(i - 1) * d, E);
+        TN_LAUNCHED(ctx);
+      }
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(results + slot, E, sizeof(cxd) * nq, cudaMemcpyDeviceToDevice, ctx->stream));
     }
-    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(results + slot, E, sizeof(cxd) * nq, cudaMemcpyDeviceToDevice, ctx->stream));
     for (int64_t q = 0; q < nq; ++q) order[slot + q] = ks[q];
     slot += (int)nq;
   }
@@ -482,7 +525,15 @@ tn_status_t launch_overlap(tn_server* S, Job* job, const Query& q) {
   cxd* F2 = (cxd*)(dev + cxb(mb * mb));
   cxd* T = (cxd*)(dev + 2 * cxb(mb * mb));
   cxd* res = nullptr;
-  TN_RETURN_IF(overlap_sweep(ctx, a, b, F, F2, T, &res));
+  if (S->prec == TN_PREC_MIXED) {  // FP32 environment sweep over the FP32 site copies
+    cxf* r32 = nullptr;
+    TN_RETURN_IF(overlap_sweep<float>(ctx, a, b, (cxf*)F, (cxf*)F2, (cxf*)T, &r32));
+    res = (cxd*)(r32 == (cxf*)F ? F2 : F);  // the buffer the sweep did not end in
+    k_f2d_cx<<<1, 32, 0, ctx->stream>>>(1, r32, res);
+    TN_LAUNCHED(ctx);
+  } else {
+    TN_RETURN_IF(overlap_sweep<double>(ctx, a, b, F, F2, T, &res));
+  }
   TN_CHECK_CUDA(ctx, cudaMemcpyAsync(S->slots[job->slot].h, res, sizeof(cxd), cudaMemcpyDeviceToHost, ctx->stream));
   job->tickets = {q.ticket};
   job->submit = {q.t_submit};
@@ -687,7 +738,8 @@ tn_status_t pool_alloc(tn_server* S, int L, int d, const int64_t* bonds, PoolMPS
   size_t bytes = 0;
   for (int i = 1; i <= L; ++i) bytes += cxb(p.bond[i - 1] * d * p.bond[i]);
   bytes *= 2;  // A_i and X_i
-  if (S->budget && ctx->in_use + bytes > S->budget)
+  if (S->prec == TN_PREC_MIXED)
+    for (int i = 1; i <= L; ++i) bytes += al(sizeof(cxf) * (size_t)(p.bond[i - 1] * d * p.bond[i]));  if (S->budget && ctx->in_use + bytes > S->budget)
     return serr(TN_ENOMEM, "serve: the MPS needs %zu bytes; %zu of the %zu-byte HBM budget are in use", bytes,
                 ctx->in_use, S->budget);
   tn_status_t st = tn_dev_alloc(ctx, bytes, &p.block);
@@ -703,6 +755,13 @@ tn_status_t pool_alloc(tn_server* S, int L, int d, const int64_t* bonds, PoolMPS
   for (int i = 1; i <= L; ++i) {
     p.dressed[i] = (cxd*)c;
     c += cxb(p.bond[i - 1] * d * p.bond[i]);
+  }
+  if (S->prec == TN_PREC_MIXED) {
+    p.site32.assign(L + 1, nullptr);
+    for (int i = 1; i <= L; ++i) {
+      p.site32[i] = (cxf*)c;
+      c += al(sizeof(cxf) * (size_t)(p.bond[i - 1] * d * p.bond[i]));
+    }
   }
   return TN_OK;
 }
@@ -727,8 +786,8 @@ tn_status_t pool_register(tn_server* S, PoolMPS& p, int32_t* id) {
     cxd* Rb = ws_take<cxd>(ctx, (size_t)(mx * mx));
     std::vector<cxd*> Lf(L + 1);
     for (int i = 0; i <= L; ++i) Lf[i] = ws_take<cxd>(ctx, (size_t)(p.bond[i] * p.bond[i]));
-    k_fill_one<<<1, 32, 0, ctx->stream>>>(Lf[0], 1, 1);
-    k_fill_one<<<1, 32, 0, ctx->stream>>>(Ra, 1, 1);  // R_{L+1}
+    k_fill_one<double><<<1, 32, 0, ctx->stream>>>(Lf[0], 1, 1);
+    k_fill_one<double><<<1, 32, 0, ctx->stream>>>(Ra, 1, 1);  // R_{L+1}
     ctx->launches += 2;
     for (int i = 1; i <= L && st == TN_OK; ++i) {
       const int64_t x = p.bond[i - 1], x2 = p.bond[i];
@@ -754,6 +813,11 @@ tn_status_t pool_register(tn_server* S, PoolMPS& p, int32_t* id) {
       if (st == TN_OK)
         st = gemm_cx<double>(ctx, 'N', 'C', x, x, d * x2, kOne, T, x, 0, p.site[i], x, 0, kZero, Rf, x, 0, 1);
       std::swap(Rn, Rf);
+    }
+    for (int i = 1; i <= L && st == TN_OK && S->prec == TN_PREC_MIXED; ++i) {
+      const int64_t e = p.bond[i - 1] * d * p.bond[i];
+      k_d2f_cx<<<nblk(e), 256, 0, ctx->stream>>>(e, p.site[i], p.site32[i]);
+      ctx->launches++;
     }
   }
   cxd h = {0, 0};
@@ -793,8 +857,10 @@ std::vector<int64_t> clamped_bonds(int L, int d, int64_t chi) {
 extern "C" {
 
 tn_status_t tn_serve_create(int32_t device, size_t hbm_budget, size_t work_bytes, int32_t max_batch,
-                            tn_server** out) {
+                            tn_precision_t precision, tn_server** out) {
   if (!out) return serr(TN_EINVAL, "tn_serve_create: null output");
+  if (precision != TN_PREC_NATIVE && precision != TN_PREC_MIXED)
+    return serr(TN_EINVAL, "tn_serve_create: precision must be native or mixed");
   if (work_bytes < (1 << 20)) return serr(TN_EINVAL, "tn_serve_create: work_bytes must be at least 1 MiB");
   if (hbm_budget && work_bytes >= hbm_budget)
     return serr(TN_EINVAL, "tn_serve_create: work_bytes (%zu) must be below the HBM budget (%zu)", work_bytes,
@@ -807,6 +873,7 @@ tn_status_t tn_serve_create(int32_t device, size_t hbm_budget, size_t work_bytes
   S->device = device;
   S->budget = hbm_budget;
   S->max_batch = max_batch > 0 ? max_batch : 64;
+  S->prec = precision;
   // short jobs (amplitudes, ⟨O_i⟩) get the highest stream priority: their thread blocks
   // are scheduled ahead of the long overlap sweeps as SMs free up
   int prio_low = 0, prio_high = 0;

@@ -517,9 +517,9 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
     TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
     const int N = (int)(n + (n & 1));
     // A sweep whose largest off-diagonal ratio is ρ leaves ~ρ² for the next one
-    // (one-sided Jacobi converges quadratically); when ρ² is far below tol the next
+    // (one-sided Jacobi converges quadratically); when ρ² is below tol/10 the next
     // sweep would rotate nothing and is skipped.
-    const double stop_ratio = sqrt((double)tol * 1e-2);
+    const double stop_ratio = sqrt((double)tol * 1e-1);
     // graph for one sweep
     char key[256];
     snprintf(key, sizeof(key), "jac%zu:%lld:%lld:%lld:%p:%p:%p:%p:%p:%p", sizeof(T), (long long)m, (long long)n,
@@ -563,7 +563,10 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * 2 * batch, cudaMemcpyDeviceToHost,
                                          ctx->stream));
       TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      if (sweeps < (int)(sizeof(ctx->sweep_rotations) / sizeof(int))) ctx->sweep_rotations[sweeps] = h_rot[0];
+      if (sweeps < (int)(sizeof(ctx->sweep_rotations) / sizeof(int))) {
+        ctx->sweep_rotations[sweeps] = h_rot[0];
+        memcpy(&ctx->sweep_ratio[sweeps], &h_rot[batch], sizeof(float));
+      }
       n_active = 0;
       int64_t max_rot = 0;
       for (int64_t b = 0; b < batch; ++b) {
@@ -762,8 +765,7 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   //   V ← V (I − E/2 + 3E²/8 − 5E³/16)   (the (I + E)^{-1/2} series; residual ~ (35/128)E⁴)
   // FP32 rotation accumulation leaves |E| ~ 1e-4, so E² and E³ need only ~1e-4 relative
   // accuracy: both are FP32 GEMMs.
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', n, n, n, mkcx(1.0, 0.0), V64, n, n * n, V64, n, n * n, mkcx(0.0, 0.0), G,
-                               n, n * n, batch));
+  TN_RETURN_IF(herk_cx<double>(ctx, n, n, V64, n, n * n, G, n, n * n, batch));
   {
     const int64_t cnt = n * n * batch;
     const unsigned blocks = (unsigned)std::min<int64_t>((cnt + 255) / 256, 4096);
@@ -1030,6 +1032,12 @@ extern "C" tn_status_t tn_svd_last_sweeps(tn_ctx* ctx, int32_t* fp32_sweeps, int
   if (fp32_sweeps) *fp32_sweeps = ctx->last_sweeps_fp32;
   if (fp64_sweeps) *fp64_sweeps = ctx->last_sweeps_fp64;
   for (int i = 0; rotations && i < n_rot && i < 64; ++i) rotations[i] = ctx->sweep_rotations[i];
+  return TN_OK;
+}
+
+extern "C" tn_status_t tn_svd_last_ratios(tn_ctx* ctx, float* ratios, int32_t n) {
+  if (!ctx || !ratios) return TN_EINVAL;
+  for (int i = 0; i < n && i < 64; ++i) ratios[i] = ctx->sweep_ratio[i];
   return TN_OK;
 }
 

@@ -28,11 +28,18 @@ from .mps import (
     canonize_,
     compress,
     compress_,
+    entropy_vonneumann,
+    entropy_vonneumann_,
     evolve_,
+    evolve_mpo,
+    evolve_mpo_,
     normalize,
     normalize_,
     norm,
     overlap,
+    sample,
+    schmidt_values,
+    schmidt_values_,
     simple_update_,
     truncate,
     truncate_,

@@ -95,6 +95,7 @@ SIGNATURES = {
     "tn_qr_thin": (_st, [_vp, C.c_int, C.c_int, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _i64]),
     "tn_svd_thin": (_st, [_vp, C.c_int, C.c_int, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64]),
     "tn_svd_last_sweeps": (_st, [_vp, _pi32, _pi32, _pi32, _i32]),
+    "tn_svd_last_ratios": (_st, [_vp, C.POINTER(C.c_float), _i32]),
     "tn_svd_thin_noalloc": (_st, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _vp]),
     "tn_truncation_rank": (_st, [_vp, _vp, _i64, _i64, _dbl, _pi64]),
     "tn_hadamard": (_st, [_vp, C.c_int, _i32, _pi64, _i32, _vp, _vp, _vp]),
@@ -128,8 +129,10 @@ SIGNATURES = {
     "tn_mps_normalize": (_st, [_vp]),
     "tn_mps_amplitude": (_st, [_vp, _vp, _pdbl]),
     "tn_mps_local_expectations": (_st, [_vp, _vp, _pdbl]),
+    "tn_mps_sample": (_st, [_vp, _i32, _i64, _pdbl, _pi32]),
+    "tn_mps_evolve_mpo": (_st, [_vp, C.POINTER(_vp), _pi64, _i32, _i64, _dbl]),
     # query server
-    "tn_serve_create": (_st, [_i32, _sz, _sz, _i32, C.POINTER(_vp)]),
+    "tn_serve_create": (_st, [_i32, _sz, _sz, _i32, C.c_int, C.POINTER(_vp)]),
     "tn_serve_destroy": (_st, [_vp]),
     "tn_serve_add_mps": (_st, [_vp, _i32, _i32, _pi64, C.POINTER(_vp), _pi32]),
     "tn_serve_add_random_mps": (_st, [_vp, _i32, _i32, _i64, C.c_uint64, _pi32]),

@@ -384,3 +384,79 @@ def normalize_(psi):
 
 def normalize(psi):
     return psi.copy().normalize_()
+
+
+# ----------------------------------------------------------------------------------
+# sampling and Schmidt values (src/Operations/sample.jl:20-72, entropy.jl:25-67)
+# ----------------------------------------------------------------------------------
+def sample(psi, nsamples=1, seed=None, uniforms=None, instance=0):
+    """sample(ψ, nsamples): ``nsamples`` bit strings as lists of 1-based outcomes, drawn
+    on the device site by site from the marginals of ψ (moved to MixedCanonical(1) on a
+    copy, as the reference does).  ``uniforms`` (nsamples × L in [0, 1)) replaces the
+    reference's RNG; by default they come from numpy's default_rng(seed)."""
+    L = psi.nsites
+    if uniforms is None:
+        uniforms = np.random.default_rng(seed).random((nsamples, L))
+    u = np.ascontiguousarray(uniforms, dtype=np.float64)
+    if u.shape != (nsamples, L):
+        raise ValueError(f"uniforms must have shape ({nsamples}, {L})")
+    out = np.zeros((nsamples, L), np.int32)
+    tmp = psi.copy()
+    tmp._chk(tmp.lib.tn_mps_sample(tmp.h, int(instance), int(nsamples), u.ctypes.data_as(C.POINTER(C.c_double)),
+                                   out.ctypes.data_as(C.POINTER(C.c_int32))))
+    return [list(map(int, row)) for row in out]
+
+
+def schmidt_values_(psi, bond):
+    """schmidt_values!(ψ, bond): canonize!(ψ, BondCanonical(bond)), then Λ."""
+    a, b = (bond, bond + 1) if isinstance(bond, (int, np.integer)) else tuple(sorted(bond))
+    psi.canonize_(BondCanonical(a, b))
+    return psi.lambda_()
+
+
+def schmidt_values(psi, bond):
+    return schmidt_values_(psi.copy(), bond)
+
+
+def entropy_vonneumann_(psi, bond=None):
+    """entropy_vonneumann!(ψ[, bond]) = −Σ x² · 2 log(x) over the Schmidt values, per
+    bond 1..L−1 when no bond is given (entropy.jl:25-35); the MPS should be normalised."""
+    if bond is not None:
+        x = np.asarray(schmidt_values_(psi, bond), dtype=np.float64)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            return float(-np.sum(x**2 * 2 * np.log(x)))
+    return np.array([entropy_vonneumann_(psi, i) for i in range(1, psi.nsites)])
+
+
+def entropy_vonneumann(psi, bond=None):
+    return entropy_vonneumann_(psi.copy(), bond)
+
+
+# ----------------------------------------------------------------------------------
+# MPO × MPS evolution (src/Operations/evolve.jl:19-137)
+# ----------------------------------------------------------------------------------
+def evolve_mpo_(psi, mpo, algorithm="direct", maxdim=None, threshold=None):
+    """evolve!(ψ, op::MPO): ``mpo`` is a list of site arrays (w_l, d_out, d_in, w_r) (2-D
+    or 3-D boundary sites are lifted).  ``algorithm`` "direct" (the reference's
+    evolve!(::MPS, ::MPO): exact, bonds multiply, MixedCanonical(all)) or "zipup"
+    (generic_evolve_mps_mpo_zipup!, truncated to maxdim / threshold)."""
+    L = psi.nsites
+    if len(mpo) != L:
+        raise ValueError("MPS and MPO must have the same number of sites")
+    arrs = []
+    for i, W in enumerate(mpo):
+        W = np.asarray(W, dtype=np.complex128)
+        if W.ndim == 3:
+            W = W[None] if i == 0 else W[..., None]
+        if W.ndim == 2:
+            W = W[None, :, :, None]
+        arrs.append(np.asfortranarray(W))
+    wb = (C.c_int64 * max(1, L - 1))(*[a.shape[3] for a in arrs[:-1]])
+    ptrs = (C.c_void_p * L)(*[a.ctypes.data for a in arrs])
+    alg = {"direct": 0, "zipup": 1}[algorithm]
+    psi._chk(psi.lib.tn_mps_evolve_mpo(psi.h, ptrs, wb, alg, int(maxdim or 0), float(threshold or 0.0)))
+    return psi
+
+
+def evolve_mpo(psi, mpo, **kw):
+    return evolve_mpo_(psi.copy(), mpo, **kw)

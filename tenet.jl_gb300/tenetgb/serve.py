@@ -48,10 +48,13 @@ STAT_KEYS = ("completed", "short_jobs", "overlap_jobs", "max_batch", "deferred",
 
 
 class Server:
-    def __init__(self, device=0, hbm_budget=0, work_bytes=1 << 30, max_batch=64):
+    def __init__(self, device=0, hbm_budget=0, work_bytes=1 << 30, max_batch=64, precision="native"):
+        """precision "native" (FP64) or "mixed" (FP32 amplitude and overlap sweeps)."""
         self.lib = _lib.load()
         h = C.c_void_p()
-        _check(self.lib.tn_serve_create(device, int(hbm_budget), int(work_bytes), int(max_batch), C.byref(h)))
+        prec = {"native": _lib.TN_PREC_NATIVE, "fp64": _lib.TN_PREC_NATIVE, "mixed": _lib.TN_PREC_MIXED}[precision]
+        _check(self.lib.tn_serve_create(device, int(hbm_budget), int(work_bytes), int(max_batch), prec, C.byref(h)))
+        self.precision = precision
         self.h = h
         self._shape = {}
 

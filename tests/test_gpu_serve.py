@@ -216,3 +216,23 @@ def test_remove_while_queries_run():
                 assert who == "gone"
                 failed += 1
         assert ok + failed == len(ts)
+
+
+def test_mixed_precision_server_within_fp32_tolerance(pool):
+    """A mixed server (FP32 amplitude chains and overlap sweeps, FP64 ⟨O_i⟩) agrees with
+    the oracle to 1e-5 of each value's scale (FP32 products over ≤ 13 sites), and its
+    batched results equal its lone results exactly."""
+    from tenetgb import serve
+
+    _, _, omps = pool
+    with serve.Server(work_bytes=256 << 20, precision="mixed") as srv:
+        ids = {k: srv.add_mps(m.sites) for k, m in omps.items()}
+        qs = make_queries(ids, omps, seed=5, n_amp=3, n_exp=2)
+        alone = [srv.wait(submit(srv, ids, q))[0] for q in qs]
+        tickets = [submit(srv, ids, q) for q in qs]
+        mixed = [srv.wait(t)[0] for t in tickets]
+        for q, a, m in zip(qs, alone, mixed):
+            ref = oracle_value(q, omps)
+            tol = 1e-12 if q[0] == "exp" else 1e-5
+            assert abs(a - ref) <= tol * scale(q, omps), (q[0], a, ref)
+            assert a == m
