@@ -384,6 +384,31 @@ def profile_gate(args):
                       "bond": psi.bondsizes()[9], "launches": ctx.launches()}))
 
 
+def profile_svd(args):
+    """The roofline kernel's own workload: tensor_svd_thin of one 512×512 C64 Gaussian
+    matrix in FP64 (U, S and V), run twice; the second call is bracketed by
+    cudaProfilerStart/Stop (small ncu case for the k_jacobi_step_reg traffic)."""
+    import torch
+
+    import tenetgb
+
+    ctx = tenetgb.Context(0)
+    rng = np.random.default_rng(0)
+    A = tenetgb.DeviceTensor.from_numpy(ctx, rng.standard_normal((512, 512)) + 1j * rng.standard_normal((512, 512)),
+                                        ["r", "c"])
+    for rep in range(2):
+        ctx.sync()
+        if rep == 1:
+            torch.cuda.profiler.start()
+        t0 = time.perf_counter()
+        tenetgb.tensor_svd_thin(A, ["r"], ["c"], "s")
+        ctx.sync()
+        dt = time.perf_counter() - t0
+        if rep == 1:
+            torch.cuda.profiler.stop()
+    print(json.dumps({"profile_svd_ms": 1e3 * dt, "m": 512, "n": 512}))
+
+
 def run_lattice(args):
     """Closed 8×8 lattice, bond 8, ComplexF32 (seed 4): contraction to a scalar along the
     planner's path, in 3×TF32 (tensor pipe), TF32, FP32 (CUDA cores) and FP64; errors
@@ -728,6 +753,7 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=200.0, help="HBM budget of the server (serving)")
     ap.add_argument("--serve-precision", default="native", choices=["native", "mixed"], help="serving arithmetic")
     ap.add_argument("--profile-gate", action="store_true", help="one saturated gate (small ncu case)")
+    ap.add_argument("--profile-svd", action="store_true", help="the roofline kernel's SVD (small ncu case)")
     ap.add_argument("--precision", default="native", choices=["native", "mixed"])
     ap.add_argument("--batch", type=int, default=16, help="MPS instances advanced in lockstep")
     ap.add_argument("--gpus", type=int, default=1)
@@ -739,6 +765,8 @@ def main():
         args.warmup = 3
     if args.profile_gate:
         profile_gate(args)
+    elif args.profile_svd:
+        profile_svd(args)
     elif args.workload == "lattice":
         run_lattice(args)
     elif args.workload == "serving":

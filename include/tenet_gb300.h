@@ -278,6 +278,12 @@ tn_status_t tn_mps_sample(tn_mps* mps, int32_t instance, int64_t nshots, const d
  * (maxdim > 0 and/or threshold > 0; single-instance MPS). */
 tn_status_t tn_mps_evolve_mpo(tn_mps* mps, const void* const* h_mpo_sites, const int64_t* mpo_bonds, int32_t algorithm,
                               int64_t maxdim, double threshold);
+/* dump / load of a device MPS (all instances, the form and Λ) as a raw file: magic
+ * "TNMPS001", int32 L, d, B, form, lo, hi, precision, int64 Λ length, int64 bonds[0..L],
+ * column-major ComplexF64 sites per instance, then Λ.  max_bond as tn_mps_create. */
+tn_status_t tn_mps_save(const tn_mps* mps, const char* path);
+tn_status_t tn_mps_shape(const tn_mps* mps, int32_t* L, int32_t* d, int32_t* B);
+tn_status_t tn_mps_load(tn_ctx* ctx, const char* path, int64_t max_bond, tn_mps** out);
 
 /* ---------------------------------------------------------------------------------
  * Query server: a device-resident pool of MPS answering amplitude, local expectation

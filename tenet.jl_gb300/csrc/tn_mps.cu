@@ -1120,3 +1120,122 @@ tn_status_t tn_mps_evolve_mpo(tn_mps* p, const void* const* h_mpo_sites, const i
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------
+// dump / load of a device MPS (warm restart of a pool, hand-over between processes).
+// File: 8-byte magic "TNMPS001", int32 L, d, B, form kind, lo, hi, precision, int64
+// lambda length, int64 bonds[0..L], then for each instance and site the column-major
+// (χ_{i-1}, d, χ_i) ComplexF64 data, then Λ (B × lambda length doubles) if bond-canonical.
+// ---------------------------------------------------------------------------------
+namespace {
+const char kMagic[8] = {'T', 'N', 'M', 'P', 'S', '0', '0', '1'};
+}
+
+extern "C" {
+
+tn_status_t tn_mps_save(const tn_mps* p, const char* path) {
+  if (!p || !path) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  FILE* f = fopen(path, "wb");
+  if (!f) return tn_set_error(ctx, TN_EINVAL, "tn_mps_save: cannot open %s", path);
+  const int32_t hdr[7] = {p->L, p->d, p->B, p->kind, p->lo, p->hi, (int32_t)p->prec};
+  const int64_t lam_len = p->kind == TN_FORM_BOND ? p->lam_len : 0;
+  bool ok = fwrite(kMagic, 1, 8, f) == 8 && fwrite(hdr, sizeof(int32_t), 7, f) == 7 &&
+            fwrite(&lam_len, sizeof(int64_t), 1, f) == 1 &&
+            fwrite(p->bond.data(), sizeof(int64_t), p->L + 1, f) == (size_t)(p->L + 1);
+  std::vector<cxd> buf;
+  for (int b = 0; b < p->B && ok; ++b)
+    for (int i = 1; i <= p->L && ok; ++i) {
+      buf.resize((size_t)sz(p, i));
+      if (cudaMemcpyAsync(buf.data(), p->site[i] + (size_t)b * p->cap[i], sizeof(cxd) * buf.size(),
+                          cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+          cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        fclose(f);
+        return tn_set_error(ctx, TN_ECUDA, "tn_mps_save: device read failed");
+      }
+      ok = fwrite(buf.data(), sizeof(cxd), buf.size(), f) == buf.size();
+    }
+  if (ok && lam_len > 0) {
+    std::vector<double> lam((size_t)(lam_len * p->B));
+    for (int b = 0; b < p->B; ++b)
+      cudaMemcpyAsync(lam.data() + (size_t)b * lam_len, p->lam + (size_t)b * p->lam_cap, sizeof(double) * lam_len,
+                      cudaMemcpyDeviceToHost, ctx->stream);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+      fclose(f);
+      return tn_set_error(ctx, TN_ECUDA, "tn_mps_save: device read failed");
+    }
+    ok = fwrite(lam.data(), sizeof(double), lam.size(), f) == lam.size();
+  }
+  ok = (fclose(f) == 0) && ok;
+  return ok ? TN_OK : tn_set_error(ctx, TN_EINVAL, "tn_mps_save: write to %s failed", path);
+}
+
+tn_status_t tn_mps_shape(const tn_mps* p, int32_t* L, int32_t* d, int32_t* B) {
+  if (!p) return TN_EINVAL;
+  if (L) *L = p->L;
+  if (d) *d = p->d;
+  if (B) *B = p->B;
+  return TN_OK;
+}
+
+tn_status_t tn_mps_load(tn_ctx* ctx, const char* path, int64_t max_bond, tn_mps** out) {
+  if (!ctx || !path || !out) return TN_EINVAL;
+  FILE* f = fopen(path, "rb");
+  if (!f) return tn_set_error(ctx, TN_EINVAL, "tn_mps_load: cannot open %s", path);
+  char magic[8];
+  int32_t hdr[7];
+  int64_t lam_len = 0;
+  bool ok = fread(magic, 1, 8, f) == 8 && memcmp(magic, kMagic, 8) == 0 && fread(hdr, sizeof(int32_t), 7, f) == 7 &&
+            fread(&lam_len, sizeof(int64_t), 1, f) == 1;
+  const int32_t L = hdr[0], d = hdr[1], B = hdr[2];
+  ok = ok && L >= 2 && L <= (1 << 20) && d >= 1 && d <= 1024 && B >= 1 && B <= 8192 && lam_len >= 0;
+  std::vector<int64_t> bond(ok ? L + 1 : 0);
+  ok = ok && fread(bond.data(), sizeof(int64_t), L + 1, f) == (size_t)(L + 1) && bond[0] == 1 && bond[L] == 1;
+  for (int i = 1; ok && i < L; ++i) ok = bond[i] >= 1 && bond[i] <= (int64_t)1 << 24;
+  if (!ok) {
+    fclose(f);
+    return tn_set_error(ctx, TN_EINVAL, "tn_mps_load: %s is not an MPS dump", path);
+  }
+  tn_mps* p = nullptr;
+  tn_status_t st = tn_mps_create_batched(ctx, B, L, d, bond.data() + 1, max_bond, (tn_precision_t)hdr[6], &p);
+  if (st != TN_OK) {
+    fclose(f);
+    return st;
+  }
+  std::vector<cxd> buf;
+  for (int b = 0; b < B && st == TN_OK; ++b)
+    for (int i = 1; i <= L && st == TN_OK; ++i) {
+      buf.resize((size_t)sz(p, i));
+      if (fread(buf.data(), sizeof(cxd), buf.size(), f) != buf.size())
+        st = tn_set_error(ctx, TN_EINVAL, "tn_mps_load: %s is truncated", path);
+      else
+        st = tn_mps_set_instance_site(p, b, i, p->bond[i - 1], p->bond[i], buf.data());
+    }
+  if (st == TN_OK && hdr[3] == TN_FORM_BOND && lam_len > 0) {
+    std::vector<double> lam((size_t)(lam_len * B));
+    if (fread(lam.data(), sizeof(double), lam.size(), f) != lam.size()) {
+      st = tn_set_error(ctx, TN_EINVAL, "tn_mps_load: %s is truncated", path);
+    } else {
+      st = ensure_lam(p, lam_len);
+      for (int b = 0; b < B && st == TN_OK; ++b)
+        if (cudaMemcpyAsync(p->lam + (size_t)b * p->lam_cap, lam.data() + (size_t)b * lam_len, sizeof(double) * lam_len,
+                            cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess)
+          st = tn_set_error(ctx, TN_ECUDA, "tn_mps_load: upload failed");
+      if (st == TN_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        st = tn_set_error(ctx, TN_ECUDA, "tn_mps_load: upload failed");
+      p->lam_len = lam_len;
+    }
+  }
+  fclose(f);
+  if (st != TN_OK) {
+    tn_mps_destroy(p);
+    return st;
+  }
+  p->kind = hdr[3];
+  p->lo = hdr[4];
+  p->hi = hdr[5];
+  *out = p;
+  return TN_OK;
+}
+
+}  // extern "C"

@@ -170,10 +170,18 @@ __global__ void __launch_bounds__(NT)
       al = nrm[b * n + i];
       be = nrm[b * n + j];
     }
-    const RotC<T> Rt = make_rot_c(al, be, g, tol);
+    RotC<T> Rt = make_rot_c(al, be, g, tol);
+    float monitor = Rt.ratio;
+    if (tail && (tail[b * n + i] != tail[b * n + j]) && al > T(0) && be > T(0)) {
+      // a kept column against a tail column: only the kept column is used, and the
+      // rotation changes it by ρ·β_tail/α_kept (relative); below tol the pair is done
+      const T ak = tail[b * n + i] ? be : al, at = tail[b * n + i] ? al : be;
+      monitor = (float)((T)Rt.ratio * (at / ak));
+      if (!(monitor > (float)tol)) Rt.apply = 0;
+    }
     if (al > T(0) && be > T(0)) {
       // largest off-diagonal ratio of the sweep (positive floats order like their bits)
-      atomicMax(&rotated[gridDim.y + b], __float_as_int(Rt.ratio));
+      atomicMax(&rotated[gridDim.y + b], __float_as_int(monitor));
     }
     s_apply = Rt.apply;
     if (Rt.apply) {
@@ -713,9 +721,10 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   // V == nullptr: right vectors not wanted; the FP64 sweeps then skip accumulating them.
   // keep > 0 (only with V == nullptr): only the `keep` largest singular triplets are
   // wanted (a truncation to maxdim follows).  Columns ranked below keep + margin by the
-  // running norms are the tail; rotations between two tail columns are skipped in both
-  // phases, so the kept columns are exact to FP64 and the tail entries of U and S are
-  // approximate (never used by the caller).
+  // running norms are the tail; rotations between two tail columns are skipped, and a
+  // kept–tail pair stops rotating once the rotation would change the kept column by less
+  // than tol relative (ρ·β_tail/α_kept ≤ tol), so the kept columns are exact to FP64 and
+  // the tail entries of U and S are approximate (never used by the caller).
   if (m < n) return tn_set_error(ctx, TN_EINVAL, "svd_tall_mixed: m < n");
   const bool want_v = V != nullptr;
   if (n == 0 || batch == 0) return TN_OK;
@@ -744,10 +753,10 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
     TN_LAUNCHED(ctx);
   }
   bool noconv = false;
-  // FP32 pre-pass, stopped once a sweep rotates ≤ 1 % of the pairs (the FP64 phase removes
+  // FP32 pre-pass, stopped once a sweep rotates ≤ 5 % of the pairs (the FP64 phase removes
   // the residue)
   TN_RETURN_IF(jacobi_core<float>(ctx, m, n, W32, V32, batch, false, active, rotated, nrm32, kMaxSweeps, nullptr, &noconv,
-                                  (keep_m > 0 && keep_m < n) ? tail : nullptr, keep_m, false, 0.01));
+                                  (keep_m > 0 && keep_m < n) ? tail : nullptr, keep_m, false, 0.05));
   if (keep_m > 0 && keep_m < n) {
     // rank the columns by their FP32 norms (the pre-pass left them nearly orthogonal)
     int64_t nb = std::min<int64_t>((n * batch * 32 + 255) / 256, (int64_t)ctx->num_sms * 8);

@@ -216,6 +216,22 @@ class MPS:
         m._L, m._d = self._L, self._d
         return m
 
+    def save(self, path):
+        """Dump all instances, the form and Λ to a raw file (tn_mps_save)."""
+        self._chk(self.lib.tn_mps_save(self.h, str(path).encode()))
+
+    @classmethod
+    def load(cls, path, ctx=None, max_bond=0):
+        """An MPS dumped by ``save`` back on the device (tn_mps_load)."""
+        ctx = ctx or default_context()
+        h = C.c_void_p()
+        ctx.check(ctx.lib.tn_mps_load(ctx.h, str(path).encode(), int(max_bond), C.byref(h)))
+        m = MPS(ctx=ctx, _handle=h)
+        Lc, dc = C.c_int32(), C.c_int32()
+        ctx.check(ctx.lib.tn_mps_shape(h, C.byref(Lc), C.byref(dc), None))
+        m._L, m._d = Lc.value, dc.value
+        return m
+
     def site(self, i, instance=0):
         """Site tensor i (1-based) as a (χl, d, χr) numpy array."""
         b = [1] + self.bondsizes() + [1]
