@@ -296,8 +296,12 @@ def roofline_entry(ctx, stream, dev):
     e1.record(stream)
     e1.synchronize()
     peak = 8 * N**3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+    # DRAM bytes of one launch of this kernel in this configuration, from one ncu capture
+    # (bench.py --profile-svd; cold cache, so W and V are read once: 8.43 MB), per launch
+    traffic = 8.428032e6
     return {"bound": "tensor", "kernel": "k_jacobi_step_reg<double> (FP64 pipe)", "achieved": achieved,
-            "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+            "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/jacobi_fp64_step_svd512_b1.md",
             "peak_source": "FP64 pipe measured in this run (own zgemm 2048^3); MEASURED_PEAKS.json has no FP64 entry",
             "flops_per_launch": flops, "svd_512_ms": svd_ms, "launch_avg_ms": per_launch_ms}
 

@@ -188,6 +188,10 @@ tn_status_t tn_hadamard(tn_ctx* ctx, tn_dtype_t dtype, int32_t rank, const int64
 tn_status_t tn_norm2(tn_ctx* ctx, tn_dtype_t dtype, int64_t n, const void* d_x,
                      double* h_out);
 tn_status_t tn_scale(tn_ctx* ctx, tn_dtype_t dtype, int64_t n, void* d_x, double s);
+/* Krylov-solver vector operations on ComplexF64 device vectors (the DMRG eigensolver):
+ * h_out = ⟨x, y⟩ = Σ conj(x_i) y_i as (re, im); y += (ar + i·ai) x */
+tn_status_t tn_dotc(tn_ctx* ctx, int64_t n, const void* d_x, const void* d_y, double* h_out);
+tn_status_t tn_axpy(tn_ctx* ctx, int64_t n, double ar, double ai, const void* d_x, void* d_y);
 
 /* Muscle.simple_update(A, ia, B, ib, bond, op, oa, ob; maxdim, absorb=AbsorbEqually())
  * (called at src/Operations/simple_update.jl:53-64): A (chl, d1, chm), B (chm, d2, chr),

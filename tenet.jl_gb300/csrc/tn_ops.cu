@@ -354,6 +354,19 @@ tn_status_t zdotc_batched(tn_ctx* ctx, int64_t n, const cxd* x, int64_t sx, cons
   return TN_OK;
 }
 
+namespace {
+// y += a x (complex a)
+__global__ void k_axpy_cx(int64_t n, double ar, double ai, const double2* __restrict__ x, double2* __restrict__ y) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = x[t];
+    double2 w = y[t];
+    w.x = fma(ar, v.x, fma(-ai, v.y, w.x));
+    w.y = fma(ar, v.y, fma(ai, v.x, w.y));
+    y[t] = w;
+  }
+}
+}  // namespace
+
 extern "C" {
 
 tn_status_t tn_truncation_rank(tn_ctx* ctx, const double* S, int64_t k, int64_t maxdim, double threshold,
@@ -418,6 +431,27 @@ tn_status_t tn_scale(tn_ctx* ctx, tn_dtype_t dtype, int64_t n, void* x, double s
     case TN_C32: k_scale<float2><<<nb, 256, 0, ctx->stream>>>(n, (float2*)x, s); break;
     default: return tn_set_error(ctx, TN_EINVAL, "tn_scale: bad dtype");
   }
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+// ⟨x, y⟩ = Σ conj(x_i) y_i for ComplexF64 vectors (h_out = re, im): the Krylov solver's dot
+tn_status_t tn_dotc(tn_ctx* ctx, int64_t n, const void* x, const void* y, double* h_out) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, n >= 0 && h_out && (n == 0 || (x && y)), "tn_dotc: bad arguments");
+  if (n == 0) {
+    h_out[0] = h_out[1] = 0;
+    return TN_OK;
+  }
+  return zdotc_batched(ctx, n, (const cxd*)x, 0, (const cxd*)y, 0, 1, h_out);
+}
+
+// y += a x for ComplexF64 vectors, a = (ar, ai)
+tn_status_t tn_axpy(tn_ctx* ctx, int64_t n, double ar, double ai, const void* x, void* y) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, n >= 0 && (n == 0 || (x && y)), "tn_axpy: bad arguments");
+  if (n == 0) return TN_OK;
+  k_axpy_cx<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, ar, ai, (const double2*)x, (double2*)y);
   TN_LAUNCHED(ctx);
   return TN_OK;
 }

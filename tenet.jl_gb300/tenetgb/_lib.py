@@ -101,6 +101,8 @@ SIGNATURES = {
     "tn_hadamard": (_st, [_vp, C.c_int, _i32, _pi64, _i32, _vp, _vp, _vp]),
     "tn_norm2": (_st, [_vp, C.c_int, _i64, _vp, _pdbl]),
     "tn_scale": (_st, [_vp, C.c_int, _i64, _vp, _dbl]),
+    "tn_dotc": (_st, [_vp, _i64, _vp, _vp, _pdbl]),
+    "tn_axpy": (_st, [_vp, _i64, _dbl, _dbl, _vp, _vp]),
     "tn_simple_update": (
         _st,
         [_vp, C.c_int, C.c_int, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp, _i64, _dbl, _vp, _vp, _vp, _pi64],
