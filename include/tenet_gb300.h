@@ -282,6 +282,18 @@ tn_status_t tn_mps_sample(tn_mps* mps, int32_t instance, int64_t nshots, const d
  * (maxdim > 0 and/or threshold > 0; single-instance MPS). */
 tn_status_t tn_mps_evolve_mpo(tn_mps* mps, const void* const* h_mpo_sites, const int64_t* mpo_bonds, int32_t algorithm,
                               int64_t maxdim, double threshold);
+/* dmrg!(ψ, H; method) (src/Algorithms/DMRG.jl:45-461): ground-state search in place.
+ * method 1 = Dmrg1 (DMRG.jl:45-210, bonds unchanged), 2 = Dmrg2 (DMRG.jl:212-459, pair
+ * split by a thin SVD keeping min(maxdim, k) values; maxdim <= 0 means 128).  The local
+ * eigensolver is KrylovKit's eigsolve(x0, 1, :LM; ishermitian = true, krylovdim, maxiter)
+ * with tolerance tol (<= 0: 1e-12).  MPO sites as for tn_mps_evolve_mpo; mpo_count is 1
+ * (one Hamiltonian for every instance) or B (h_mpo_sites[b*L + i] is site i+1 of
+ * instance b's Hamiltonian; all share mpo_bonds).  h_energy receives B values: the
+ * eigenvalue of the last local problem; h_history (optional) 2·nsweeps·B values: the
+ * same after each half sweep.  Ends in MixedCanonical(site 1). */
+tn_status_t tn_mps_dmrg(tn_mps* mps, const void* const* h_mpo_sites, const int64_t* mpo_bonds, int32_t mpo_count,
+                        int32_t method, int32_t nsweeps, int64_t maxdim, int32_t krylovdim, int32_t maxiter, double tol,
+                        double* h_energy, double* h_history);
 /* dump / load of a device MPS (all instances, the form and Λ) as a raw file: magic
  * "TNMPS001", int32 L, d, B, form, lo, hi, precision, int64 Λ length, int64 bonds[0..L],
  * column-major ComplexF64 sites per instance, then Λ.  max_bond as tn_mps_create. */

@@ -640,3 +640,232 @@ def tebd(psi: OMPS, layers, maxdim, threshold):
             a = start + 2 * j
             simple_update(psi, G, (a, a + 1), maxdim=maxdim, threshold=threshold)
     return psi
+
+
+# ----------------------------------------------------------------------------------
+# DMRG (src/Algorithms/DMRG.jl) with the Ising MPO (src/Models/Ising.jl)
+# ----------------------------------------------------------------------------------
+
+
+def ising_1d_mpo(L, h, J):
+    """ising_1d_mpo(L, h, J) (src/Models/Ising.jl:12-31): H = -J Σ Z_i Z_{i+1} - h Σ X_i
+    as a lower-triangular MPO with bond dimension 3 (start state 3, end state 1).  Sites
+    are returned as (w_l, d_out, d_in, w_r) with the open ends lifted to size 1."""
+    Id = np.eye(2)
+    sx = np.array([[0.0, 1.0], [1.0, 0.0]])
+    sz = np.array([[1.0, 0.0], [0.0, -1.0]])
+    W = np.zeros((3, 2, 2, 3), dtype=np.complex128)  # (l, o, i, r)
+    W[0, :, :, 0] = Id
+    W[1, :, :, 0] = sz
+    W[2, :, :, 0] = -h * sx
+    W[2, :, :, 1] = -J * sz
+    W[2, :, :, 2] = Id
+    first = W[2:3].copy()  # W_1 = W[:, :, 3, :]
+    last = W[:, :, :, 0:1].copy()  # W_n = W[:, :, :, 1]
+    return [first] + [W.copy() for _ in range(L - 2)] + [last]
+
+
+def mpo_dense(mpo):
+    """The MPO as a dense 2^L × 2^L matrix (small L only): H[o…, i…]."""
+    M = mpo[0][0]  # (o, i, r)
+    for W in mpo[1:]:
+        # M[(O), (I), a] · W[a, o, i, b] → M[(O o), (I i), b]
+        t = np.einsum("OIa,aoib->OoIib", M, W)
+        O, o, I, i, b = t.shape
+        M = t.reshape(O * o, I * i, b)
+    return M[:, :, 0]
+
+
+def lanczos_lm(apply, x0, krylovdim=3, maxiter=2, tol=1e-12):
+    """KrylovKit.eigsolve(f, x0, 1, :LM; ishermitian=true, krylovdim, maxiter) (KrylovKit
+    0.9.5–0.10, src/eigsolve/lanczos.jl; a dependency absent from the reference tree)
+    restated in exact-arithmetic terms:
+
+    * the Lanczos factorisation grows from x0/‖x0‖ until it holds ``krylovdim`` vectors or
+      the residual norm β drops to ``tol`` (an invariant subspace);
+    * the tridiagonal Rayleigh quotient is diagonalised and its eigenpairs sorted by
+      descending |θ| (``which = :LM``, a stable sort of the ascending spectrum);
+    * the leading Ritz pair is converged when |β·u_K| ≤ tol; otherwise, unless the
+      iteration count reached ``maxiter``, the factorisation is shrunk to
+      keep = ⌊(3·krylovdim + 2·converged)/5⌋ = 1 vector (the Ritz vector, with the
+      residual as the next basis direction) and grown again.
+
+    Full re-orthogonalisation replaces KrylovKit's local one; in exact arithmetic both
+    give the same factorisation.  Returns (θ, Ritz vector (unit norm), matvecs)."""
+    shape = x0.shape
+    v = x0.reshape(-1) / np.linalg.norm(x0)
+    V = [v]
+    alpha, beta = [], []
+    w = apply(v.reshape(shape)).reshape(-1)
+    nops = 1
+    a = np.vdot(v, w).real
+    r = w - a * v
+    r -= V[0] * np.vdot(V[0], r)
+    alpha.append(a)
+    b = np.linalg.norm(r)
+    it = 1
+    while True:
+        K = len(V)
+        if K == krylovdim or b <= tol:
+            if K == 1:
+                theta, U = np.array([alpha[0]]), np.ones((1, 1))
+                f = np.array([b])
+            else:
+                T = np.diag(alpha) + np.diag(beta, 1) + np.diag(beta, -1)
+                theta, U = np.linalg.eigh(T)  # ascending
+                p = sorted(range(K), key=lambda j: -abs(theta[j]))  # stable
+                theta, U = theta[p], U[:, p]
+                f = U[K - 1, :] * b
+            converged = abs(f[0]) <= tol
+            if converged or (K == krylovdim and it == maxiter) or (b <= tol):
+                x = sum(U[j, 0] * V[j] for j in range(K))
+                return float(theta[0]), x.reshape(shape), nops
+        if K < krylovdim:
+            vn = r / b
+            V.append(vn)
+            beta.append(b)
+            w = apply(vn.reshape(shape)).reshape(-1)
+            nops += 1
+            a = np.vdot(vn, w).real
+            r = w - a * vn - b * V[-2]
+            for _ in range(2):
+                for q in V:
+                    r = r - q * np.vdot(q, r)
+            alpha.append(a)
+            b = np.linalg.norm(r)
+        else:
+            # thick restart with one kept vector: [u₁ | r̂], T = [[θ₁, |f₁|], …]
+            u = sum(U[j, 0] * V[j] for j in range(K))
+            rhat = (np.sign(f[0]) if f[0] != 0 else 1.0) * r / b
+            V = [u, rhat]
+            alpha = [float(theta[0])]
+            beta = [abs(f[0])]
+            w = apply(rhat.reshape(shape)).reshape(-1)
+            nops += 1
+            a = np.vdot(rhat, w).real
+            r = w - a * rhat - beta[0] * u
+            for _ in range(2):
+                for q in V:
+                    r = r - q * np.vdot(q, r)
+            alpha.append(a)
+            b = np.linalg.norm(r)
+            it += 1
+
+
+def _env_left(Lenv, A, W):
+    """Left environment update: L'[b, v, b'] = Σ L[a, w, a'] A[a, s, b] W[w, o, s, v]
+    conj(A[a', o, b']) — the binary_einsum chain of DMRG.jl:106-115."""
+    t = np.tensordot(Lenv, A, axes=(0, 0))  # [w, a', s, b]
+    t = np.tensordot(t, W, axes=([0, 2], [0, 2]))  # [a', b, o, v]
+    return np.tensordot(t, A.conj(), axes=([0, 2], [0, 1]))  # [b, v, b']
+
+
+def _env_right(Renv, A, W):
+    """Right environment update: R'[a, w, a'] = Σ A[a, s, b] W[w, o, s, v] conj(A[a', o, b'])
+    R[b, v, b'] (DMRG.jl:69-79)."""
+    t = np.tensordot(A, Renv, axes=(2, 0))  # [a, s, v, b']
+    t = np.tensordot(t, W, axes=([1, 2], [2, 3]))  # [a, b', w, o]
+    return np.tensordot(t, A.conj(), axes=([3, 1], [1, 2]))  # [a, w, a']
+
+
+def _heff1(Lenv, W, Renv):
+    def apply(x):
+        t = np.tensordot(Lenv, x, axes=(0, 0))  # [w, a', s, b]
+        t = np.tensordot(t, W, axes=([0, 2], [0, 2]))  # [a', b, o, v]
+        return np.tensordot(t, Renv, axes=([1, 3], [0, 1]))  # [a', o, b']
+    return apply
+
+
+def _heff2(Lenv, W1, W2, Renv):
+    def apply(x):
+        t = np.tensordot(Lenv, x, axes=(0, 0))  # [w, a', s1, s2, c]
+        t = np.tensordot(t, W1, axes=([0, 2], [0, 2]))  # [a', s2, c, o1, v]
+        t = np.tensordot(t, W2, axes=([4, 1], [0, 2]))  # [a', c, o1, o2, u]
+        t = np.tensordot(t, Renv, axes=([1, 4], [0, 1]))  # [a', o1, o2, c']
+        return t
+    return apply
+
+
+def dmrg(psi: OMPS, mpo, nsweeps=4, method="dmrg1", maxdim=128, krylovdim=3, maxiter=2, tol=1e-12,
+         history=None):
+    """dmrg!(ψ, H; method) (src/Algorithms/DMRG.jl:45-461) on a copy of ψ.
+
+    Dmrg1 (DMRG.jl:45-210): right environments from canonize!(ψ, i), i = n-1…1; each sweep
+    optimises sites 2…n left→right then n-1…1 right→left, moving the centre with a QR
+    gauge move before the environment update and replacing the site by the Ritz vector.
+    Dmrg2 (DMRG.jl:212-459): the pair (i-1, i) [left→right, centre i] or (i, i+1)
+    [right→left, centre i] is optimised as one tensor θ, split by a thin SVD, the leading
+    min(maxdim, k) values kept and normalised, and S absorbed towards the sweep direction.
+    Returns (ψ, energy of the last eigensolve).  ``history`` (a list) receives the energy
+    after each half sweep."""
+    psi = psi.copy()
+    n = psi.L
+    one = np.ones((1, 1, 1), dtype=np.complex128)
+    envL = {0: one}
+    envR = {n: one}
+    for i in range(n - 1, 0, -1):
+        canonize(psi, MixedCanonical(i))
+        envR[i] = _env_right(envR[i + 1], psi.site(i + 1), mpo[i])
+    energy = 0.0
+    if method == "dmrg1":
+        for _ in range(nsweeps):
+            for i in range(2, n + 1):
+                canonize(psi, MixedCanonical(i))
+                envL[i - 1] = _env_left(envL[i - 2], psi.site(i - 1), mpo[i - 2])
+                energy, y, _ = lanczos_lm(_heff1(envL[i - 1], mpo[i - 1], envR[i]), psi.site(i), krylovdim, maxiter,
+                                          tol)
+                psi.set_site(i, y)
+            if history is not None:
+                history.append(energy)
+            for i in range(n - 1, 0, -1):
+                canonize(psi, MixedCanonical(i))
+                envR[i] = _env_right(envR[i + 1], psi.site(i + 1), mpo[i])
+                energy, y, _ = lanczos_lm(_heff1(envL[i - 1], mpo[i - 1], envR[i]), psi.site(i), krylovdim, maxiter,
+                                          tol)
+                psi.set_site(i, y)
+            if history is not None:
+                history.append(energy)
+        return psi, energy
+    if method != "dmrg2":
+        raise ValueError(f"unknown DMRG method {method!r}")
+
+    def split(y, absorb_right):
+        a, s1, s2, c = y.shape
+        U, S, Vh = svd_thin(y.reshape(a * s1, s2 * c))
+        keep = min(maxdim, S.size)
+        U, S, Vh = U[:, :keep], S[:keep], Vh[:keep]
+        S = S / np.linalg.norm(S)
+        if absorb_right:
+            Vh = S[:, None] * Vh
+        else:
+            U = U * S[None, :]
+        return U.reshape(a, s1, keep), Vh.reshape(keep, s2, c)
+
+    for _ in range(nsweeps):
+        for i in range(2, n + 1):
+            canonize(psi, MixedCanonical(i))
+            if i > 2:
+                envL[i - 2] = _env_left(envL[i - 3], psi.site(i - 2), mpo[i - 3])
+            theta = np.tensordot(psi.site(i - 1), psi.site(i), axes=(2, 0))
+            energy, y, _ = lanczos_lm(_heff2(envL[i - 2], mpo[i - 2], mpo[i - 1], envR[i]), theta, krylovdim, maxiter,
+                                      tol)
+            A, B = split(y, True)
+            psi.set_site(i - 1, A)
+            psi.set_site(i, B)
+            psi.form = MixedCanonical(i)
+        if history is not None:
+            history.append(energy)
+        for i in range(n - 1, 0, -1):
+            canonize(psi, MixedCanonical(i))
+            if i < n - 1:
+                envR[i + 1] = _env_right(envR[i + 2], psi.site(i + 2), mpo[i + 1])
+            theta = np.tensordot(psi.site(i), psi.site(i + 1), axes=(2, 0))
+            energy, y, _ = lanczos_lm(_heff2(envL[i - 1], mpo[i - 1], mpo[i], envR[i + 1]), theta, krylovdim, maxiter,
+                                      tol)
+            A, B = split(y, False)
+            psi.set_site(i, A)
+            psi.set_site(i + 1, B)
+            psi.form = MixedCanonical(i)
+        if history is not None:
+            history.append(energy)
+    return psi, energy

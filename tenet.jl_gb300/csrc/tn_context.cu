@@ -1,5 +1,6 @@
 // Context, device memory accounting, workspace arena, errors.
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 
 #include "tn_internal.cuh"
@@ -44,6 +45,14 @@ tn_status_t tn_dev_free(tn_ctx* ctx, void* p) {
   ctx->allocs.erase(it);
   TN_CHECK_CUDA(ctx, cudaFree(p));
   return TN_OK;
+}
+
+void ws_overflow(tn_ctx* ctx, size_t need) {
+  cudaStreamSynchronize(ctx->stream);
+  fprintf(stderr, "tenetgb: workspace overflow: %zu bytes taken, %zu reserved (a missing ws_reserve)\n", need,
+          ctx->ws_cap);
+  fflush(stderr);
+  std::abort();
 }
 
 tn_status_t ws_reserve(tn_ctx* ctx, size_t bytes) {

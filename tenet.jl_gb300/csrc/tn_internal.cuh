@@ -153,9 +153,14 @@ tn_status_t tn_dev_free(tn_ctx* ctx, void* p);
 // workspace: reserve (may reallocate: only between operations), then take
 tn_status_t ws_reserve(tn_ctx* ctx, size_t bytes);
 inline size_t ws_round(size_t b) { return (b + 255) & ~size_t(255); }
+// a take beyond the reserved arena is a bug in the caller's size computation: stop the
+// process on the host (after the stream has drained, so no kernel is left in flight)
+// rather than hand a kernel memory outside the arena
+[[noreturn]] void ws_overflow(tn_ctx* ctx, size_t need);
 template <typename T>
 T* ws_take(tn_ctx* ctx, size_t count) {
   size_t b = ws_round(count * sizeof(T));
+  if (ctx->ws_top + b > ctx->ws_cap) ws_overflow(ctx, ctx->ws_top + b);
   char* p = ctx->ws + ctx->ws_top;
   ctx->ws_top += b;
   return reinterpret_cast<T*>(p);

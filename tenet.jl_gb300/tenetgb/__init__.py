@@ -19,6 +19,7 @@ from .core import (
     tensor_qr_thin,
     tensor_svd_thin,
 )
+from .dmrg import Dmrg1, Dmrg2, dmrg, dmrg_, ising_1d_mpo
 from .mps import (
     MPS,
     BondCanonical,
