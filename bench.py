@@ -413,6 +413,33 @@ def profile_svd(args):
     print(json.dumps({"profile_svd_ms": 1e3 * dt, "m": 512, "n": 512}))
 
 
+def profile_dmrg(args):
+    """One saturated dmrg!(ψ, H, 1; Dmrg2, maxdim = 128) call on the 100-site Ising chain:
+    five untimed calls from the product state saturate the bonds, the sixth is bracketed by
+    cudaProfilerStart/Stop (launch list of one sweep)."""
+    import torch
+
+    import tenetgb
+
+    n, chi = 100, 128
+    ctx = tenetgb.Context(0)
+    H = tenetgb.ising_1d_mpo(n, 1.0, 1.0)
+    psi = tenetgb.MPS([np.array([1.0, 0.0], dtype=np.complex128).reshape(1, 2, 1) for _ in range(n)], ctx=ctx)
+    for rep in range(6):
+        ctx.sync()
+        if rep == 5:
+            l0 = ctx.launches()
+            torch.cuda.profiler.start()
+        t0 = time.perf_counter()
+        _, E = tenetgb.dmrg_(psi, H, 1, method=tenetgb.Dmrg2, maxdim=chi)
+        ctx.sync()
+        dt = time.perf_counter() - t0
+        if rep == 5:
+            torch.cuda.profiler.stop()
+    print(json.dumps({"profile_dmrg_ms": 1e3 * dt, "energy": float(E), "launches": ctx.launches() - l0,
+                      "bond_max": max(psi.bondsizes())}))
+
+
 def run_lattice(args):
     """Closed 8×8 lattice, bond 8, ComplexF32 (seed 4): contraction to a scalar along the
     planner's path, in 3×TF32 (tensor pipe), TF32, FP32 (CUDA cores) and FP64; errors
@@ -749,15 +776,99 @@ def run_serving(args):
     }))
 
 
+def run_dmrg(args):
+    """2-site DMRG of the 100-site Ising chain (h = J = 1) at χ = 128, the workload of the
+    reference's examples/dmrg.ipynb: ``dmrg!(ψ, H, 1; method = Dmrg2(), maxdim = 128)``
+    called once per step, starting from the product state |0…0⟩.  Ten calls in all (the
+    notebook's count; bonds saturate at 128 after four), the last ``steps`` of them timed
+    with CUDA events on the library's stream, L2 flushed between steps.  The energy after
+    the tenth call is compared with the notebook's value, -126.96187478469312.  One JSON
+    line (a secondary workload)."""
+    import torch
+
+    import tenetgb
+    from oracle import tenet_oracle as O
+
+    n, chi, total = 100, 128, max(10, args.steps + args.warmup + 4)
+    ctx = tenetgb.Context(0)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    H = tenetgb.ising_1d_mpo(n, 1.0, 1.0)
+    prod = [np.array([1.0, 0.0], dtype=np.complex128).reshape(1, 2, 1) for _ in range(n)]
+    psi = tenetgb.MPS([s.copy() for s in prod], ctx=ctx)
+    times, energies = [], []
+    launches0 = None
+    with ClockSampler(0) as clk:
+        for call in range(1, total + 1):
+            timed = call > total - args.steps
+            with torch.cuda.stream(stream):
+                flush_l2(torch, flush)
+            ctx.sync()
+            if timed and launches0 is None:
+                launches0 = ctx.launches()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            _, E = tenetgb.dmrg_(psi, H, 1, method=tenetgb.Dmrg2, maxdim=chi)
+            e1.record(stream)
+            e1.synchronize()
+            energies.append(float(E))
+            if timed:
+                times.append(e0.elapsed_time(e1))
+    launches = ctx.launches() - launches0
+    ms = float(np.mean(times))
+    # end to end: the MPS from pinned host buffers, one call, the MPS and energy back
+    host_sites = [psi.site(i) for i in range(1, n + 1)]
+    pinned = [torch.from_numpy(np.asfortranarray(s).reshape(-1, order="F").view(np.float64)).pin_memory()
+              for s in host_sites]
+    h2d = sum(t.numel() * 8 for t in pinned)
+    e2e_times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        arrays = [t.numpy().view(np.complex128).reshape(s.shape, order="F") for t, s in zip(pinned, host_sites)]
+        q = tenetgb.MPS(arrays, ctx=ctx)
+        q.unsafe_setform_(tenetgb.MixedCanonical(1))
+        _, Eq = tenetgb.dmrg_(q, H, 1, method=tenetgb.Dmrg2, maxdim=chi)
+        back = q.sites()
+        e2e_times.append(time.perf_counter() - t0)
+        del q
+    d2h = sum(b.nbytes for b in back) + 8
+    # CPU: the oracle on the same saturated state: environments plus the first 40 of the
+    # 2(n-1) local updates of one call, extrapolated to the whole call
+    tm = {}
+    O.dmrg(O.OMPS([s.copy() for s in host_sites], form=O.MixedCanonical(1)), O.ising_1d_mpo(n, 1.0, 1.0), 1,
+           method="dmrg2", maxdim=chi, limit=40, timing=tm)
+    cpu_s = tm["env_s"] + tm["updates_s"] / max(1, tm["updates"]) * 2 * (n - 1)
+    known = -126.96187478469312
+    print(json.dumps({
+        "metric": "dmrg2_sweeps_per_s_ising_n100_chi128", "value": 1e3 / ms, "unit": "sweeps/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": total - args.steps, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "replicas", "vs_baseline": None, "dtype": "c128 (FP64 GEMMs, Lanczos and Jacobi SVD)",
+        "data": "synthetic (Ising MPO h = J = 1, product start state; examples/dmrg.ipynb)",
+        "config": {"workload": "dmrg2_ising_n100_chi128", "n": n, "maxdim": chi, "krylovdim": 3, "maxiter": 2,
+                   "calls": total, "step": "dmrg!(ψ, H, 1) on the saturated MPS (environments + one sweep)",
+                   "l2": "flushed between steps (256 MB write)"},
+        "energy_after_10_calls": energies[9], "energy_known_notebook": known,
+        "energy_abs_diff": abs(energies[9] - known), "energies": energies,
+        "e2e": {"value": 1.0 / float(np.mean(e2e_times)), "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches / max(1, args.steps)), "clocks": clk.summary(),
+        "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": "oracle (numpy/LAPACK) on the same saturated MPS: environments + 40 of the 198 "
+                                   "local updates of one dmrg!(ψ, H, 1) call, scaled to the call"},
+    }))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tebd", choices=["tebd", "lattice", "serving", "kernels", "batched"])
+    ap.add_argument("--workload", default="tebd", choices=["tebd", "lattice", "serving", "kernels", "batched", "dmrg"])
     ap.add_argument("--batched-sample", type=int, default=32, help="instances of the 512-MPS population (batched)")
     ap.add_argument("--queries", type=int, default=200, help="queries per arrival rate (serving)")
     ap.add_argument("--serve-budget-gb", type=float, default=200.0, help="HBM budget of the server (serving)")
     ap.add_argument("--serve-precision", default="native", choices=["native", "mixed"], help="serving arithmetic")
     ap.add_argument("--profile-gate", action="store_true", help="one saturated gate (small ncu case)")
     ap.add_argument("--profile-svd", action="store_true", help="the roofline kernel's SVD (small ncu case)")
+    ap.add_argument("--profile-dmrg", action="store_true", help="one saturated 2-site DMRG sweep (launch list)")
     ap.add_argument("--precision", default="native", choices=["native", "mixed"])
     ap.add_argument("--batch", type=int, default=16, help="MPS instances advanced in lockstep")
     ap.add_argument("--gpus", type=int, default=1)
@@ -771,6 +882,8 @@ def main():
         profile_gate(args)
     elif args.profile_svd:
         profile_svd(args)
+    elif args.profile_dmrg:
+        profile_dmrg(args)
     elif args.workload == "lattice":
         run_lattice(args)
     elif args.workload == "serving":
@@ -779,6 +892,8 @@ def main():
         run_kernels(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "dmrg":
+        run_dmrg(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -786,8 +786,12 @@ def _heff2(Lenv, W1, W2, Renv):
     return apply
 
 
+class _Stop(Exception):
+    pass
+
+
 def dmrg(psi: OMPS, mpo, nsweeps=4, method="dmrg1", maxdim=128, krylovdim=3, maxiter=2, tol=1e-12,
-         history=None):
+         history=None, limit=None, timing=None):
     """dmrg!(ψ, H; method) (src/Algorithms/DMRG.jl:45-461) on a copy of ψ.
 
     Dmrg1 (DMRG.jl:45-210): right environments from canonize!(ψ, i), i = n-1…1; each sweep
@@ -797,7 +801,12 @@ def dmrg(psi: OMPS, mpo, nsweeps=4, method="dmrg1", maxdim=128, krylovdim=3, max
     [right→left, centre i] is optimised as one tensor θ, split by a thin SVD, the leading
     min(maxdim, k) values kept and normalised, and S absorbed towards the sweep direction.
     Returns (ψ, energy of the last eigensolve).  ``history`` (a list) receives the energy
-    after each half sweep."""
+    after each half sweep.  ``limit`` stops after that many local updates (a bounded CPU
+    sample; ``timing``, a dict, then receives the environment set-up time and the number
+    and time of the updates done)."""
+    import time as _time
+
+    t_start = _time.perf_counter()
     psi = psi.copy()
     n = psi.L
     one = np.ones((1, 1, 1), dtype=np.complex128)
@@ -806,6 +815,29 @@ def dmrg(psi: OMPS, mpo, nsweeps=4, method="dmrg1", maxdim=128, krylovdim=3, max
     for i in range(n - 1, 0, -1):
         canonize(psi, MixedCanonical(i))
         envR[i] = _env_right(envR[i + 1], psi.site(i + 1), mpo[i])
+    energy = 0.0
+    t_env = _time.perf_counter() - t_start
+    done = [0]
+    lanczos = lanczos_lm
+
+    def lanczos_lm_counted(*a):  # noqa: ANN001
+        if limit is not None and done[0] >= limit:
+            raise _Stop
+        done[0] += 1
+        return lanczos(*a)
+
+    try:
+        return _dmrg_sweeps(psi, mpo, nsweeps, method, maxdim, krylovdim, maxiter, tol, history, envL, envR,
+                            lanczos_lm_counted)
+    except _Stop:
+        return psi, energy
+    finally:
+        if timing is not None:
+            timing.update({"env_s": t_env, "updates": done[0], "updates_s": _time.perf_counter() - t_start - t_env})
+
+
+def _dmrg_sweeps(psi, mpo, nsweeps, method, maxdim, krylovdim, maxiter, tol, history, envL, envR, lanczos_lm):
+    n = psi.L
     energy = 0.0
     if method == "dmrg1":
         for _ in range(nsweeps):

@@ -23,6 +23,8 @@
 // sequence of launches with no host round trip.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <vector>
 
 #include "tn_mps_internal.cuh"
@@ -503,35 +505,108 @@ tn_status_t copy_out(tn_ctx* ctx, cxd* dst, size_t sDst, const cxd* src, size_t 
   return TN_OK;
 }
 
-// split the optimised pair (j, j+1) held in slot 0: thin SVD, keep min(maxdim, k) values,
-// normalise them and absorb them into site j+1 (absorb_right) or site j
-tn_status_t split_pair(Dmrg& D, int j, bool absorb_right) {
+// X_b ← inv_b · X_b (elems elements per instance)
+__global__ void k_scale_inst(int64_t elems, cxd* __restrict__ X, int64_t sX, const double* __restrict__ inv) {
+  const int b = blockIdx.y;
+  const double g = inv[b];
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < elems; t += (int64_t)gridDim.x * blockDim.x) {
+    cxd v = X[b * sX + t];
+    X[b * sX + t] = mkcx(g * v.x, g * v.y);
+  }
+}
+
+tn_status_t scale_inst(Dmrg& D, cxd* X, int64_t sX, int64_t elems) {
+  dim3 grid(grid_for(D.ctx, elems, 256), (unsigned)D.B);
+  k_scale_inst<<<grid, 256, 0, D.ctx->stream>>>(elems, X, sX, D.inv);
+  TN_LAUNCHED(D.ctx);
+  return TN_OK;
+}
+
+// split the optimised pair (j, j+1) held in slot 0 (θ, m × n with m = χ_{j-1} d and
+// n = d χ_{j+1}): thin SVD, keep min(maxdim, k) values, normalise them and absorb them
+// into site j+1 (absorb_right) or site j (DMRG.jl:338-349, 437-448).  Only the singular
+// vectors on the side that stays an isometry are computed; the other side is the
+// projection of θ onto them, which equals S·Vᴴ (or U·S) without dividing by S:
+//   absorb right, m ≥ n:  U S = svd_left(θ);   site j = U_keep,   site j+1 = U_keepᴴ θ / ‖S_keep‖
+//   absorb left,  n ≥ m:  V S = svd_left(θᴴ);  site j+1 = V_keepᴴ, site j = θ V_keep / ‖S_keep‖
+// Near the chain ends (the other shapes) the full thin SVD is used.
+tn_status_t split_pair_impl(Dmrg& D, int j, bool absorb_right) {
   tn_mps* p = D.p;
   tn_ctx* ctx = D.ctx;
   const int64_t d = D.d, m = p->bond[j - 1] * d, n = d * p->bond[j + 1], k = std::min(m, n);
   const int64_t keep = std::min(D.maxdim, k);
-  TN_RETURN_IF(ws_reserve(ctx, svd_any_workspace(TN_C64, p->prec, m, n, D.B)));
-  TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, D.V, m, D.sV, D.U, D.Nmax, D.S, D.Nmax, D.Vh, D.Nmax, D.B));
-  k_inv_norm<<<D.B, 256, 0, ctx->stream>>>((int)keep, D.S, D.Nmax, D.inv);
-  TN_LAUNCHED(ctx);
-  TN_RETURN_IF(mps_ensure_site(p, j, (size_t)(m * keep)));
-  TN_RETURN_IF(mps_ensure_site(p, j + 1, (size_t)(keep * n)));
-  dim3 gU(grid_for(ctx, m * keep, 256), (unsigned)D.B), gV(grid_for(ctx, keep * n, 256), (unsigned)D.B);
-  if (absorb_right) {
+  const cxd* theta = D.V;
+  if (absorb_right && m >= n) {
+    TN_RETURN_IF(ws_reserve(ctx, svd_left_workspace(p->prec, m, n, D.B)));
+    TN_RETURN_IF(svd_left(ctx, p->prec, m, n, theta, m, D.sV, D.U, D.Nmax, D.S, D.Nmax, D.B, keep));
+    k_inv_norm<<<D.B, 256, 0, ctx->stream>>>((int)keep, D.S, D.Nmax, D.inv);
+    TN_LAUNCHED(ctx);
+    TN_RETURN_IF(mps_ensure_site(p, j, (size_t)(m * keep)));
+    TN_RETURN_IF(mps_ensure_site(p, j + 1, (size_t)(keep * n)));
     TN_RETURN_IF(copy_out(ctx, p->site[j], p->cap[j], D.U, D.Nmax, (size_t)(m * keep), D.B));
-    k_absorb_rows<<<gV, 256, 0, ctx->stream>>>(keep, n, D.Vh, k, D.Nmax, D.S, D.Nmax, D.inv, p->site[j + 1],
-                                               (int64_t)p->cap[j + 1]);
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', keep, n, m, kOne, D.U, m, D.Nmax, theta, m, D.sV, kZero,
+                                 p->site[j + 1], keep, (int64_t)p->cap[j + 1], D.B));
+    TN_RETURN_IF(scale_inst(D, p->site[j + 1], (int64_t)p->cap[j + 1], keep * n));
+  } else if (!absorb_right && n >= m) {
+    // θᴴ (n × m) into the x0 buffer (θ itself stays in slot 0)
+    TN_RETURN_IF(transpose_cx<double>(ctx, m, n, theta, m, D.sV, D.x0, n, D.Nmax, D.B, true));
+    TN_RETURN_IF(ws_reserve(ctx, svd_left_workspace(p->prec, n, m, D.B)));
+    TN_RETURN_IF(svd_left(ctx, p->prec, n, m, D.x0, n, D.Nmax, D.U, D.Nmax, D.S, D.Nmax, D.B, keep));
+    k_inv_norm<<<D.B, 256, 0, ctx->stream>>>((int)keep, D.S, D.Nmax, D.inv);
     TN_LAUNCHED(ctx);
+    TN_RETURN_IF(mps_ensure_site(p, j, (size_t)(m * keep)));
+    TN_RETURN_IF(mps_ensure_site(p, j + 1, (size_t)(keep * n)));
+    TN_RETURN_IF(transpose_cx<double>(ctx, n, keep, D.U, n, D.Nmax, p->site[j + 1], keep, (int64_t)p->cap[j + 1], D.B,
+                                      true));
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, keep, n, kOne, theta, m, D.sV, D.U, n, D.Nmax, kZero, p->site[j], m,
+                                 (int64_t)p->cap[j], D.B));
+    TN_RETURN_IF(scale_inst(D, p->site[j], (int64_t)p->cap[j], m * keep));
   } else {
-    k_absorb_cols<<<gU, 256, 0, ctx->stream>>>(m, keep, D.U, D.Nmax, D.S, D.Nmax, D.inv, p->site[j],
-                                               (int64_t)p->cap[j]);
+    TN_RETURN_IF(ws_reserve(ctx, svd_any_workspace(TN_C64, p->prec, m, n, D.B)));
+    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, theta, m, D.sV, D.U, D.Nmax, D.S, D.Nmax, D.Vh, D.Nmax, D.B));
+    k_inv_norm<<<D.B, 256, 0, ctx->stream>>>((int)keep, D.S, D.Nmax, D.inv);
     TN_LAUNCHED(ctx);
-    TN_RETURN_IF(copy_matrix_cxd(ctx, keep, n, D.Vh, k, p->site[j + 1], keep, D.Nmax, (int64_t)p->cap[j + 1], D.B));
+    TN_RETURN_IF(mps_ensure_site(p, j, (size_t)(m * keep)));
+    TN_RETURN_IF(mps_ensure_site(p, j + 1, (size_t)(keep * n)));
+    dim3 gU(grid_for(ctx, m * keep, 256), (unsigned)D.B), gV(grid_for(ctx, keep * n, 256), (unsigned)D.B);
+    if (absorb_right) {
+      TN_RETURN_IF(copy_out(ctx, p->site[j], p->cap[j], D.U, D.Nmax, (size_t)(m * keep), D.B));
+      k_absorb_rows<<<gV, 256, 0, ctx->stream>>>(keep, n, D.Vh, k, D.Nmax, D.S, D.Nmax, D.inv, p->site[j + 1],
+                                                 (int64_t)p->cap[j + 1]);
+      TN_LAUNCHED(ctx);
+    } else {
+      k_absorb_cols<<<gU, 256, 0, ctx->stream>>>(m, keep, D.U, D.Nmax, D.S, D.Nmax, D.inv, p->site[j],
+                                                 (int64_t)p->cap[j]);
+      TN_LAUNCHED(ctx);
+      TN_RETURN_IF(copy_matrix_cxd(ctx, keep, n, D.Vh, k, p->site[j + 1], keep, D.Nmax, (int64_t)p->cap[j + 1], D.B));
+    }
   }
   p->bond[j] = keep;
   p->cap_bond[j] = std::max(p->cap_bond[j], keep);
   p->lam_len = 0;
   return TN_OK;
+}
+
+// A split whose SVD does not converge leaves the pair matrix (instance 0) in
+// $TENETGB_DUMP_DIR/dmrg_pair_<j>.bin when that variable is set: int64 m, n, then the
+// column-major ComplexF64 data — the input a bug report needs.
+tn_status_t split_pair(Dmrg& D, int j, bool absorb_right) {
+  const tn_status_t st = split_pair_impl(D, j, absorb_right);
+  const char* dir = getenv("TENETGB_DUMP_DIR");
+  if (st != TN_ENOCONV || !dir) return st;
+  tn_mps* p = D.p;
+  const int64_t m = p->bond[j - 1] * D.d, n = D.d * p->bond[j + 1];
+  std::vector<cxd> h((size_t)(m * n));
+  if (cudaMemcpy(h.data(), D.V, sizeof(cxd) * h.size(), cudaMemcpyDeviceToHost) != cudaSuccess) return st;
+  char path[1024];
+  snprintf(path, sizeof(path), "%s/dmrg_pair_%d.bin", dir, j);
+  if (FILE* f = fopen(path, "wb")) {
+    fwrite(&m, sizeof(m), 1, f);
+    fwrite(&n, sizeof(n), 1, f);
+    fwrite(h.data(), sizeof(cxd), h.size(), f);
+    fclose(f);
+  }
+  return st;
 }
 
 // θ = site j · site j+1 over their shared bond, into D.x0 (instance stride Nmax)

@@ -358,6 +358,23 @@ __global__ void k_g_colnorms(const JacD* __restrict__ D, const int* __restrict__
   }
 }
 
+// d.nrm[d.n] = ‖W‖²_F (fixed summation order), for the negligible-column threshold
+__global__ void __launch_bounds__(256) k_g_fro(const JacD* __restrict__ D, const int* __restrict__ active) {
+  __shared__ double red[8];
+  const JacD d = D[blockIdx.x];
+  if (!active[blockIdx.x]) return;
+  double f = 0.0;
+  for (int64_t c = threadIdx.x; c < d.n; c += 256) f += d.nrm[c];
+  f = warp_sum(f);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = f;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0;
+    for (int w = 0; w < 8; ++w) a += red[w];
+    d.nrm[d.n] = a;
+  }
+}
+
 // one round of the circle ordering: CTA (pair, instance), the pair's columns held in
 // registers (m ≤ NT·R); rotation formed by one thread (see the uniform-batch kernel)
 template <int NT, int R>
@@ -404,12 +421,29 @@ __global__ void __launch_bounds__(NT)
       g.y += red[w][1];
     }
     const double al = d.nrm[i], be = d.nrm[j];
-    const double ag2 = abs2(g), ab = al * be;
-    int apply = ag2 > tol * tol * ab && ag2 > 0.0;
-    if (ab > 0.0) atomicMax(&rotated[nprob + b], __float_as_int(sqrtf((float)(ag2 / ab))));
+    // columns at or below ε²·‖W‖²_F are numerically zero and left alone (the uniform
+    // batch kernel's rule: a graded matrix's near-null columns otherwise keep nearly every
+    // pair rotating for tens of sweeps); |γ| and √α√β without squaring small numbers
+    const double negl = 4.930380657631324e-32 * d.nrm[d.n];
+    const double fl = negl > 1e-290 ? negl : 1e-290;
+    double ag = 0.0;
+    int apply = 0;
+    if (al > fl && be > fl) {
+      const double ab = al * be;
+      if (ab > 1e-290) {
+        const double ag2 = abs2(g);
+        apply = ag2 > tol * tol * ab && ag2 > 0.0;
+        atomicMax(&rotated[nprob + b], __float_as_int(sqrtf((float)(ag2 / ab))));
+        ag = sqrt(ag2);
+      } else {
+        ag = hypot(g.x, g.y);
+        const double sab = sqrt(al) * sqrt(be);
+        apply = ag > tol * sab && ag > 0.0;
+        atomicMax(&rotated[nprob + b], __float_as_int((float)(ag / sab)));
+      }
+    }
     double c = 1.0, sx = 0.0, sy = 0.0;
     if (apply) {
-      const double ag = sqrt(ag2);
       const double zeta = (be - al) / (2.0 * ag);
       const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
       if (t == 0.0) {
@@ -496,6 +530,20 @@ __global__ void __launch_bounds__(512) k_g_svd_finish(const JacD* __restrict__ D
     const cxd w = d.W[row + (int64_t)idx[c] * d.m];
     d.U[t] = s > 0.0 ? mkcx(w.x / s, w.y / s) : mkcx(0.0, 0.0);
   }
+}
+
+// orthonormal completion of the kept U columns whose σ is numerically zero (the columns
+// the sweeps left alone), as for the uniform batch
+__global__ void __launch_bounds__(256) k_g_complete(const JacD* __restrict__ D) {
+  extern __shared__ unsigned char smem_raw[];
+  cxd* c = reinterpret_cast<cxd*>(smem_raw);
+  __shared__ double red[32];
+  __shared__ int64_t first, next_k;
+  const JacD d = D[blockIdx.x];
+  if (threadIdx.x == 0) first = negligible_start(d.S, d.n, 4.930380657631324e-32, 1e-290);  // ε² of FP64
+  __syncthreads();
+  if (first >= d.r) return;
+  complete_columns<double>(d.m, d.r, first, d.U, c, red, &next_k);
 }
 
 // Gaussian fill (counter-based hash → Box–Muller) with per-site variance 1/(d χ_{i-1})
@@ -644,6 +692,7 @@ tn_status_t g_svd_left(tn_ctx* ctx, std::vector<JacD>& h, int* active, int* rota
   TN_CHECK_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   cudaMemsetAsync(rotated, 0, sizeof(int) * 2 * P, ctx->stream);
   k_g_colnorms<<<dim3(blk(32 * 512, 64), P), 256, 0, ctx->stream>>>(d, active);
+  k_g_fro<<<(unsigned)P, 256, 0, ctx->stream>>>(d, active);
   const dim3 grid((unsigned)(Nmax / 2), (unsigned)P);
   for (int r = 0; r < Nmax - 1; ++r) {
     if (mmax <= 512)
@@ -670,7 +719,7 @@ tn_status_t g_svd_left(tn_ctx* ctx, std::vector<JacD>& h, int* active, int* rota
   int n_active = P;
   for (int sweep = 0; sweep < 40 && n_active > 0; ++sweep) {
     TN_CHECK_CUDA(ctx, cudaGraphLaunch(ge, ctx->stream));
-    ctx->launches += Nmax;
+    ctx->launches += Nmax + 1;
     TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * 2 * P, cudaMemcpyDeviceToHost, ctx->stream));
     TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     n_active = 0;
@@ -689,6 +738,10 @@ tn_status_t g_svd_left(tn_ctx* ctx, std::vector<JacD>& h, int* active, int* rota
   while (P2 < nmax) P2 <<= 1;
   const size_t smem = (sizeof(double) + sizeof(int)) * (size_t)P2;  // ≤ 48 KB for n ≤ 4096
   k_g_svd_finish<<<(unsigned)P, 512, smem, ctx->stream>>>(d, P2);
+  TN_LAUNCHED(ctx);
+  const size_t csm = sizeof(cxd) * (size_t)nmax;
+  TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_g_complete, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csm));
+  k_g_complete<<<(unsigned)P, 256, csm, ctx->stream>>>(d);
   TN_LAUNCHED(ctx);
   return TN_OK;
 }
@@ -925,7 +978,7 @@ tn_status_t tn_group_canonize_compress_norm(tn_group* g, const int64_t* maxdim, 
       const int64_t m = g->bond[b][k - 1] * d, n = g->bond[b][k], n2 = d * g->bond[b][k + 1];
       const int64_t r = std::min<int64_t>(maxdim[b], std::min(m, n));
       need += al256(sizeof(cxd) * (size_t)(m * n)) + al256(sizeof(cxd) * (size_t)(m * r)) +
-              2 * al256(sizeof(double) * (size_t)n) + al256(sizeof(int) * (size_t)n) +
+              al256(sizeof(double) * (size_t)(n + 1)) + al256(sizeof(double) * (size_t)n) + al256(sizeof(int) * (size_t)n) +
               al256(sizeof(cxd) * (size_t)(r * n)) + al256(sizeof(cxd) * (size_t)(r * n2));
     }
     TN_RETURN_IF(ws_reserve(ctx, need));
@@ -947,7 +1000,7 @@ tn_status_t tn_group_canonize_compress_norm(tn_group* g, const int64_t* maxdim, 
       q.N = 0;
       q.W = ws_take<cxd>(ctx, (size_t)(m * n));
       q.U = ws_take<cxd>(ctx, (size_t)(m * r));
-      q.nrm = ws_take<double>(ctx, (size_t)n);
+      q.nrm = ws_take<double>(ctx, (size_t)(n + 1));  // column norms, then ‖W‖²_F
       q.S = ws_take<double>(ctx, (size_t)n);
       q.order = ws_take<int>(ctx, (size_t)n);
       cxd* Z = ws_take<cxd>(ctx, (size_t)(r * n));

@@ -76,6 +76,71 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// Orthonormal completion of columns [first, ncols) of U (m × ncols, ld m, m ≥ ncols)
+// against all earlier columns, as a Householder SVD's U has for numerically zero σ: unit
+// vectors e_k taken in turn, orthogonalised twice, accepted once ≥ 0.5/√m of them remains
+// (the complement's projector has trace m − j ≥ 1, so some e_k keeps ≥ 1/√m).  Called by
+// a whole block (blockDim.x a multiple of 32, ≤ 1024); c: shared scratch of ncols
+// elements, red: 32 shared doubles, next_k: a shared counter.
+template <typename T>
+__device__ void complete_columns(int64_t m, int64_t ncols, int64_t first, cx<T>* U0, cx<T>* c, double* red,
+                                 int64_t* next_k) {
+  if (threadIdx.x == 0) *next_k = 0;
+  __syncthreads();
+  const double accept = 0.5 / sqrt((double)m);
+  for (int64_t j = first; j < ncols; ++j) {
+    cx<T>* u = U0 + j * m;
+    for (int64_t attempt = 0; attempt < m; ++attempt) {
+      const int64_t k = *next_k;
+      for (int64_t t = threadIdx.x; t < m; t += blockDim.x) u[t] = mkcx<T>(t == k ? T(1) : T(0), T(0));
+      __syncthreads();
+      for (int pass = 0; pass < 2; ++pass) {
+        for (int64_t q = threadIdx.x; q < j; q += blockDim.x) {
+          cx<T> acc = mkcx<T>(0, 0);
+          const cx<T>* uq = U0 + q * m;
+          for (int64_t t = 0; t < m; ++t) cfma_cj(acc, uq[t], u[t]);
+          c[q] = acc;
+        }
+        __syncthreads();
+        for (int64_t t = threadIdx.x; t < m; t += blockDim.x) {
+          cx<T> v = u[t];
+          for (int64_t q = 0; q < j; ++q) v = v - U0[q * m + t] * c[q];
+          u[t] = v;
+        }
+        __syncthreads();
+      }
+      double ss = 0.0;
+      for (int64_t t = threadIdx.x; t < m; t += blockDim.x) ss += (double)abs2(u[t]);
+      ss = warp_sum(ss);
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = ss;
+      __syncthreads();
+      double nrm = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) nrm += red[w];
+      nrm = sqrt(nrm);
+      __syncthreads();
+      if (threadIdx.x == 0) *next_k = (k + 1) % m;
+      if (nrm >= accept) {
+        const T inv = T(1.0 / nrm);
+        for (int64_t t = threadIdx.x; t < m; t += blockDim.x) u[t] = inv * u[t];
+        __syncthreads();
+        break;
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// first index of the trailing σ (sorted descending, n values) with σ² ≤ 2·max(negl_rel·Σσ²,
+// floor_abs): the columns one-sided Jacobi leaves as numerically zero
+__device__ inline int64_t negligible_start(const double* s, int64_t n, double negl_rel, double floor_abs) {
+  double f = 0.0;
+  for (int64_t j = 0; j < n; ++j) f += s[j] * s[j];
+  const double thr2 = 2.0 * (negl_rel * f > floor_abs ? negl_rel * f : floor_abs);
+  int64_t r = n;
+  while (r > 0 && !(s[r - 1] * s[r - 1] > thr2)) --r;
+  return r;
+}
+
 // ---------------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------------
@@ -105,10 +170,10 @@ struct tn_ctx {
   int refs = 0;
   bool destroy_requested = false;
   // diagnostics of the last Jacobi SVD: sweeps per precision, rotations per sweep of
-  // the first matrix of the large-matrix path (-1: shared-memory path)
+  // the worst active matrix of the large-matrix path (-1: shared-memory path)
   int last_sweeps_fp32 = 0, last_sweeps_fp64 = 0;
   int sweep_rotations[64] = {0};
-  float sweep_ratio[64] = {0};  // largest off-diagonal ratio of each sweep (first matrix)
+  float sweep_ratio[64] = {0};  // largest off-diagonal ratio of each sweep (worst active matrix)
   // autotuned launch parameters, keyed by kernel family + shape bucket
   bool autotune = false;
   std::unordered_map<std::string, std::pair<int, int>> tuning;

@@ -65,18 +65,59 @@ struct RotC {
   int apply;
 };
 
+// Squared column norms at or below the floor are numerically zero: the squares of their
+// entries would be subnormal, so neither their norms nor their inner products carry any
+// precision.  Such columns are left out of the rotations (and of the convergence test);
+// the finaliser gives them orthonormal U columns.  Relative to an O(1) matrix this is far
+// below the absolute accuracy of a Householder SVD (ε‖A‖).
+// unit roundoff of T: columns with ‖w‖ ≤ ε‖A‖_F are numerically zero
 template <typename T>
-__device__ __forceinline__ RotC<T> make_rot_c(T alpha, T beta, cx<T> g, T tol) {
+__host__ __device__ constexpr T jacobi_eps() {
+  return sizeof(T) == 8 ? T(2.220446049250313e-16) : T(1.1920929e-7);
+}
+
+template <typename T>
+struct JacobiFloor;
+template <>
+struct JacobiFloor<double> {
+  static constexpr double value = 1e-290;
+};
+template <>
+struct JacobiFloor<float> {
+  static constexpr float value = 1e-32f;
+};
+
+// negl: squared norm at or below which a column is numerically zero relative to its
+// matrix (ε²·‖A‖²_F): one-sided Jacobi orthogonalises such columns only at the pace of
+// a graded matrix (tens of sweeps with nearly every pair rotating), while their content
+// is below the absolute accuracy of the factorisation anyway
+template <typename T>
+__device__ __forceinline__ RotC<T> make_rot_c(T alpha, T beta, cx<T> g, T tol, T negl) {
   RotC<T> R;
-  const T ag2 = abs2(g);
-  const T ab = alpha * beta;
-  R.apply = ag2 > tol * tol * ab && ag2 > T(0);
-  R.ratio = ab > T(0) ? sqrtf((float)(ag2 / ab)) : 0.f;
   R.c = T(1);
   R.tag = T(0);
   R.se = mkcx<T>(0, 0);
-  if (!R.apply) return R;
-  const T ag = sqrt(ag2);
+  R.apply = 0;
+  R.ratio = 0.f;
+  const T fl = negl > JacobiFloor<T>::value ? negl : JacobiFloor<T>::value;
+  if (!(alpha > fl) || !(beta > fl)) return R;
+  T ag;
+  const T ab = alpha * beta;
+  if (ab > JacobiFloor<T>::value) {
+    // the usual scale: squares are exact enough (one square root on the critical path)
+    const T ag2 = abs2(g);
+    R.ratio = sqrtf((float)(ag2 / ab));
+    R.apply = ag2 > tol * tol * ab && ag2 > T(0);
+    if (!R.apply) return R;
+    ag = sqrt(ag2);
+  } else {
+    // tiny columns: |γ| and √α·√β without squaring small quantities
+    ag = hypot(g.x, g.y);
+    const T sab = sqrt(alpha) * sqrt(beta);
+    R.ratio = (float)(ag / sab);
+    R.apply = ag > tol * sab && ag > T(0);
+    if (!R.apply) return R;
+  }
   const T zeta = (beta - alpha) / (T(2) * ag);
   const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
   if (t == T(0)) {
@@ -170,7 +211,9 @@ __global__ void __launch_bounds__(NT)
       al = nrm[b * n + i];
       be = nrm[b * n + j];
     }
-    RotC<T> Rt = make_rot_c(al, be, g, tol);
+    // ‖A‖²_F of this matrix, stored after the n·batch column norms by k_fro
+    const T negl = jacobi_eps<T>() * jacobi_eps<T>() * nrm[(int64_t)n * gridDim.y + b];
+    RotC<T> Rt = make_rot_c(al, be, g, tol, negl);
     float monitor = Rt.ratio;
     if (tail && (tail[b * n + i] != tail[b * n + j]) && al > T(0) && be > T(0)) {
       // a kept column against a tail column: only the kept column is used, and the
@@ -234,6 +277,25 @@ __global__ void k_col_norms(int64_t m, int64_t n, const cx<T>* W, int64_t sW, T*
   }
 }
 
+// nrm[n·batch + b] = Σ_c nrm[b][c] = ‖W_b‖²_F (fixed summation order: deterministic)
+template <typename T>
+__global__ void __launch_bounds__(256) k_fro(int64_t n, T* nrm, int64_t batch) {
+  __shared__ T red[8];
+  for (int64_t b = blockIdx.x; b < batch; b += gridDim.x) {
+    T f = 0;
+    for (int64_t c = threadIdx.x; c < n; c += 256) f += nrm[b * n + c];
+    f = warp_sum(f);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = f;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T a = 0;
+      for (int w = 0; w < 8; ++w) a += red[w];
+      nrm[n * batch + b] = a;
+    }
+    __syncthreads();
+  }
+}
+
 // whole SVD of one matrix per CTA in shared memory (W m×n and V n×n resident)
 template <typename T>
 __global__ void __launch_bounds__(512)
@@ -254,6 +316,22 @@ __global__ void __launch_bounds__(512)
   __syncthreads();
   const int N = (int)(n + (n & 1));
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  // ‖A‖²_F (invariant under the rotations) for the negligible-column threshold
+  __shared__ T s_fro[16];
+  {
+    T f = 0;
+    for (int64_t t = threadIdx.x; t < m * n; t += blockDim.x) f += abs2(sw[t]);
+    f = warp_sum(f);
+    if (lane == 0) s_fro[warp] = f;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T a = 0;
+      for (int w = 0; w < nwarps; ++w) a += s_fro[w];
+      s_fro[0] = a;
+    }
+    __syncthreads();
+  }
+  const T negl = jacobi_eps<T>() * jacobi_eps<T>() * s_fro[0];
   int sweep = 0;
   for (; sweep < max_sweeps; ++sweep) {
     if (threadIdx.x == 0) s_rot = 0;
@@ -277,7 +355,7 @@ __global__ void __launch_bounds__(512)
         be = warp_sum(be);
         g.x = warp_sum(g.x);
         g.y = warp_sum(g.y);
-        const RotC<T> R = make_rot_c(al, be, g, tol);
+        const RotC<T> R = make_rot_c(al, be, g, tol, negl);
         if (!R.apply) continue;
         if (lane == 0) s_rot = 1;
         for (int64_t t = lane; t < m; t += 32) {
@@ -403,13 +481,30 @@ __global__ void k_svd_gather(int64_t m, int64_t n, const cx<T>* W, int64_t sW, c
   }
 }
 
+// U columns of numerically zero σ (the columns the sweeps left alone, exact zeros of a
+// rank-deficient matrix) get an orthonormal completion, as a Householder SVD's U has; one
+// block per matrix, nothing to do (one pass over S) in the usual full-rank case
+template <typename T>
+__global__ void __launch_bounds__(256) k_svd_complete(int64_t m, int64_t n, cx<T>* U, int64_t sU, const double* S,
+                                                      int64_t sS, double negl_rel, double floor_abs) {
+  extern __shared__ unsigned char smem_raw[];
+  cx<T>* c = reinterpret_cast<cx<T>*>(smem_raw);
+  __shared__ double red[32];
+  __shared__ int64_t first, next_k;
+  const int64_t b = blockIdx.x;
+  if (threadIdx.x == 0) first = negligible_start(S + b * sS, n, negl_rel, floor_abs);
+  __syncthreads();
+  if (first >= n) return;
+  complete_columns<T>(m, n, first, U + b * sU, c, red, &next_k);
+}
+
 }  // namespace
 
 template <typename T>
 size_t svd_workspace(int64_t m, int64_t n, int64_t batch) {
   return ws_round(sizeof(cx<T>) * (size_t)(m * n * batch)) + ws_round(sizeof(cx<T>) * (size_t)(n * n * batch)) +
          ws_round(sizeof(int) * (size_t)(n * batch)) + ws_round(sizeof(int) * (size_t)(batch + 1)) +
-         ws_round(sizeof(int) * (size_t)(2 * batch + 2)) + ws_round(sizeof(T) * (size_t)(n * batch));
+         ws_round(sizeof(int) * (size_t)(2 * batch + 2)) + ws_round(sizeof(T) * (size_t)((n + 1) * batch));
 }
 template size_t svd_workspace<double>(int64_t, int64_t, int64_t);
 template size_t svd_workspace<float>(int64_t, int64_t, int64_t);
@@ -476,6 +571,9 @@ static tn_status_t launch_step(tn_ctx* ctx, int64_t m, int64_t n, int N, int r, 
   TN_LAUNCHED(ctx);
   return TN_OK;
 }
+
+// sweeps of one phase after which the truncation-aware flags are dropped
+constexpr int kTailSweeps = 8;
 
 // Jacobi sweeps on W (m×n dense, batch stride m·n) accumulating into V (n×n dense; may
 // be null on the large-matrix path).  V is set to the identity first unless v_given.
@@ -546,6 +644,7 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       cudaMemsetAsync(rotated, 0, sizeof(int) * 2 * batch, ctx->stream);
       int64_t nb = std::min<int64_t>((n * batch * 32 + 255) / 256, (int64_t)ctx->num_sms * 8);
       k_col_norms<T><<<(unsigned)std::max<int64_t>(nb, 1), 256, 0, ctx->stream>>>(m, n, W, m * n, nrm, batch);
+      k_fro<T><<<(unsigned)std::min<int64_t>(batch, 65535), 256, 0, ctx->stream>>>(n, nrm, batch);
       tn_status_t st = TN_OK;
       for (int r = 0; r < N - 1 && st == TN_OK; ++r)
         st = launch_step<T>(ctx, m, n, N, r, W, V, nrm, active, rotated, tol, gy, tail);
@@ -567,13 +666,24 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
     int n_active = (int)batch;
     for (sweeps = 0; sweeps < max_sweeps && n_active > 0; ++sweeps) {
       TN_CHECK_CUDA(ctx, cudaGraphLaunch(ge, ctx->stream));
-      ctx->launches += N;  // norm refresh + N-1 steps
+      ctx->launches += N + 1;  // norm refresh, ‖A‖_F, N-1 steps
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * 2 * batch, cudaMemcpyDeviceToHost,
                                          ctx->stream));
       TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
       if (sweeps < (int)(sizeof(ctx->sweep_rotations) / sizeof(int))) {
-        ctx->sweep_rotations[sweeps] = h_rot[0];
-        memcpy(&ctx->sweep_ratio[sweeps], &h_rot[batch], sizeof(float));
+        // the matrix with the largest off-diagonal ratio among those still active
+        int64_t worst = 0;
+        float wr = -1.f;
+        for (int64_t b = 0; b < batch; ++b) {
+          float ratio;
+          memcpy(&ratio, &h_rot[batch + b], sizeof(float));
+          if (h_act[b] && ratio > wr) {
+            wr = ratio;
+            worst = b;
+          }
+        }
+        ctx->sweep_rotations[sweeps] = h_rot[worst];
+        ctx->sweep_ratio[sweeps] = wr < 0.f ? 0.f : wr;
       }
       n_active = 0;
       int64_t max_rot = 0;
@@ -583,6 +693,15 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
         if (h_act[b]) max_rot = std::max<int64_t>(max_rot, h_rot[b]);
         h_act[b] = h_act[b] && h_rot[b] && ratio > stop_ratio && h_rot[b] > min_rot;
         n_active += h_act[b];
+      }
+      if (tail && n_active > 0 && sweeps + 1 >= kTailSweeps) {
+        // Without tail–tail rotations the kept columns converge like a subspace
+        // iteration, at a rate set by the gap between the kept and the tail values; a
+        // near-degenerate boundary (entanglement spectra of symmetric ground states)
+        // makes that slow.  Clearing the flags turns the remaining sweeps into full,
+        // quadratically convergent Jacobi (the captured sweep reads the flags).
+        TN_CHECK_CUDA(ctx, cudaMemsetAsync(tail, 0, (size_t)(n * batch), ctx->stream));
+        tail = nullptr;
       }
       if (tail && n_active > 0 && (tail_preset || 2 * max_rot < pairs))
         TN_RETURN_IF(update_tail_flags<T>(ctx, n, batch, nrm, keep, tail));
@@ -616,6 +735,13 @@ static tn_status_t jacobi_finalize(tn_ctx* ctx, int64_t m, int64_t n, const cx<T
   k_svd_gather<T><<<dim3((unsigned)blocks, gy), 256, 0, ctx->stream>>>(m, n, W, m * n, V, n * n, S, sS, order, U, sU,
                                                                         Vo, sVo, vh, batch);
   TN_LAUNCHED(ctx);
+  const size_t csm = sizeof(cx<T>) * (size_t)n;
+  if (csm <= kSmemMax) {
+    TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_svd_complete<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+    const double e = (double)jacobi_eps<T>();
+    k_svd_complete<T><<<gy, 256, csm, ctx->stream>>>(m, n, U, sU, S, sS, e * e, (double)JacobiFloor<T>::value);
+    TN_LAUNCHED(ctx);
+  }
   return TN_OK;
 }
 
@@ -632,7 +758,7 @@ static tn_status_t svd_tall_impl(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>*
   int* order = ws_take<int>(ctx, (size_t)(n * batch));
   int* active = ws_take<int>(ctx, (size_t)(batch + 1));
   int* rotated = ws_take<int>(ctx, (size_t)(2 * batch + 2));
-  T* nrm = ws_take<T>(ctx, (size_t)(n * batch));
+  T* nrm = ws_take<T>(ctx, (size_t)((n + 1) * batch));  // column norms, then ‖W_b‖²_F
   {
     int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
     k_copy_mat<T><<<dim3((unsigned)blocks, (unsigned)batch), 256, 0, ctx->stream>>>(m, n, A, lda, sA, W, m * n, batch);
@@ -709,7 +835,7 @@ size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
   s += 2 * ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // V64, G
   s += ws_round(sizeof(int) * (size_t)(n * batch));
   s += ws_round(sizeof(int) * (size_t)(batch + 1)) + ws_round(sizeof(int) * (size_t)(2 * batch + 2));
-  s += ws_round(sizeof(double) * (size_t)(n * batch)) + ws_round(sizeof(float) * (size_t)(n * batch));
+  s += ws_round(sizeof(double) * (size_t)((n + 1) * batch)) + ws_round(sizeof(float) * (size_t)((n + 1) * batch));
   s += ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // V scratch when V is not wanted
   s += ws_round(sizeof(cxf) * (size_t)(n * n * batch));  // E³ when W32 has no room for it
   s += ws_round((size_t)(n * batch));                     // tail flags
@@ -743,8 +869,8 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   int* order = ws_take<int>(ctx, (size_t)(n * batch));
   int* active = ws_take<int>(ctx, (size_t)(batch + 1));
   int* rotated = ws_take<int>(ctx, (size_t)(2 * batch + 2));
-  double* nrm64 = ws_take<double>(ctx, (size_t)(n * batch));
-  float* nrm32 = ws_take<float>(ctx, (size_t)(n * batch));
+  double* nrm64 = ws_take<double>(ctx, (size_t)((n + 1) * batch));
+  float* nrm32 = ws_take<float>(ctx, (size_t)((n + 1) * batch));
   unsigned char* tail = ws_take<unsigned char>(ctx, (size_t)(n * batch));
   const int64_t keep_m = (!want_v && keep > 0) ? keep + std::max<int64_t>(16, keep / 8) : 0;
   for (int64_t b = 0; b < batch; ++b) {
@@ -832,7 +958,7 @@ tn_status_t svd_left(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_t n, con
   int* order = ws_take<int>(ctx, (size_t)(n * batch));
   int* active = ws_take<int>(ctx, (size_t)(batch + 1));
   int* rotated = ws_take<int>(ctx, (size_t)(2 * batch + 2));
-  double* nrm = ws_take<double>(ctx, (size_t)(n * batch));
+  double* nrm = ws_take<double>(ctx, (size_t)((n + 1) * batch));
   {
     int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
     k_copy_mat<double><<<dim3((unsigned)blocks, (unsigned)batch), 256, 0, ctx->stream>>>(m, n, A, lda, sA, W, m * n,
@@ -958,7 +1084,7 @@ extern "C" tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, c
   if (!d_A || !d_U || !d_S || !d_Vh) return tn_set_error(nullptr, TN_EINVAL, "tn_svd_thin_noalloc: null pointer");
   // scratch layout: W (m×n) | V (n×n) | column norms (n) | order (n) | active | rotated
   const size_t oW = 0, oV = oW + al256(sizeof(cxd) * (size_t)(m * n)), oN = oV + al256(sizeof(cxd) * (size_t)(n * n)),
-               oO = oN + al256(sizeof(double) * (size_t)n), oF = oO + al256(sizeof(int) * (size_t)n),
+               oO = oN + al256(sizeof(double) * (size_t)(n + 1)), oF = oO + al256(sizeof(int) * (size_t)n),
                total = oF + 256;
   if (total > kNoAllocScratchBytes)
     return tn_set_error(nullptr, TN_EINVAL,
@@ -998,6 +1124,8 @@ extern "C" tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, c
     k_col_norms<double><<<(unsigned)std::max<int64_t>(1, std::min<int64_t>((n * 32 + 255) / 256, 1216)), 256, 0, st>>>(
         m, n, W, m * n, nrm, 1);
     NA_CHECK(cudaGetLastError());
+    k_fro<double><<<1, 256, 0, st>>>(n, nrm, 1);
+    NA_CHECK(cudaGetLastError());
     for (int r = 0; r < N - 1; ++r) {
       if (m <= 512)
         k_jacobi_step_reg<double, 128, 4, false><<<grid, 128, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
@@ -1028,6 +1156,12 @@ extern "C" tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, c
   k_svd_gather<double><<<dim3((unsigned)std::min<int64_t>((m * n + 255) / 256, 1024), 1), 256, 0, st>>>(
       m, n, W, m * n, V, n * n, d_S, 0, order, (cxd*)d_U, 0, (cxd*)d_Vh, 0, true, 1);
   NA_CHECK(cudaGetLastError());
+  if (sizeof(cxd) * (size_t)n <= kSmemMax) {
+    NA_CHECK(cudaFuncSetAttribute(k_svd_complete<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmemMax));
+    k_svd_complete<double><<<1, 256, sizeof(cxd) * (size_t)n, st>>>(
+        m, n, (cxd*)d_U, 0, d_S, 0, jacobi_eps<double>() * jacobi_eps<double>(), JacobiFloor<double>::value);
+    NA_CHECK(cudaGetLastError());
+  }
   NA_CHECK(cudaStreamSynchronize(st));
 #undef NA_CHECK
   if (!converged)

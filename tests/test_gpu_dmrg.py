@@ -150,3 +150,34 @@ def test_dmrg_argument_errors():
         tenetgb.dmrg(psi, tenetgb.ising_1d_mpo(4, 1.0, 1.0), 1, ishermitian=False)
     with pytest.raises(ValueError, match="krylovdim"):
         tenetgb.dmrg(psi, tenetgb.ising_1d_mpo(4, 1.0, 1.0), 1, krylovdim=1)
+
+
+def test_dmrg_mixed_precision_matches_native():
+    """Mixed precision (FP32 Jacobi pre-pass, truncation-aware FP64 polish) on the DMRG
+    pair splits: the Ising ground state's near-degenerate Schmidt values at the
+    truncation boundary must not stall the polish; energies equal the FP64 run."""
+    import tenetgb
+
+    n, chi = 20, 64
+    H = tenetgb.ising_1d_mpo(n, 1.0, 1.0)
+    res = {}
+    for prec in ("native", "mixed"):
+        psi = tenetgb.MPS(start_sites("product", n), precision=prec)
+        _, res[prec] = tenetgb.dmrg_(psi, H, 6, method=tenetgb.Dmrg2, maxdim=chi)
+    assert abs(res["native"] - res["mixed"]) < 1e-9
+
+
+def test_dmrg_ordered_phase_spectrum_below_fp64_range():
+    """h = 0.5 (ordered phase): the Schmidt values of the pairs decay past 1e-300 once the
+    bond saturates; the pair SVDs must converge and the sites stay isometries."""
+    import tenetgb
+
+    n, chi, h = 40, 64, 0.5
+    psi = tenetgb.MPS(start_sites("product", n))
+    _, E = tenetgb.dmrg_(psi, tenetgb.ising_1d_mpo(n, h, 1.0), 5, method=tenetgb.Dmrg2, maxdim=chi)
+    _, Er = O.dmrg(O.OMPS(start_sites("product", n)), O.ising_1d_mpo(n, h, 1.0), 5, method="dmrg2", maxdim=chi)
+    assert abs(E - Er) < 1e-9 * abs(Er)
+    for i in range(2, n + 1):
+        A = psi.site(i)
+        m = A.reshape(A.shape[0], -1, order="F")
+        assert np.linalg.norm(m @ m.conj().T - np.eye(A.shape[0])) < 1e-10, i
