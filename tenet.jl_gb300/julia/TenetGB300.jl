@@ -238,4 +238,21 @@ end
 
 LinearAlgebra.normalize!(ψ::GB300MPS) = (check(ccall((:tn_mps_normalize, libtenetgb), Int32, (Ptr{Cvoid},), ψ.h), ψ.ctx.h); ψ)
 
+# dmrg!(ψ, H, nsweeps; method) — src/Algorithms/DMRG.jl:45-459.  H: the MPO's site arrays,
+# column-major (w_l, d_out, d_in, w_r) with w_0 = w_L = 1 (`MPO(arrays; order=(:l, :o, :i, :r))`).
+function dmrg!(ψ::GB300MPS, H::Vector{Array{ComplexF64,4}}, nsweeps::Integer=4; method::Symbol=:dmrg1,
+               maxdim::Integer=128, krylovdim::Integer=3, maxiter::Integer=2, tol::Real=1e-12)
+    ptrs = Ptr{ComplexF64}[pointer(W) for W in H]
+    bonds = Int64[size(W, 4) for W in H[1:end-1]]
+    energy = Ref{Float64}(0.0)
+    GC.@preserve H begin
+        check(ccall((:tn_mps_dmrg, libtenetgb), Int32,
+                    (Ptr{Cvoid}, Ptr{Ptr{ComplexF64}}, Ptr{Int64}, Int32, Int32, Int32, Int64, Int32, Int32, Float64,
+                     Ref{Float64}, Ptr{Float64}),
+                    ψ.h, ptrs, bonds, 1, method === :dmrg2 ? 2 : 1, nsweeps, maxdim, krylovdim, maxiter, tol, energy,
+                    C_NULL), ψ.ctx.h)
+    end
+    return ψ, energy[]
+end
+
 end # module
