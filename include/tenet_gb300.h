@@ -294,6 +294,11 @@ tn_status_t tn_mps_evolve_mpo(tn_mps* mps, const void* const* h_mpo_sites, const
 tn_status_t tn_mps_dmrg(tn_mps* mps, const void* const* h_mpo_sites, const int64_t* mpo_bonds, int32_t mpo_count,
                         int32_t method, int32_t nsweeps, int64_t maxdim, int32_t krylovdim, int32_t maxiter, double tol,
                         double* h_energy, double* h_history);
+/* Device time of the last tn_mps_dmrg on this context, per phase (ms): [0] gauge moves
+ * (canonize!), [1] environment updates, [2] local eigensolves (with forming the pair),
+ * [3] pair splits (Dmrg2); h_updates[0] = local updates timed, h_updates[1] = Jacobi
+ * sweeps summed over the pair splits. */
+tn_status_t tn_dmrg_last_stats(tn_ctx* ctx, double* h_ms, int64_t* h_updates);
 /* dump / load of a device MPS (all instances, the form and Λ) as a raw file: magic
  * "TNMPS001", int32 L, d, B, form, lo, hi, precision, int64 Λ length, int64 bonds[0..L],
  * column-major ComplexF64 sites per instance, then Λ.  max_bond as tn_mps_create. */

@@ -377,8 +377,21 @@ struct Dmrg {
   LzState* st = nullptr;
   int64_t Nmax = 0, sV = 0, sTA = 0, sTB = 0;
   std::vector<void*> owned;
+  // phase timing: an event before each phase of each local update; the elapsed times are
+  // summed once at the end (no synchronisation inside the sweep)
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> ev_phase;  // phase that starts at ev[k] (-1: end marker)
+  tn_status_t mark(int phase) {
+    cudaEvent_t e;
+    TN_CHECK_CUDA(ctx, cudaEventCreate(&e));
+    TN_CHECK_CUDA(ctx, cudaEventRecord(e, ctx->stream));
+    ev.push_back(e);
+    ev_phase.push_back(phase);
+    return TN_OK;
+  }
 
   ~Dmrg() {
+    for (cudaEvent_t e : ev) cudaEventDestroy(e);
     if (ctx) {
       cudaStreamSynchronize(ctx->stream);
       for (void* q : owned) tn_dev_free(ctx, q);
@@ -592,6 +605,7 @@ tn_status_t split_pair_impl(Dmrg& D, int j, bool absorb_right) {
 // column-major ComplexF64 data — the input a bug report needs.
 tn_status_t split_pair(Dmrg& D, int j, bool absorb_right) {
   const tn_status_t st = split_pair_impl(D, j, absorb_right);
+  D.ctx->dmrg_svd_sweeps += std::max(0, D.ctx->last_sweeps_fp64) + std::max(0, D.ctx->last_sweeps_fp32);
   const char* dir = getenv("TENETGB_DUMP_DIR");
   if (st != TN_ENOCONV || !dir) return st;
   tn_mps* p = D.p;
@@ -638,6 +652,7 @@ tn_status_t run(Dmrg& D, const void* const* h_mpo, int mpo_count, int nsweeps, d
   const int64_t d = D.d;
   // bond capacities: Dmrg1 never grows a bond (QR gauge moves keep k = min(m, n) ≤ n);
   // Dmrg2 bonds reach at most min(maxdim, d^k, d^(L-k))
+  ctx->dmrg_svd_sweeps = 0;
   D.cap.assign(L + 1, 1);
   for (int k = 1; k < L; ++k) {
     D.cap[k] = p->bond[k];
@@ -715,45 +730,69 @@ tn_status_t run(Dmrg& D, const void* const* h_mpo, int mpo_count, int nsweeps, d
   for (int sweep = 0; sweep < nsweeps; ++sweep) {
     if (D.method == 1) {
       for (int i = 2; i <= L; ++i) {  // DMRG.jl:88-146
+        TN_RETURN_IF(D.mark(0));
         TN_RETURN_IF(tn_mps_canonize_mixed(p, i, i));
+        TN_RETURN_IF(D.mark(1));
         TN_RETURN_IF(update_left(D, i - 1));
         const int64_t N = p->bond[i - 1] * d * p->bond[i];
+        TN_RETURN_IF(D.mark(2));
         TN_RETURN_IF(eigsolve(D, 1, i, N, p->site[i], (int64_t)p->cap[i]));
         TN_RETURN_IF(copy_out(ctx, p->site[i], p->cap[i], D.V, D.sV, (size_t)N, B));
       }
       if (h_hist) TN_RETURN_IF(read_energies(D, h_hist + (size_t)(hist++) * B));
       for (int i = L - 1; i >= 1; --i) {  // DMRG.jl:150-206
+        TN_RETURN_IF(D.mark(0));
         TN_RETURN_IF(tn_mps_canonize_mixed(p, i, i));
+        TN_RETURN_IF(D.mark(1));
         TN_RETURN_IF(update_right(D, i + 1));
         const int64_t N = p->bond[i - 1] * d * p->bond[i];
+        TN_RETURN_IF(D.mark(2));
         TN_RETURN_IF(eigsolve(D, 1, i, N, p->site[i], (int64_t)p->cap[i]));
         TN_RETURN_IF(copy_out(ctx, p->site[i], p->cap[i], D.V, D.sV, (size_t)N, B));
       }
       if (h_hist) TN_RETURN_IF(read_energies(D, h_hist + (size_t)(hist++) * B));
     } else {
       for (int i = 2; i <= L; ++i) {  // DMRG.jl:258-357
+        TN_RETURN_IF(D.mark(0));
         TN_RETURN_IF(tn_mps_canonize_mixed(p, i, i));
+        TN_RETURN_IF(D.mark(1));
         if (i > 2) TN_RETURN_IF(update_left(D, i - 2));
+        TN_RETURN_IF(D.mark(2));
         TN_RETURN_IF(form_pair(D, i - 1));
         const int64_t N = p->bond[i - 2] * d * d * p->bond[i];
         TN_RETURN_IF(eigsolve(D, 2, i - 1, N, D.x0, D.Nmax));
+        TN_RETURN_IF(D.mark(3));
         TN_RETURN_IF(split_pair(D, i - 1, true));
         p->kind = TN_FORM_MIXED;
         p->lo = p->hi = i;
       }
       if (h_hist) TN_RETURN_IF(read_energies(D, h_hist + (size_t)(hist++) * B));
       for (int i = L - 1; i >= 1; --i) {  // DMRG.jl:361-455
+        TN_RETURN_IF(D.mark(0));
         TN_RETURN_IF(tn_mps_canonize_mixed(p, i, i));
+        TN_RETURN_IF(D.mark(1));
         if (i < L - 1) TN_RETURN_IF(update_right(D, i + 2));
+        TN_RETURN_IF(D.mark(2));
         TN_RETURN_IF(form_pair(D, i));
         const int64_t N = p->bond[i - 1] * d * d * p->bond[i + 1];
         TN_RETURN_IF(eigsolve(D, 2, i, N, D.x0, D.Nmax));
+        TN_RETURN_IF(D.mark(3));
         TN_RETURN_IF(split_pair(D, i, false));
         p->kind = TN_FORM_MIXED;
         p->lo = p->hi = i;
       }
       if (h_hist) TN_RETURN_IF(read_energies(D, h_hist + (size_t)(hist++) * B));
     }
+  }
+  TN_RETURN_IF(D.mark(-1));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (int k = 0; k < 4; ++k) ctx->dmrg_ms[k] = 0.0;
+  ctx->dmrg_updates = 0;
+  for (size_t k = 0; k + 1 < D.ev.size(); ++k) {
+    float ms = 0.f;
+    if (D.ev_phase[k] < 0 || cudaEventElapsedTime(&ms, D.ev[k], D.ev[k + 1]) != cudaSuccess) continue;
+    ctx->dmrg_ms[D.ev_phase[k]] += ms;
+    ctx->dmrg_updates += D.ev_phase[k] == 0;
   }
   if (h_energy) {
     if (nsweeps == 0)
@@ -800,6 +839,16 @@ tn_status_t tn_mps_dmrg(tn_mps* p, const void* const* h_mpo_sites, const int64_t
     D.w[i] = mpo_bonds[i - 1];
   }
   return run(D, h_mpo_sites, mpo_count, nsweeps, h_energy, h_history);
+}
+
+tn_status_t tn_dmrg_last_stats(tn_ctx* ctx, double* h_ms, int64_t* h_updates) {
+  if (!ctx) return TN_EINVAL;
+  for (int k = 0; h_ms && k < 4; ++k) h_ms[k] = ctx->dmrg_ms[k];
+  if (h_updates) {
+    h_updates[0] = ctx->dmrg_updates;
+    h_updates[1] = ctx->dmrg_svd_sweeps;
+  }
+  return TN_OK;
 }
 
 }  // extern "C"

@@ -174,6 +174,11 @@ struct tn_ctx {
   int last_sweeps_fp32 = 0, last_sweeps_fp64 = 0;
   int sweep_rotations[64] = {0};
   float sweep_ratio[64] = {0};  // largest off-diagonal ratio of each sweep (worst active matrix)
+  // time of the last DMRG run per phase (ms): gauge moves, environments, eigensolves,
+  // pair splits; and its local updates
+  double dmrg_ms[4] = {0, 0, 0, 0};
+  int64_t dmrg_updates = 0;
+  int64_t dmrg_svd_sweeps = 0;  // Jacobi sweeps summed over the pair splits
   // autotuned launch parameters, keyed by kernel family + shape bucket
   bool autotune = false;
   std::unordered_map<std::string, std::pair<int, int>> tuning;

@@ -19,6 +19,8 @@
 // The complex 2×2 rotation: with γ = |γ|e^{iφ}, ζ = (β−α)/(2|γ|),
 // t = sgn(ζ)/(|ζ|+√(1+ζ²)), c = 1/√(1+t²), s = c·t:
 //   w_i' = c·w_i − s·e^{−iφ}·w_j,   w_j' = s·e^{iφ}·w_i + c·w_j.
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <mutex>
 
@@ -147,15 +149,14 @@ __device__ __forceinline__ void rot_apply_c(T c, cx<T> se, cx<T>& wi, cx<T>& wj)
 // use the cached norms nrm[], updated analytically (α' = α − t|γ|, β' = β + t|γ|) and
 // recomputed exactly at the start of every sweep (FP64).  V may be null (no
 // accumulation: the caller recovers Vh from U and A).
+// The rotation of columns (i, j) of matrix b by one CTA (shared by the per-round kernel
+// and the persistent cooperative one).  nmat: matrices in the batch (‖W_b‖²_F sits at
+// nrm[n·nmat + b]); counters: rotations of matrix b at cnt[b], the largest off-diagonal
+// ratio (float bits) at ratio[b].
 template <typename T, int NT, int R, bool EXACT>
-__global__ void __launch_bounds__(NT)
-    k_jacobi_step_reg(int64_t m, int64_t n, int N, int r, cx<T>* W, int64_t sW, cx<T>* V, int64_t sV, T* nrm,
-                      const int* active, int* rotated, T tol, const unsigned char* __restrict__ tail) {
-  const int64_t b = blockIdx.y;
-  if (!active[b]) return;
-  int i, j;
-  rr_pair(N, r, blockIdx.x, i, j);
-  if (j >= n) return;
+__device__ __forceinline__ void jacobi_pair(int64_t m, int64_t n, int64_t b, int i, int j, cx<T>* W, int64_t sW,
+                                            cx<T>* V, int64_t sV, T* nrm, int64_t nmat, int* cnt, int* ratio, T tol,
+                                            const unsigned char* __restrict__ tail) {
   // both columns ranked below the kept set: their mutual orthogonality is never used
   if (tail && tail[b * n + i] && tail[b * n + j]) return;
   cx<T>* wi = W + b * sW + (int64_t)i * m;
@@ -212,7 +213,7 @@ __global__ void __launch_bounds__(NT)
       be = nrm[b * n + j];
     }
     // ‖A‖²_F of this matrix, stored after the n·batch column norms by k_fro
-    const T negl = jacobi_eps<T>() * jacobi_eps<T>() * nrm[(int64_t)n * gridDim.y + b];
+    const T negl = jacobi_eps<T>() * jacobi_eps<T>() * nrm[n * nmat + b];
     RotC<T> Rt = make_rot_c(al, be, g, tol, negl);
     float monitor = Rt.ratio;
     if (tail && (tail[b * n + i] != tail[b * n + j]) && al > T(0) && be > T(0)) {
@@ -224,11 +225,11 @@ __global__ void __launch_bounds__(NT)
     }
     if (al > T(0) && be > T(0)) {
       // largest off-diagonal ratio of the sweep (positive floats order like their bits)
-      atomicMax(&rotated[gridDim.y + b], __float_as_int(monitor));
+      atomicMax(&ratio[b], __float_as_int(monitor));
     }
     s_apply = Rt.apply;
     if (Rt.apply) {
-      atomicAdd(&rotated[b], 1);
+      atomicAdd(&cnt[b], 1);
       nrm[b * n + i] = al - Rt.tag;
       nrm[b * n + j] = be + Rt.tag;
       s_rot[0] = Rt.c;
@@ -258,6 +259,110 @@ __global__ void __launch_bounds__(NT)
       vi[t] = a;
       vj[t] = e;
     }
+  }
+}
+
+template <typename T, int NT, int R, bool EXACT>
+__global__ void __launch_bounds__(NT)
+    k_jacobi_step_reg(int64_t m, int64_t n, int N, int r, cx<T>* W, int64_t sW, cx<T>* V, int64_t sV, T* nrm,
+                      const int* active, int* rotated, T tol, const unsigned char* __restrict__ tail) {
+  const int64_t b = blockIdx.y;
+  if (!active[b]) return;
+  int i, j;
+  rr_pair(N, r, blockIdx.x, i, j);
+  if (j >= n) return;
+  jacobi_pair<T, NT, R, EXACT>(m, n, b, i, j, W, sW, V, sV, nrm, gridDim.y, rotated, rotated + gridDim.y, tol, tail);
+}
+
+// Persistent one-sided Jacobi for small matrices, where a round is far too little work to
+// hide a launch: one cooperative launch runs every sweep of every matrix.  Rounds are
+// separated by grid-wide barriers (all CTAs co-resident by construction of the cooperative
+// launch); the exact column norms, ‖W‖²_F and the convergence test of each sweep are done
+// on the device, so there is no host round trip until the end.  Every loop is bounded by
+// max_sweeps.  ctl (ints, zeroed by the caller): [0, 2B) and [2B, 4B) the rotation
+// counters / largest ratios of even and odd sweeps; [4B] any matrix still active; [4B+1]
+// sweeps run; [4B+2 …] worst ratio (float bits) and its rotation count per sweep (≤ 64).
+constexpr int kCoopDiag = 64;
+template <typename T, int NT, int R>
+__global__ void __launch_bounds__(NT)
+    k_jacobi_coop(int64_t m, int64_t n, int N, cx<T>* W, cx<T>* V, T* nrm, int* active, int* ctl, int64_t batch, T tol,
+                  int max_sweeps, float stop_ratio) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ T red[NT / 32];
+  const int64_t G = gridDim.x, g = blockIdx.x;
+  const int64_t pairs = N / 2, items = pairs * batch;
+  const int64_t sW = m * n, sV = n * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int* any = ctl + 4 * batch;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    int* cnt = ctl + (sweep & 1) * 2 * batch;
+    int* rat = cnt + batch;
+    // exact column norms, one warp per column (as k_col_norms)
+    for (int64_t col = g * (NT / 32) + warp; col < n * batch; col += G * (NT / 32)) {
+      const int64_t b = col / n, c = col % n;
+      if (!active[b]) continue;
+      const cx<T>* w = W + b * sW + c * m;
+      T sq = 0;
+      for (int64_t t = lane; t < m; t += 32) sq += abs2(w[t]);
+      sq = warp_sum(sq);
+      if (lane == 0) nrm[col] = sq;
+    }
+    grid.sync();
+    // ‖W_b‖²_F, one CTA per matrix
+    for (int64_t b = g; b < batch; b += G) {
+      if (!active[b]) continue;
+      T f = 0;
+      for (int64_t c = threadIdx.x; c < n; c += NT) f += nrm[b * n + c];
+      f = warp_sum(f);
+      if (lane == 0) red[warp] = f;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        T a = 0;
+        for (int w = 0; w < NT / 32; ++w) a += red[w];
+        nrm[n * batch + b] = a;
+      }
+      __syncthreads();
+    }
+    grid.sync();
+    for (int r = 0; r < N - 1; ++r) {
+      for (int64_t it = g; it < items; it += G) {
+        const int64_t b = it / pairs;
+        if (!active[b]) continue;
+        int i, j;
+        rr_pair(N, r, (int)(it % pairs), i, j);
+        if (j >= n) continue;
+        jacobi_pair<T, NT, R, false>(m, n, b, i, j, W, sW, V, sV, nrm, batch, cnt, rat, tol, nullptr);
+        __syncthreads();
+      }
+      // the other parity's counters were last read before this sweep began
+      if (r == 0 && g == 0)
+        for (int64_t t = threadIdx.x; t < 2 * batch; t += NT) ctl[((sweep + 1) & 1) * 2 * batch + t] = 0;
+      grid.sync();
+    }
+    if (g == 0 && threadIdx.x == 0) {
+      int n_act = 0, worst_rot = 0;
+      float worst = 0.f;
+      for (int64_t b = 0; b < batch; ++b) {
+        if (!active[b]) continue;
+        const float rt = __int_as_float(rat[b]);
+        if (rt > worst) {
+          worst = rt;
+          worst_rot = cnt[b];
+        }
+        const int a = cnt[b] > 0 && rt > stop_ratio;
+        active[b] = a;
+        n_act += a;
+      }
+      *any = n_act;
+      ctl[4 * batch + 1] = sweep + 1;
+      if (sweep < kCoopDiag) {
+        ctl[4 * batch + 2 + sweep] = __float_as_int(worst);
+        ctl[4 * batch + 2 + kCoopDiag + sweep] = worst_rot;
+      }
+    }
+    grid.sync();
+    if (*any == 0) break;
   }
 }
 
@@ -572,6 +677,45 @@ static tn_status_t launch_step(tn_ctx* ctx, int64_t m, int64_t n, int N, int r, 
   return TN_OK;
 }
 
+// matrices with at most this many columns take the persistent cooperative path
+constexpr int64_t kCoopMaxN = 256;
+
+// the whole Jacobi iteration of a small FP64 batch in one cooperative launch
+template <typename T>
+static tn_status_t jacobi_coop(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T>* V, int64_t batch, int* active,
+                               T* nrm, int max_sweeps, int* sweeps_out, bool* noconv_out) {
+  constexpr int NT = 128, R = 4;  // m ≤ 512
+  const int N = (int)(n + (n & 1));
+  const int64_t items = (int64_t)(N / 2) * batch;
+  int per_sm = 0;
+  TN_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_coop<T, NT, R>, NT, 0));
+  const int64_t G = std::min<int64_t>(items, (int64_t)std::max(per_sm, 1) * ctx->num_sms);
+  const size_t nctl = (size_t)(4 * batch + 2 + 2 * kCoopDiag);
+  int* ctl = nullptr;
+  TN_RETURN_IF(ctx_flags(ctx, nctl, &ctl));
+  TN_CHECK_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(int) * nctl, ctx->stream));
+  std::vector<int> h_act(batch, 1);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
+  const T tol = jacobi_tol<T>(m);
+  const float stop_ratio = (float)sqrt((double)tol * 1e-1);
+  int64_t bt = batch;
+  void* args[] = {&m, &n, (void*)&N, &W, &V, &nrm, &active, &ctl, &bt, (void*)&tol, &max_sweeps, (void*)&stop_ratio};
+  TN_CHECK_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_jacobi_coop<T, NT, R>, dim3((unsigned)G), dim3(NT), args,
+                                                 0, ctx->stream));
+  TN_LAUNCHED(ctx);
+  std::vector<int> h(nctl);
+  TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h.data(), ctl, sizeof(int) * nctl, cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const int sweeps = h[4 * batch + 1];
+  for (int k = 0; k < kCoopDiag && k < 64; ++k) {
+    memcpy(&ctx->sweep_ratio[k], &h[4 * batch + 2 + k], sizeof(float));
+    ctx->sweep_rotations[k] = h[4 * batch + 2 + kCoopDiag + k];
+  }
+  *sweeps_out = sweeps;
+  *noconv_out = h[4 * batch] > 0;
+  return TN_OK;
+}
+
 // sweeps of one phase after which the truncation-aware flags are dropped
 constexpr int kTailSweeps = 8;
 
@@ -613,6 +757,13 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
     TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (int64_t b = 0; b < batch; ++b) noconv |= st[b] != 0;
     sweeps = -1;
+  } else if (sizeof(T) == 8 && !tail && min_rot_frac <= 0.0 && m <= 512 && n <= kCoopMaxN) {
+    if (V && !v_given) {
+      int64_t blocks = std::min<int64_t>((n * n + 255) / 256, 2048);
+      k_identity<T><<<dim3((unsigned)blocks, gy), 256, 0, ctx->stream>>>(n, V, n * n, batch);
+      TN_LAUNCHED(ctx);
+    }
+    TN_RETURN_IF(jacobi_coop<T>(ctx, m, n, W, V, batch, active, nrm, max_sweeps, &sweeps, &noconv));
   } else {
     if (V && !v_given) {
       int64_t blocks = std::min<int64_t>((n * n + 255) / 256, 2048);

@@ -20,6 +20,7 @@ from .core import (
     tensor_svd_thin,
 )
 from .dmrg import Dmrg1, Dmrg2, dmrg, dmrg_, ising_1d_mpo
+from .dmrg import last_stats as dmrg_last_stats
 from .mps import (
     MPS,
     BondCanonical,

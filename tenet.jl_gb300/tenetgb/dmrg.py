@@ -98,3 +98,16 @@ def dmrg_(psi, H, nsweeps=4, *, method=Dmrg1, maxdim=128, ishermitian=True, kryl
 def dmrg(psi, H, nsweeps=4, **kw):
     """dmrg(ψ, H, …) = dmrg!(copy(ψ), H, …) (DMRG.jl:41)."""
     return dmrg_(psi.copy(), H, nsweeps, **kw)
+
+
+def last_stats(ctx=None):
+    """Device time (ms) of the last DMRG run per phase — gauge moves, environments,
+    eigensolves, pair splits — and the number of local updates (tn_dmrg_last_stats)."""
+    from .core import default_context
+
+    ctx = ctx or default_context()
+    ms = np.zeros(4, dtype=np.float64)
+    n = (C.c_int64 * 2)()
+    ctx.check(ctx.lib.tn_dmrg_last_stats(ctx.h, ms.ctypes.data_as(L._pdbl), n))
+    return {"canonize_ms": ms[0], "environments_ms": ms[1], "eigsolve_ms": ms[2], "split_ms": ms[3],
+            "updates": n[0], "svd_sweeps": n[1]}
