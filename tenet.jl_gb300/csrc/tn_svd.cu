@@ -1117,7 +1117,12 @@ tn_status_t svd_left(tn_ctx* ctx, tn_precision_t prec, int64_t m, int64_t n, con
     TN_LAUNCHED(ctx);
   }
   // the one-CTA shared-memory kernel needs V resident; the large path runs without it
-  const bool small = sizeof(cxd) * (size_t)(m * n + n * n) <= kSmemMax && n <= 256;
+  // small matrices: one CTA per matrix in shared memory when there are many of them; a
+  // few (a DMRG or TEBD pair, one MPS) take the persistent cooperative sweeps instead,
+  // which spread each round's pairs over many SMs (one SM's FP64 rate serialises a whole
+  // SVD; no right vectors are needed here)
+  const bool coop = m <= 512 && n <= kCoopMaxN;
+  const bool small = sizeof(cxd) * (size_t)(m * n + n * n) <= kSmemMax && n <= 256 && !(coop && batch < 32);
   bool noconv = false;
   ctx->last_sweeps_fp32 = 0;
   TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W, small ? V : nullptr, batch, false, active, rotated, nrm, kMaxSweeps,
