@@ -249,6 +249,35 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def fp64_peak(ctx, stream, dev):
+    """The FP64 pipe rate (TFLOP/s) measured with the library's own complex FP64 GEMM at
+    2048³ (MEASURED_PEAKS.json carries no FP64 rate)."""
+    import ctypes as C
+
+    import torch
+
+    import tenetgb
+
+    rng = np.random.default_rng(1)
+    N = 2048
+    X = tenetgb.DeviceTensor.from_numpy(ctx, rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N)))
+    Y = tenetgb.DeviceTensor(ctx, (N, N), np.complex128)
+    one, zero = (C.c_double * 2)(1, 0), (C.c_double * 2)(0, 0)
+
+    def g():
+        ctx.check(ctx.lib.tn_gemm(ctx.h, 3, 0, b"N", b"N", N, N, N, one, C.c_void_p(X.ptr), N, 0, C.c_void_p(X.ptr), N,
+                                  0, zero, C.c_void_p(Y.ptr), N, 0, 1))
+
+    g()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    g()
+    e1.record(stream)
+    e1.synchronize()
+    return 8 * N**3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+
+
 def roofline_entry(ctx, stream, dev):
     """Dominant kernel: the FP64 Jacobi rotation step (k_jacobi_step_reg) on the 512×512
     θ of a saturated gate.  Algorithmic flops per launch = 256 pairs × (8m for wᵢᴴwⱼ +
@@ -279,23 +308,7 @@ def roofline_entry(ctx, stream, dev):
     per_launch_ms = svd_ms / steps
     flops = (n // 2) * (8 * m + 24 * m + 24 * n)
     achieved = flops / (per_launch_ms * 1e-3) / 1e12
-    # FP64 pipe: zgemm 2048^3
-    N = 2048
-    X = tenetgb.DeviceTensor.from_numpy(ctx, rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N)))
-    Y = tenetgb.DeviceTensor(ctx, (N, N), np.complex128)
-    one, zero = (C.c_double * 2)(1, 0), (C.c_double * 2)(0, 0)
-
-    def g():
-        ctx.check(ctx.lib.tn_gemm(ctx.h, 3, 0, b"N", b"N", N, N, N, one, C.c_void_p(X.ptr), N, 0, C.c_void_p(X.ptr), N,
-                                  0, zero, C.c_void_p(Y.ptr), N, 0, 1))
-
-    g()
-    torch.cuda.synchronize(dev)
-    e0.record(stream)
-    g()
-    e1.record(stream)
-    e1.synchronize()
-    peak = 8 * N**3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+    peak = fp64_peak(ctx, stream, dev)
     # DRAM bytes of one launch of this kernel in this configuration, from one ncu capture
     # (bench.py --profile-svd; cold cache, so W and V are read once: 8.43 MB), per launch
     traffic = 8.428032e6
@@ -817,6 +830,45 @@ def run_dmrg(args):
                 times.append(e0.elapsed_time(e1))
     launches = ctx.launches() - launches0
     ms = float(np.mean(times))
+    stats = tenetgb.dmrg_last_stats(ctx)
+    # dominant kernel: the pair SVD (k_jacobi_coop, one launch per 256×256 split).
+    # Algorithmic flops per launch = sweeps × 255 rounds × 128 pairs × (8m + 24m), m = 256
+    # (no right vectors), the sweeps averaged over the call's splits; time per launch =
+    # the splits' device time (CUDA events) ÷ the local updates
+    sweeps_per_split = stats["svd_sweeps"] / max(1, stats["updates"])
+    flops = sweeps_per_split * 255 * 128 * 32 * 256
+    split_ms = stats["split_ms"] / max(1, stats["updates"])
+    peak = fp64_peak(ctx, stream, torch.device("cuda", 0))
+    achieved = flops / (split_ms * 1e-3) / 1e12
+    roofline = {"bound": "tensor", "kernel": "k_jacobi_coop<double> (FP64 pipe; latency-bound rounds)",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                "peak_source": "FP64 pipe measured in this run (own zgemm 2048^3); MEASURED_PEAKS.json has no FP64 entry",
+                "flops_per_launch": flops, "sweeps_per_split": sweeps_per_split, "launch_avg_ms": split_ms,
+                "phases_ms_per_step": {k: stats[k] for k in ("canonize_ms", "environments_ms", "eigsolve_ms",
+                                                             "split_ms")}}
+    # 16 Hamiltonians (h ∈ [0.5, 1.5]) on a batched MPS in lockstep: five untimed calls
+    # from the product state, then one timed call
+    scan = None
+    if args.dmrg_batch > 1:
+        fields = np.linspace(0.5, 1.5, args.dmrg_batch)
+        q = tenetgb.MPS.batched([[s.copy() for s in prod] for _ in fields], ctx=ctx)
+        Hs = [tenetgb.ising_1d_mpo(n, h, 1.0) for h in fields]
+        for _ in range(5):
+            tenetgb.dmrg_(q, Hs, 1, method=tenetgb.Dmrg2, maxdim=chi)
+        with torch.cuda.stream(stream):
+            flush_l2(torch, flush)
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        _, Es = tenetgb.dmrg_(q, Hs, 1, method=tenetgb.Dmrg2, maxdim=chi)
+        e1.record(stream)
+        e1.synchronize()
+        sms = e0.elapsed_time(e1)
+        scan = {"instances": int(args.dmrg_batch), "fields": [float(fields[0]), float(fields[-1])],
+                "value": args.dmrg_batch * 1e3 / sms, "unit": "instance-sweeps/s", "ms_per_step": sms,
+                "per_instance_vs_single": (args.dmrg_batch * 1e3 / sms) / (1e3 / ms),
+                "energies_per_site": [float(e) / n for e in Es]}
+        del q
     # end to end: the MPS from pinned host buffers, one call, the MPS and energy back
     host_sites = [psi.site(i) for i in range(1, n + 1)]
     pinned = [torch.from_numpy(np.asfortranarray(s).reshape(-1, order="F").view(np.float64)).pin_memory()
@@ -852,7 +904,8 @@ def run_dmrg(args):
         "energy_abs_diff": abs(energies[9] - known), "energies": energies,
         "e2e": {"value": 1.0 / float(np.mean(e2e_times)), "unit": "sweeps/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": int(launches / max(1, args.steps)), "clocks": clk.summary(),
+        "gpu_launches": int(launches / max(1, args.steps)), "clocks": clk.summary(), "roofline": roofline,
+        "batched_scan": scan,
         "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": "oracle (numpy/LAPACK) on the same saturated MPS: environments + 40 of the 198 "
                                    "local updates of one dmrg!(ψ, H, 1) call, scaled to the call"},
@@ -871,6 +924,7 @@ def main():
     ap.add_argument("--profile-dmrg", action="store_true", help="one saturated 2-site DMRG sweep (launch list)")
     ap.add_argument("--precision", default="native", choices=["native", "mixed"])
     ap.add_argument("--batch", type=int, default=16, help="MPS instances advanced in lockstep")
+    ap.add_argument("--dmrg-batch", type=int, default=16, help="Hamiltonians of the batched DMRG scan (dmrg)")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
