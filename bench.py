@@ -283,8 +283,6 @@ def roofline_entry(ctx, stream, dev):
     θ of a saturated gate.  Algorithmic flops per launch = 256 pairs × (8m for wᵢᴴwⱼ +
     24m for the two rotated columns of W + 24n for V).  Peak: the FP64 pipe measured here
     with the library's own FP64 complex GEMM (MEASURED_PEAKS.json carries no FP64 rate)."""
-    import ctypes as C
-
     import torch
 
     import tenetgb

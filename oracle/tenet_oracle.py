@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY.  Nothing in the product (the CUDA library and its host
 mirror) imports this module; only ``tests/``, ``__graft_entry__.smoke()`` and the CPU
-legs of ``bench.py`` use it, as the checker and as the timed CPU baseline.
+legs of ``bench.py`` use it, as the parity reference and as the timed CPU baseline.
 
 What it restates (Tenet.jl v0.10.3, file:line relative to the project root):
 
@@ -663,6 +663,26 @@ def ising_1d_mpo(L, h, J):
     first = W[2:3].copy()  # W_1 = W[:, :, 3, :]
     last = W[:, :, :, 0:1].copy()  # W_n = W[:, :, :, 1]
     return [first] + [W.copy() for _ in range(L - 2)] + [last]
+
+
+def heisenberg_mpo(L, J, Jz, h):
+    """XXZ chain H = Σ J(S⁺S⁻ + S⁻S⁺)/2 + Jz SᶻSᶻ + h Σ Sᶻ as a bond-5 MPO in the layout of
+    ising_1d_mpo (w_l, d_out, d_in, w_r): start state 4, end state 0.  Not a reference
+    model: a second Hamiltonian (MPO bond 5) for the DMRG parity tests."""
+    sp = np.array([[0.0, 1.0], [0.0, 0.0]])
+    sm = sp.T.copy()
+    sz = np.diag([0.5, -0.5])
+    W = np.zeros((5, 2, 2, 5), dtype=np.complex128)
+    W[0, :, :, 0] = np.eye(2)
+    W[1, :, :, 0] = sp
+    W[2, :, :, 0] = sm
+    W[3, :, :, 0] = sz
+    W[4, :, :, 0] = h * sz
+    W[4, :, :, 1] = 0.5 * J * sm
+    W[4, :, :, 2] = 0.5 * J * sp
+    W[4, :, :, 3] = Jz * sz
+    W[4, :, :, 4] = np.eye(2)
+    return [W[4:5].copy()] + [W.copy() for _ in range(L - 2)] + [W[:, :, :, 0:1].copy()]
 
 
 def mpo_dense(mpo):

@@ -181,3 +181,27 @@ def test_dmrg_ordered_phase_spectrum_below_fp64_range():
         A = psi.site(i)
         m = A.reshape(A.shape[0], -1, order="F")
         assert np.linalg.norm(m @ m.conj().T - np.eye(A.shape[0])) < 1e-10, i
+
+
+@pytest.mark.parametrize("method", [1, 2])
+def test_dmrg_heisenberg_bond5_matches_oracle(method):
+    """XXZ chain with a field (MPO bond 5: the fibre contractions take 10 inputs per
+    output) from a Néel state (Dmrg2) or a random bond-4 MPS (Dmrg1)."""
+    import tenetgb
+
+    n = 8
+    H = O.heisenberg_mpo(n, 1.0, 0.7, 0.2)
+    if method == 2:
+        sites = [np.array([1.0, 0.0] if i % 2 else [0.0, 1.0], dtype=np.complex128).reshape(1, 2, 1) for i in range(n)]
+    else:
+        sites = rand_sites(np.random.default_rng(63), [1, 2, 4, 4, 4, 4, 4, 2, 1])
+    psi = tenetgb.MPS([s.copy() for s in sites])
+    meth = tenetgb.Dmrg1 if method == 1 else tenetgb.Dmrg2
+    _, E, hist = tenetgb.dmrg_(psi, H, 4, method=meth, maxdim=16, history=True)
+    ref_hist = []
+    _, Er = O.dmrg(O.OMPS([s.copy() for s in sites]), H, 4, method="dmrg1" if method == 1 else "dmrg2", maxdim=16,
+                   history=ref_hist)
+    assert np.allclose(hist, ref_hist, rtol=0, atol=1e-9)
+    if method == 2:  # full bond: the extreme eigenvalue of H (which = :LM)
+        w = np.linalg.eigvalsh(O.mpo_dense(H))
+        assert abs(E - w[np.argmax(np.abs(w))]) < 1e-9

@@ -350,3 +350,27 @@ def test_lanczos_lm_exact_on_small_space():
     w = np.linalg.eigvalsh(M)
     assert abs(theta - w[np.argmax(abs(w))]) < 1e-12
     assert np.linalg.norm(M @ x - theta * x) < 1e-10
+
+
+def test_heisenberg_mpo_matches_dense_hamiltonian():
+    n, J, Jz, h = 5, 1.0, 0.7, 0.2
+    H = O.mpo_dense(O.heisenberg_mpo(n, J, Jz, h))
+    sp = np.array([[0.0, 1.0], [0.0, 0.0]])
+    sm = sp.T.copy()
+    sz = np.diag([0.5, -0.5])
+
+    def op(site_ops):
+        m = np.eye(1)
+        for i in range(n):
+            m = np.kron(m, site_ops.get(i, np.eye(2)))
+        return m
+
+    ref = sum(0.5 * J * (op({i: sp, i + 1: sm}) + op({i: sm, i + 1: sp})) + Jz * op({i: sz, i + 1: sz})
+              for i in range(n - 1)) + sum(h * op({i: sz}) for i in range(n))
+    assert np.allclose(H, ref, atol=1e-14)
+    # and the oracle's DMRG reaches its ground state with a full bond
+    psi0 = O.OMPS([np.array([1.0, 0.0] if i % 2 else [0.0, 1.0], dtype=np.complex128).reshape(1, 2, 1)
+                   for i in range(n)])
+    _, E = O.dmrg(psi0, O.heisenberg_mpo(n, J, Jz, h), 6, method="dmrg2", maxdim=8)
+    w = np.linalg.eigvalsh(H)
+    assert abs(E - w[np.argmax(np.abs(w))]) < 1e-9
