@@ -112,6 +112,26 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def max_over_ranks(values, ws):
+    """Each timing's maximum over the ranks (an all-reduce over the process group: gloo
+    under torchrun here, the timings being host floats); the values themselves for one
+    rank."""
+    if ws <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor(list(values), dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_throughput(ws, instances, steps, seconds):
+    """Whole-job throughput of ws replicas, each advancing `instances` MPS by `steps`
+    layers in `seconds` (the slowest rank's time)."""
+    return ws * instances * steps / seconds
+
+
 def layers_for(n):
     from tenetgb import workloads as W
 
@@ -207,13 +227,9 @@ def run_ours(args):
             d2h = sum(s.nbytes for st in new_states for s in st)
         states = new_states
     # max over ranks
-    tm, tf, te = sum(t_mixed), sum(t_fp64), sum(t_e2e)
-    if ws > 1:
-        t = torch.tensor([tm, tf, te], dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tm, tf, te = t.tolist()
+    tm, tf, te = max_over_ranks([sum(t_mixed), sum(t_fp64), sum(t_e2e)], ws)
     K = args.steps
-    value = ws * Bt * K / tm
+    value = replica_throughput(ws, Bt, K, tm)
     out = {
         "metric": METRIC,
         "value": value,
@@ -229,7 +245,7 @@ def run_ours(args):
         "data": "synthetic (seeded Gaussian MPS, Haar gates)",
         "config": dict(CONFIG, parallelism=f"replicas{ws}", batch_instances=Bt,
                        l2="flushed between steps (256 MB write)"),
-        "fp64": {"value": ws * K / tf, "unit": UNIT, "ms_per_step": 1e3 * tf / K, "instances": 1,
+        "fp64": {"value": replica_throughput(ws, 1, K, tf), "unit": UNIT, "ms_per_step": 1e3 * tf / K, "instances": 1,
                  "speedup_of_value": (Bt * tf) / tm},
         "accuracy_mixed_vs_fp64": {
             "overlap_rel_err": abs(ov_m - ov_f) / abs(ov_f),
@@ -237,7 +253,7 @@ def run_ours(args):
             "z_max_abs_err": float(np.abs(z_m - z_f).max()),
             "layers_compared": len(run_layers),
         },
-        "e2e": {"value": ws * Bt * K / te, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": replica_throughput(ws, Bt, K, te), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(round(launches_per_step * K)),
         "clocks": clk.summary(),
     }
