@@ -134,6 +134,52 @@ __device__ __forceinline__ RotC<T> make_rot_c(T alpha, T beta, cx<T> g, T tol, T
   return R;
 }
 
+// The rotation for the latency-bound small-matrix kernels: the same angle as make_rot_c
+// from fewer long-latency operations on the one thread that forms it (1/|γ| once, no
+// monitor ratio: another thread derives that off the critical path).
+template <typename T>
+__device__ __forceinline__ RotC<T> make_rot_lean(T alpha, T beta, cx<T> g, T tol, T negl) {
+  RotC<T> R;
+  R.c = T(1);
+  R.tag = T(0);
+  R.se = mkcx<T>(0, 0);
+  R.apply = 0;
+  R.ratio = 0.f;
+  const T fl = negl > JacobiFloor<T>::value ? negl : JacobiFloor<T>::value;
+  if (!(alpha > fl) || !(beta > fl)) return R;
+  T ag;
+  const T ab = alpha * beta;
+  if (ab > JacobiFloor<T>::value) {
+    const T ag2 = abs2(g);
+    if (!(ag2 > tol * tol * ab && ag2 > T(0))) return R;
+    ag = sqrt(ag2);
+  } else {
+    ag = hypot(g.x, g.y);
+    if (!(ag > tol * (sqrt(alpha) * sqrt(beta)) && ag > T(0))) return R;
+  }
+  const T inv_ag = T(1) / ag;
+  const T zeta = (beta - alpha) * (T(0.5) * inv_ag);
+  const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+  if (t == T(0)) return R;
+  const T c = T(1) / sqrt(T(1) + t * t);
+  const T sn = c * t * inv_ag;
+  R.apply = 1;
+  R.c = c;
+  R.tag = t * ag;
+  R.se = mkcx<T>(sn * g.x, sn * g.y);
+  return R;
+}
+
+// the convergence monitor of a pair, as make_rot_c computes it
+template <typename T>
+__device__ __forceinline__ float rot_ratio(T alpha, T beta, cx<T> g, T negl) {
+  const T fl = negl > JacobiFloor<T>::value ? negl : JacobiFloor<T>::value;
+  if (!(alpha > fl) || !(beta > fl)) return 0.f;
+  const T ab = alpha * beta;
+  if (ab > JacobiFloor<T>::value) return sqrtf((float)(abs2(g) / ab));
+  return (float)(hypot(g.x, g.y) / (sqrt(alpha) * sqrt(beta)));
+}
+
 template <typename T>
 __device__ __forceinline__ void rot_apply_c(T c, cx<T> se, cx<T>& wi, cx<T>& wj) {
   // wi' = c wi − conj(se) wj ; wj' = se wi + c wj
@@ -153,12 +199,23 @@ __device__ __forceinline__ void rot_apply_c(T c, cx<T> se, cx<T>& wi, cx<T>& wj)
 // and the persistent cooperative one).  nmat: matrices in the batch (‖W_b‖²_F sits at
 // nrm[n·nmat + b]); counters: rotations of matrix b at cnt[b], the largest off-diagonal
 // ratio (float bits) at ratio[b].
-template <typename T, int NT, int R, bool EXACT>
+// LAT (cached norms, no truncation flags): the latency-bound form for the dataflow
+// kernel — the cached norms and ‖A‖²_F are fetched with the columns, thread 0 forms only
+// the rotation (make_rot_lean), and thread 32 updates the norms and counters.
+template <typename T, int NT, int R, bool EXACT, bool LAT = false>
 __device__ __forceinline__ void jacobi_pair(int64_t m, int64_t n, int64_t b, int i, int j, cx<T>* W, int64_t sW,
                                             cx<T>* V, int64_t sV, T* nrm, int64_t nmat, int* cnt, int* ratio, T tol,
                                             const unsigned char* __restrict__ tail) {
+  static_assert(!(LAT && EXACT), "the latency form uses cached norms");
+  static_assert(!LAT || NT > 32, "the latency form needs a second warp");
   // both columns ranked below the kept set: their mutual orthogonality is never used
-  if (tail && tail[b * n + i] && tail[b * n + j]) return;
+  if (!LAT && tail && tail[b * n + i] && tail[b * n + j]) return;
+  T pre_al = 0, pre_be = 0, pre_f = 0;
+  if (LAT && threadIdx.x == 0) {
+    pre_al = nrm[b * n + i];
+    pre_be = nrm[b * n + j];
+    pre_f = nrm[n * nmat + b];
+  }
   cx<T>* wi = W + b * sW + (int64_t)i * m;
   cx<T>* wj = W + b * sW + (int64_t)j * m;
   constexpr int NW = NT / 32;
@@ -197,7 +254,42 @@ __device__ __forceinline__ void jacobi_pair(int64_t m, int64_t n, int64_t b, int
   // part) and hands (c, s·e^{iφ}) to the block through shared memory
   __shared__ T s_rot[3];
   __shared__ int s_apply;
-  if (threadIdx.x == 0) {
+  if (LAT) {
+    __shared__ T s_mon[6];
+    if (threadIdx.x == 0) {
+      g = mkcx<T>(0, 0);
+#pragma unroll
+      for (int w = 0; w < NW; ++w) {
+        g.x += red[w][0];
+        g.y += red[w][1];
+      }
+      const T negl = jacobi_eps<T>() * jacobi_eps<T>() * pre_f;
+      const RotC<T> Rt = make_rot_lean(pre_al, pre_be, g, tol, negl);
+      s_apply = Rt.apply;
+      s_rot[0] = Rt.c;
+      s_rot[1] = Rt.se.x;
+      s_rot[2] = Rt.se.y;
+      s_mon[0] = pre_al;
+      s_mon[1] = pre_be;
+      s_mon[2] = g.x;
+      s_mon[3] = g.y;
+      s_mon[4] = negl;
+      s_mon[5] = Rt.tag;
+    }
+    __syncthreads();
+    const int apply = s_apply;
+    if (threadIdx.x == 32) {
+      const T al2 = s_mon[0], be2 = s_mon[1];
+      if (al2 > T(0) && be2 > T(0))
+        atomicMax(&ratio[b], __float_as_int(rot_ratio(al2, be2, mkcx<T>(s_mon[2], s_mon[3]), s_mon[4])));
+      if (apply) {
+        atomicAdd(&cnt[b], 1);
+        nrm[b * n + i] = al2 - s_mon[5];
+        nrm[b * n + j] = be2 + s_mon[5];
+      }
+    }
+    if (!apply) return;
+  } else if (threadIdx.x == 0) {
     g = mkcx<T>(0, 0);
     al = 0;
     be = 0;
@@ -237,8 +329,10 @@ __device__ __forceinline__ void jacobi_pair(int64_t m, int64_t n, int64_t b, int
       s_rot[2] = Rt.se.y;
     }
   }
-  __syncthreads();
-  if (!s_apply) return;
+  if (!LAT) {
+    __syncthreads();
+    if (!s_apply) return;
+  }
   const T c = s_rot[0];
   const cx<T> se = mkcx<T>(s_rot[1], s_rot[2]);
 #pragma unroll
@@ -352,6 +446,132 @@ __global__ void __launch_bounds__(NT)
         }
         const int a = cnt[b] > 0 && rt > stop_ratio;
         active[b] = a;
+        n_act += a;
+      }
+      *any = n_act;
+      ctl[4 * batch + 1] = sweep + 1;
+      if (sweep < kCoopDiag) {
+        ctl[4 * batch + 2 + sweep] = __float_as_int(worst);
+        ctl[4 * batch + 2 + kCoopDiag + sweep] = worst_rot;
+      }
+    }
+    grid.sync();
+    if (*any == 0) break;
+  }
+}
+
+// The same iteration with the per-round grid barrier replaced by dataflow: in the circle
+// ordering a column held by slot k in round r was held in round r−1 by the slot
+// rr_holder(N, r−1, column), so a CTA (one per pair slot and matrix) waits only for the
+// two CTAs that last wrote its columns.  Each CTA publishes the round it finished
+// (release at GPU scope after its writes) and polls its two predecessors (acquire);
+// grid barriers remain only at sweep boundaries (norm refresh, stop test).  A poll that
+// exceeds kFlowSpinLimit iterations sets the error word and moves on, so every CTA still
+// reaches every barrier and the launch ends; the host reports the error.
+constexpr long long kFlowSpinLimit = 1ll << 24;
+
+__device__ __forceinline__ int rr_holder(int N, int r, int c) {
+  if (c == N - 1 || c == r % (N - 1)) return 0;
+  const int a = ((c - r) % (N - 1) + (N - 1)) % (N - 1);
+  if (a >= 1 && a <= N / 2 - 1) return a;
+  return ((r - c) % (N - 1) + (N - 1)) % (N - 1);
+}
+
+__device__ __forceinline__ int ld_acquire_gpu(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+template <typename T, int NT, int R>
+__global__ void __launch_bounds__(NT)
+    k_jacobi_flow(int64_t m, int64_t n, int N, cx<T>* W, cx<T>* V, T* nrm, int* active, int* ctl, int* done,
+                  int64_t batch, T tol, int max_sweeps, float stop_ratio) {
+  namespace cg = cooperative_groups;
+  cg::grid_group grid = cg::this_grid();
+  __shared__ T red[NT / 32];
+  const int64_t G = gridDim.x, g = blockIdx.x;
+  const int64_t pairs = N / 2;
+  const int64_t b = g / pairs;
+  const int k = (int)(g % pairs);
+  const int64_t sW = m * n, sV = n * n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int* any = ctl + 4 * batch;
+  int* err = ctl + 4 * batch + 2 + 2 * kCoopDiag;
+  int* done_b = done + b * pairs;
+  for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+    int* cnt = ctl + (sweep & 1) * 2 * batch;
+    int* rat = cnt + batch;
+    for (int64_t col = g * (NT / 32) + warp; col < n * batch; col += G * (NT / 32)) {
+      const int64_t bb = col / n, c = col % n;
+      if (!active[bb]) continue;
+      const cx<T>* w = W + bb * sW + c * m;
+      T sq = 0;
+      for (int64_t t = lane; t < m; t += 32) sq += abs2(w[t]);
+      sq = warp_sum(sq);
+      if (lane == 0) nrm[col] = sq;
+    }
+    grid.sync();
+    for (int64_t bb = g; bb < batch; bb += G) {
+      if (!active[bb]) continue;
+      T f = 0;
+      for (int64_t c = threadIdx.x; c < n; c += NT) f += nrm[bb * n + c];
+      f = warp_sum(f);
+      if (lane == 0) red[warp] = f;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        T a = 0;
+        for (int w = 0; w < NT / 32; ++w) a += red[w];
+        nrm[n * batch + bb] = a;
+      }
+      __syncthreads();
+    }
+    grid.sync();
+    if (g == 0)  // the other parity's counters were last read before this sweep began
+      for (int64_t t = threadIdx.x; t < 2 * batch; t += NT) ctl[((sweep + 1) & 1) * 2 * batch + t] = 0;
+    if (active[b]) {
+      for (int r = 0; r < N - 1; ++r) {
+        int i, j;
+        rr_pair(N, r, k, i, j);
+        if (r > 0) {
+          if (threadIdx.x == 0) {
+            const int want = sweep * N + r;  // published by a holder when it finished round r−1
+            const int h1 = rr_holder(N, r - 1, i), h2 = rr_holder(N, r - 1, j);
+            long long spins = 0;
+            while (ld_acquire_gpu(&done_b[h1]) < want || ld_acquire_gpu(&done_b[h2]) < want) {
+              if (++spins > kFlowSpinLimit) {
+                atomicExch(err, 1);
+                break;
+              }
+            }
+            __threadfence();
+          }
+          __syncthreads();
+        }
+        if (j < n) jacobi_pair<T, NT, R, false, true>(m, n, b, i, j, W, sW, V, sV, nrm, batch, cnt, rat, tol, nullptr);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) st_release_gpu(&done_b[k], sweep * N + r + 1);
+      }
+    }
+    grid.sync();
+    if (g == 0 && threadIdx.x == 0) {
+      int n_act = 0, worst_rot = 0;
+      float worst = 0.f;
+      const int failed = *err;
+      for (int64_t bb = 0; bb < batch; ++bb) {
+        if (!active[bb]) continue;
+        const float rt = __int_as_float(rat[bb]);
+        if (rt > worst) {
+          worst = rt;
+          worst_rot = cnt[bb];
+        }
+        const int a = !failed && cnt[bb] > 0 && rt > stop_ratio;
+        active[bb] = a;
         n_act += a;
       }
       *any = n_act;
@@ -689,8 +909,13 @@ static tn_status_t jacobi_coop(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
   const int64_t items = (int64_t)(N / 2) * batch;
   int per_sm = 0;
   TN_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_coop<T, NT, R>, NT, 0));
-  const int64_t G = std::min<int64_t>(items, (int64_t)std::max(per_sm, 1) * ctx->num_sms);
-  const size_t nctl = (size_t)(4 * batch + 2 + 2 * kCoopDiag);
+  int per_sm_flow = 0;
+  TN_CHECK_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_flow, k_jacobi_flow<T, NT, R>, NT, 0));
+  // dataflow rounds need one resident CTA per pair slot and matrix
+  const bool flow = items <= (int64_t)std::max(per_sm_flow, 0) * ctx->num_sms;
+  const int64_t G = flow ? items : std::min<int64_t>(items, (int64_t)std::max(per_sm, 1) * ctx->num_sms);
+  const size_t nhdr = (size_t)(4 * batch + 2 + 2 * kCoopDiag + 1);
+  const size_t nctl = nhdr + (flow ? (size_t)items : 0);
   int* ctl = nullptr;
   TN_RETURN_IF(ctx_flags(ctx, nctl, &ctl));
   TN_CHECK_CUDA(ctx, cudaMemsetAsync(ctl, 0, sizeof(int) * nctl, ctx->stream));
@@ -699,9 +924,17 @@ static tn_status_t jacobi_coop(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
   const T tol = jacobi_tol<T>(m);
   const float stop_ratio = (float)sqrt((double)tol * 1e-1);
   int64_t bt = batch;
-  void* args[] = {&m, &n, (void*)&N, &W, &V, &nrm, &active, &ctl, &bt, (void*)&tol, &max_sweeps, (void*)&stop_ratio};
-  TN_CHECK_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_jacobi_coop<T, NT, R>, dim3((unsigned)G), dim3(NT), args,
-                                                 0, ctx->stream));
+  if (flow) {
+    int* done = ctl + nhdr;
+    void* args[] = {&m, &n, (void*)&N, &W, &V, &nrm, &active, &ctl, &done, &bt, (void*)&tol, &max_sweeps,
+                    (void*)&stop_ratio};
+    TN_CHECK_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_jacobi_flow<T, NT, R>, dim3((unsigned)G), dim3(NT),
+                                                   args, 0, ctx->stream));
+  } else {
+    void* args[] = {&m, &n, (void*)&N, &W, &V, &nrm, &active, &ctl, &bt, (void*)&tol, &max_sweeps, (void*)&stop_ratio};
+    TN_CHECK_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_jacobi_coop<T, NT, R>, dim3((unsigned)G), dim3(NT),
+                                                   args, 0, ctx->stream));
+  }
   TN_LAUNCHED(ctx);
   std::vector<int> h(nctl);
   TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h.data(), ctl, sizeof(int) * nctl, cudaMemcpyDeviceToHost, ctx->stream));
@@ -713,6 +946,8 @@ static tn_status_t jacobi_coop(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
   }
   *sweeps_out = sweeps;
   *noconv_out = h[4 * batch] > 0;
+  if (h[4 * batch + 2 + 2 * kCoopDiag])
+    return tn_set_error(ctx, TN_ECUDA, "svd: a dataflow wait of the Jacobi rounds exceeded its limit");
   return TN_OK;
 }
 
