@@ -685,6 +685,27 @@ def heisenberg_mpo(L, J, Jz, h):
     return [W[4:5].copy()] + [W.copy() for _ in range(L - 2)] + [W[:, :, :, 0:1].copy()]
 
 
+def spin1_xxz_mpo(L, J, Jz, D):
+    """Spin-1 XXZ chain with single-ion anisotropy, H = Σ J(S⁺S⁻ + S⁻S⁺)/2 + Jz SᶻSᶻ +
+    D Σ (Sᶻ)², bond-5 MPO, d = 3 (the layout of heisenberg_mpo).  Not a reference model: a
+    d = 3 Hamiltonian for the DMRG parity tests."""
+    r2 = np.sqrt(2.0)
+    sp = np.array([[0.0, r2, 0.0], [0.0, 0.0, r2], [0.0, 0.0, 0.0]])
+    sm = sp.T.copy()
+    sz = np.diag([1.0, 0.0, -1.0])
+    W = np.zeros((5, 3, 3, 5), dtype=np.complex128)
+    W[0, :, :, 0] = np.eye(3)
+    W[1, :, :, 0] = sp
+    W[2, :, :, 0] = sm
+    W[3, :, :, 0] = sz
+    W[4, :, :, 0] = D * sz @ sz
+    W[4, :, :, 1] = 0.5 * J * sm
+    W[4, :, :, 2] = 0.5 * J * sp
+    W[4, :, :, 3] = Jz * sz
+    W[4, :, :, 4] = np.eye(3)
+    return [W[4:5].copy()] + [W.copy() for _ in range(L - 2)] + [W[:, :, :, 0:1].copy()]
+
+
 def mpo_dense(mpo):
     """The MPO as a dense 2^L × 2^L matrix (small L only): H[o…, i…]."""
     M = mpo[0][0]  # (o, i, r)

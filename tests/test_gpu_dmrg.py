@@ -205,3 +205,47 @@ def test_dmrg_heisenberg_bond5_matches_oracle(method):
     if method == 2:  # full bond: the extreme eigenvalue of H (which = :LM)
         w = np.linalg.eigvalsh(O.mpo_dense(H))
         assert abs(E - w[np.argmax(np.abs(w))]) < 1e-9
+
+
+def _compare_with_oracle(sites, H, nsweeps, method, maxdim=16, krylovdim=3, maxiter=2):
+    import tenetgb
+
+    psi = tenetgb.MPS([s.copy() for s in sites])
+    meth = tenetgb.Dmrg1 if method == 1 else tenetgb.Dmrg2
+    _, E, hist = tenetgb.dmrg_(psi, H, nsweeps, method=meth, maxdim=maxdim, krylovdim=krylovdim, maxiter=maxiter,
+                               history=True)
+    ref_hist = []
+    ref, Er = O.dmrg(O.OMPS([s.copy() for s in sites]), H, nsweeps, method="dmrg1" if method == 1 else "dmrg2",
+                     maxdim=maxdim, krylovdim=krylovdim, maxiter=maxiter, history=ref_hist)
+    assert np.allclose(hist, ref_hist, rtol=0, atol=1e-9)
+    assert psi.bondsizes() == ref.bondsizes()
+    return E
+
+
+@pytest.mark.parametrize("L", [2, 3])
+@pytest.mark.parametrize("method", [1, 2])
+def test_dmrg_shortest_chains(L, method):
+    """Every local update touches a boundary environment.  (An XXZ chain in a field: the
+    transverse Ising spectrum is ± symmetric, and which = :LM would tie on it.)"""
+    rng = np.random.default_rng(70 + L)
+    bonds = [1] + [2] * (L - 1) + [1]
+    _compare_with_oracle(rand_sites(rng, bonds), O.heisenberg_mpo(L, 1.0, 0.6, 0.3), 3, method)
+
+
+@pytest.mark.parametrize("method", [1, 2])
+def test_dmrg_spin1_d3(method):
+    """d = 3 sites (spin-1 XXZ with anisotropy, MPO bond 5)."""
+    rng = np.random.default_rng(72)
+    n = 6
+    bonds = [1, 3, 4, 4, 4, 3, 1]
+    _compare_with_oracle(rand_sites(rng, bonds, d=3), O.spin1_xxz_mpo(n, 1.0, 0.8, 0.3), 3, method, maxdim=9)
+
+
+def test_dmrg_larger_krylov_space():
+    """krylovdim 6 and three Lanczos iterations (the wider orthogonalisation kernels and
+    a restart from a longer basis)."""
+    rng = np.random.default_rng(73)
+    n = 8
+    bonds = [1, 2, 4, 4, 4, 4, 4, 2, 1]
+    _compare_with_oracle(rand_sites(rng, bonds), O.heisenberg_mpo(n, 1.0, 0.6, 0.1), 2, 2, maxdim=8, krylovdim=6,
+                         maxiter=3)
