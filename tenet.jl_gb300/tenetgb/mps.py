@@ -232,13 +232,21 @@ class MPS:
         m._L, m._d = Lc.value, dc.value
         return m
 
-    def site(self, i, instance=0):
-        """Site tensor i (1-based) as a (χl, d, χr) numpy array."""
+    def site(self, i, instance=0, out=None):
+        """Site tensor i (1-based) as a (χl, d, χr) numpy array.  ``out``: a flat complex128
+        buffer of at least χl·d·χr elements (e.g. page-locked host memory) to copy into;
+        the returned array is then a column-major view of it."""
         b = [1] + self.bondsizes() + [1]
         shape = (b[i - 1], self._d, b[i])
-        out = np.empty(int(np.prod(shape)), dtype=np.complex128)
-        self._chk(self.lib.tn_mps_get_instance_site(self.h, instance, i, out.ctypes.data_as(C.c_void_p)))
-        return out.reshape(shape, order="F")
+        size = int(np.prod(shape))
+        if out is None:
+            buf = np.empty(size, dtype=np.complex128)
+        else:
+            if out.dtype != np.complex128 or out.ndim != 1 or out.size < size or not out.flags.c_contiguous:
+                raise ValueError("out must be a contiguous 1-D complex128 buffer large enough for the site")
+            buf = out[:size]
+        self._chk(self.lib.tn_mps_get_instance_site(self.h, instance, i, buf.ctypes.data_as(C.c_void_p)))
+        return buf.reshape(shape, order="F")
 
     def sites(self, instance=0):
         return [self.site(i, instance) for i in range(1, self._L + 1)]
