@@ -235,7 +235,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         psi = tenetgb.MPS.batched(states, ctx=ctx, max_bond=CHI_MAX, precision="mixed")
         psi.evolve_brickwork_([ly], maxdim=CHI_MAX, threshold=CUTOFF)
-        new_states = [[psi.site(i + 1, b, out=dst[b][i]) for i in range(L_SITES)] for b in range(Bt)]
+        new_states = [psi.sites(b, out=dst[b]) for b in range(Bt)]
         dt = time.perf_counter() - t0
         del psi
         if k >= args.warmup:
@@ -914,7 +914,7 @@ def run_dmrg(args):
         q = tenetgb.MPS(arrays, ctx=ctx)
         q.unsafe_setform_(tenetgb.MixedCanonical(1))
         _, Eq = tenetgb.dmrg_(q, H, 1, method=tenetgb.Dmrg2, maxdim=chi)
-        back = [q.site(i + 1, out=out_bufs[i]) for i in range(n)]
+        back = q.sites(out=out_bufs)
         e2e_times.append(time.perf_counter() - t0)
         del q
     d2h = sum(b.nbytes for b in back) + 8

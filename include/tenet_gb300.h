@@ -234,6 +234,11 @@ tn_status_t tn_mps_batch_size(const tn_mps* mps, int32_t* B);
 tn_status_t tn_mps_set_instance_site(tn_mps* mps, int32_t b, int32_t site, int64_t chl,
                                      int64_t chr, const void* h_data);
 tn_status_t tn_mps_get_instance_site(const tn_mps* mps, int32_t b, int32_t site, void* h_data);
+/* Every site of instance b in one call: h[i-1] points at site i's column-major
+ * (χ_{i-1}, d, χ_i) data (the MPS's current bonds).  The copies are issued back to back
+ * and waited for once; page-locked host buffers make them DMA transfers. */
+tn_status_t tn_mps_set_instance_sites(tn_mps* mps, int32_t b, const void* const* h);
+tn_status_t tn_mps_get_instance_sites(const tn_mps* mps, int32_t b, void* const* h);
 tn_status_t tn_mps_destroy(tn_mps* mps);
 tn_status_t tn_mps_copy(const tn_mps* src, tn_mps** out);
 /* host data of site i (1-based), column-major (χl, d, χr) C64 */

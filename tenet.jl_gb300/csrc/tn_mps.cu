@@ -606,6 +606,34 @@ tn_status_t tn_mps_get_instance_site(const tn_mps* p, int32_t b, int32_t i, void
   return TN_OK;
 }
 
+tn_status_t tn_mps_set_instance_sites(tn_mps* p, int32_t b, const void* const* h) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_RETURN_IF(check_site_arg(p, b, 1));
+  TN_ARG(ctx, h != nullptr, "tn_mps_set_instance_sites: null data");
+  for (int i = 1; i <= p->L; ++i) TN_ARG(ctx, h[i - 1] != nullptr, "tn_mps_set_instance_sites: null site");
+  for (int i = 1; i <= p->L; ++i) {
+    TN_RETURN_IF(ensure_site(p, i, (size_t)sz(p, i)));
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i] + (size_t)b * p->cap[i], h[i - 1], sizeof(cxd) * sz(p, i),
+                                       cudaMemcpyHostToDevice, ctx->stream));
+  }
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TN_OK;
+}
+
+tn_status_t tn_mps_get_instance_sites(const tn_mps* p, int32_t b, void* const* h) {
+  if (!p) return TN_EINVAL;
+  tn_ctx* ctx = p->ctx;
+  TN_RETURN_IF(check_site_arg(p, b, 1));
+  TN_ARG(ctx, h != nullptr, "tn_mps_get_instance_sites: null output");
+  for (int i = 1; i <= p->L; ++i) TN_ARG(ctx, h[i - 1] != nullptr, "tn_mps_get_instance_sites: null site");
+  for (int i = 1; i <= p->L; ++i)
+    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h[i - 1], p->site[i] + (size_t)b * p->cap[i], sizeof(cxd) * sz(p, i),
+                                       cudaMemcpyDeviceToHost, ctx->stream));
+  TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return TN_OK;
+}
+
 tn_status_t tn_mps_set_site(tn_mps* p, int32_t i, int64_t chl, int64_t chr, const void* h) {
   return tn_mps_set_instance_site(p, 0, i, chl, chr, h);
 }

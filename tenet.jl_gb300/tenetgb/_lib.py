@@ -133,6 +133,8 @@ SIGNATURES = {
     "tn_mps_local_expectations": (_st, [_vp, _vp, _pdbl]),
     "tn_mps_sample": (_st, [_vp, _i32, _i64, _pdbl, _pi32]),
     "tn_mps_evolve_mpo": (_st, [_vp, C.POINTER(_vp), _pi64, _i32, _i64, _dbl]),
+    "tn_mps_set_instance_sites": (_st, [_vp, _i32, C.POINTER(_vp)]),
+    "tn_mps_get_instance_sites": (_st, [_vp, _i32, C.POINTER(_vp)]),
     "tn_mps_dmrg": (_st, [_vp, C.POINTER(_vp), _pi64, _i32, _i32, _i32, _i64, _i32, _i32, _dbl, _pdbl, _pdbl]),
     "tn_dmrg_last_stats": (_st, [_vp, _pdbl, _pi64]),
     "tn_mps_save": (_st, [_vp, C.c_char_p]),

@@ -132,6 +132,8 @@ class MPS:
         for i in range(L_ - 1):
             if sites[i].shape[2] != sites[i + 1].shape[0]:
                 raise ValueError(f"bond {i + 1}-{i + 2}: dims differ")
+        if any(s.ndim != 3 or s.shape[1] != d for s in sites):
+            raise ValueError("every site must be a (χl, d, χr) array with the same physical dimension d")
         if sites[0].shape[0] != 1 or sites[-1].shape[2] != 1:
             raise ValueError("open boundary: end sites must have a size-1 outer bond")
         h = C.c_void_p()
@@ -140,10 +142,9 @@ class MPS:
                                                       precision_code(precision), C.byref(h)))
         self.h = h
         for bi, inst in enumerate(instances):
-            for i, s in enumerate(inst):
-                f = np.asfortranarray(s)
-                self.ctx.check(self.lib.tn_mps_set_instance_site(self.h, bi, i + 1, s.shape[0], s.shape[2],
-                                                                 f.ctypes.data_as(C.c_void_p)))
+            fs = [np.asfortranarray(s) for s in inst]
+            ptrs = (C.c_void_p * L_)(*[f.ctypes.data for f in fs])
+            self.ctx.check(self.lib.tn_mps_set_instance_sites(self.h, bi, ptrs))
         self._L, self._d = L_, d
 
     @classmethod
@@ -248,8 +249,24 @@ class MPS:
         self._chk(self.lib.tn_mps_get_instance_site(self.h, instance, i, buf.ctypes.data_as(C.c_void_p)))
         return buf.reshape(shape, order="F")
 
-    def sites(self, instance=0):
-        return [self.site(i, instance) for i in range(1, self._L + 1)]
+    def sites(self, instance=0, out=None):
+        """All site tensors of one instance, copied in one call; ``out``: a list of flat
+        complex128 buffers (one per site, e.g. page-locked) to copy into."""
+        b = [1] + self.bondsizes() + [1]
+        shapes = [(b[i - 1], self._d, b[i]) for i in range(1, self._L + 1)]
+        bufs = []
+        for k, shp in enumerate(shapes):
+            size = int(np.prod(shp))
+            if out is None:
+                bufs.append(np.empty(size, dtype=np.complex128))
+            else:
+                o = out[k]
+                if o.dtype != np.complex128 or o.ndim != 1 or o.size < size or not o.flags.c_contiguous:
+                    raise ValueError("each out buffer must be a contiguous 1-D complex128 array large enough")
+                bufs.append(o[:size])
+        ptrs = (C.c_void_p * self._L)(*[x.ctypes.data for x in bufs])
+        self._chk(self.lib.tn_mps_get_instance_sites(self.h, instance, ptrs))
+        return [x.reshape(shp, order="F") for x, shp in zip(bufs, shapes)]
 
     def lambda_(self):
         """Λ at the bond-canonical centre (LambdaSite(bond)); (B, χ) when batched."""
