@@ -45,7 +45,7 @@ def ising_1d_mpo(L_, h, J):
     return [W[2:3].copy()] + [W.copy() for _ in range(L_ - 2)] + [W[:, :, :, 0:1].copy()]
 
 
-def _lift(mpo, n):
+def _lift(mpo, n, d=None):
     if len(mpo) != n:
         raise ValueError("MPS and MPO must have the same number of sites")
     out = []
@@ -57,6 +57,8 @@ def _lift(mpo, n):
             W = W[None, :, :, None]
         if W.ndim != 4:
             raise ValueError("MPO sites must be (w_l, d_out, d_in, w_r) arrays")
+        if d is not None and (W.shape[1] != d or W.shape[2] != d):
+            raise ValueError(f"MPO site {i + 1}: physical dimensions {W.shape[1:3]} differ from the MPS's d = {d}")
         out.append(np.asfortranarray(W))
     return out
 
@@ -73,7 +75,7 @@ def dmrg_(psi, H, nsweeps=4, *, method=Dmrg1, maxdim=128, ishermitian=True, kryl
     mpos = H if (len(H) and isinstance(H[0], (list, tuple))) else [H]
     if len(mpos) not in (1, B):
         raise ValueError("give one MPO or one per instance")
-    lifted = [_lift(m, n) for m in mpos]
+    lifted = [_lift(m, n, psi._d) for m in mpos]
     bonds = [a.shape[3] for a in lifted[0][:-1]]
     for m in lifted:
         if [a.shape[3] for a in m[:-1]] != bonds:

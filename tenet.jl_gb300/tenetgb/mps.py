@@ -491,6 +491,8 @@ def evolve_mpo_(psi, mpo, algorithm="direct", maxdim=None, threshold=None):
             W = W[None] if i == 0 else W[..., None]
         if W.ndim == 2:
             W = W[None, :, :, None]
+        if W.ndim != 4 or W.shape[1] != psi._d or W.shape[2] != psi._d:
+            raise ValueError(f"MPO site {i + 1}: expected (w_l, {psi._d}, {psi._d}, w_r), got {W.shape}")
         arrs.append(np.asfortranarray(W))
     wb = (C.c_int64 * max(1, L - 1))(*[a.shape[3] for a in arrs[:-1]])
     ptrs = (C.c_void_p * L)(*[a.ctypes.data for a in arrs])

@@ -58,3 +58,22 @@ def test_gpu_lattice_contraction(shape, mode, dtype, tol):
     # scale: product of the tensors' norms bounds |ref|; compare relative to it
     scale = math.prod(float(np.linalg.norm(a)) for a in net.arrays)
     assert abs(val - ref) <= tol * max(abs(ref), 1e-3 * scale)
+
+
+def test_mpo_dimension_checks_without_a_device():
+    """The MPO argument of dmrg! / evolve! is validated on the host before any device
+    work (the library reads (w_l, d, d, w_r) elements per site)."""
+    import pytest
+
+    import tenetgb
+
+    class FakeMPS:
+        _d = 2
+        nsites = 3
+        batch = 1
+
+    W = [np.zeros((1, 3, 3, 2)), np.zeros((2, 3, 3, 2)), np.zeros((2, 3, 3, 1))]
+    with pytest.raises(ValueError, match="physical dimensions"):
+        tenetgb.dmrg_(FakeMPS(), W, 1)
+    with pytest.raises(ValueError, match="same number of sites"):
+        tenetgb.dmrg_(FakeMPS(), W[:2], 1)
