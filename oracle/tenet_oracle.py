@@ -149,6 +149,34 @@ def mps_from_arrays(arrays, order=("l", "r", "o")):
     return OMPS(out)
 
 
+def mpo_from_arrays(arrays, order=("l", "r", "o", "i")):
+    """``MPO(arrays; order)`` (src/Components/MPO.jl:85-125, default order (:l, :r, :o, :i))
+    as an MPS whose physical index fuses (o, i) column-major (o fastest): canonize! and
+    compress! on an MPO keep both plugs on the same side of every factorisation, so the
+    fused MPS has the same gauge moves.  Returns the OMPS with ``phys`` = [(d_o, d_i)]."""
+    order = tuple(order)
+    assert sorted(order) == ["i", "l", "o", "r"]
+    L = len(arrays)
+    sites, phys = [], []
+    for k, a in enumerate(arrays):
+        a = np.asarray(a)
+        own = tuple(x for x in order if not ((k == 0 and x == "l") or (k == L - 1 and x == "r")))
+        assert a.ndim == len(own), f"site {k + 1}: expected {len(own)} dimensions"
+        t = np.moveaxis(a, [own.index(x) for x in ("o", "i")] + [own.index(x) for x in ("l", "r") if x in own],
+                        list(range(len(own))))
+        # t: (o, i[, l][, r]) → (l, o, i, r) with size-1 open ends
+        o, i = t.shape[0], t.shape[1]
+        rest = t.shape[2:]
+        l = rest[0] if "l" in own else 1
+        r = rest[-1] if "r" in own else 1
+        t = np.transpose(t.reshape(o, i, l, r), (2, 0, 1, 3))
+        sites.append(np.ascontiguousarray(t.reshape(l, o * i, r, order="F")))
+        phys.append((o, i))
+    psi = OMPS(sites)
+    psi.phys = phys
+    return psi
+
+
 # ----------------------------------------------------------------------------------
 # Muscle-level primitives (restated)
 # ----------------------------------------------------------------------------------

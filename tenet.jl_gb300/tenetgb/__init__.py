@@ -21,6 +21,7 @@ from .core import (
 )
 from .dmrg import Dmrg1, Dmrg2, dmrg, dmrg_, ising_1d_mpo
 from .dmrg import last_stats as dmrg_last_stats
+from .mpo import MPO
 from .mps import (
     MPS,
     BondCanonical,

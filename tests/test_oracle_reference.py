@@ -374,3 +374,59 @@ def test_heisenberg_mpo_matches_dense_hamiltonian():
     _, E = O.dmrg(psi0, O.heisenberg_mpo(n, J, Jz, h), 6, method="dmrg2", maxdim=8)
     w = np.linalg.eigvalsh(H)
     assert abs(E - w[np.argmax(np.abs(w))]) < 1e-9
+
+
+# ---------------------------------------------------------------------------------
+# MPO (test/unit/mpo.jl): canonize! on an MPO keeps (o, i) together on the physical side
+# ---------------------------------------------------------------------------------
+def fixture_mpo():
+    """test/unit/mpo.jl:82-88 (default order (:l, :r, :o, :i))."""
+    return O.mpo_from_arrays([jl((1, 64), 4, 4, 4)] + [jl((1, 256), 4, 4, 4, 4)] * 3 + [jl((1, 64), 4, 4, 4)])
+
+
+@pytest.mark.parametrize("case,arrays,order,bonds,phys", [
+    ("1", [np.ones((2, 3, 4)), 2 * np.ones((2, 2, 3, 4)), 3 * np.ones((2, 3, 4))], ("l", "r", "o", "i"), [2, 2],
+     [(3, 4)] * 3),
+    ("2", [np.ones((4, 7, 1)), 2 * np.ones((4, 5, 6, 3)), 3 * np.ones((5, 8, 2))], ("l", "r", "o", "i"), [4, 5],
+     [(7, 1), (6, 3), (8, 2)]),
+    ("3", [np.ones((4, 7, 1)), 2 * np.ones((5, 6, 4, 3)), 3 * np.ones((8, 5, 2))], ("r", "o", "l", "i"), [4, 5],
+     [(7, 1), (6, 3), (8, 2)]),
+])
+def test_mpo_constructor(case, arrays, order, bonds, phys):
+    # test/unit/mpo.jl:6-79: plug sizes (o, i) and bond sizes per case
+    H = O.mpo_from_arrays(arrays, order=order)
+    assert H.bondsizes() == bonds and H.phys == phys
+    # the values sit where the reference puts them (site 2 is 2·ones)
+    assert np.all(H.site(2) == 2)
+
+
+# (start, target, isometries that must hold / must not hold): test/unit/mpo.jl:81-462
+MPO_TRANSITIONS = [
+    (None, 3, [(1, "r"), (2, "r"), (4, "l"), (5, "l")], [(3, "l"), (3, "r")]),
+    (None, [2, 3], [(1, "r"), (4, "l"), (5, "l")], [(2, "l"), (3, "r")]),
+    (5, 3, [(1, "r"), (2, "r"), (4, "l"), (5, "l")], [(3, "l"), (3, "r")]),
+    ([3, 4, 5], 3, [(1, "r"), (2, "r"), (4, "l"), (5, "l")], [(3, "l"), (3, "r")]),
+    ([1, 2, 3, 4, 5], [2, 3], [(1, "r"), (4, "l"), (5, "l")], [(2, "l"), (3, "r")]),
+    (None, (2, 3), [(1, "r"), (4, "l"), (5, "l")], [(2, "l"), (3, "r")]),
+    (5, (2, 3), [(1, "r"), (4, "l"), (5, "l")], [(2, "l"), (3, "r")]),
+    ([3, 4, 5], (1, 2), [(3, "l"), (4, "l"), (5, "l")], [(2, "r")]),
+    ((4, 5), (2, 3), [(1, "r"), (4, "l"), (5, "l")], []),
+    ((2, 3), 3, [(1, "r"), (2, "r"), (4, "l"), (5, "l")], []),
+    ((4, 5), 3, [(1, "r"), (2, "r"), (4, "l"), (5, "l")], []),
+]
+
+
+@pytest.mark.parametrize("start,target,isos,not_isos", MPO_TRANSITIONS)
+def test_mpo_canonize_transitions(start, target, isos, not_isos):
+    psi = fixture_mpo()
+    if start is None:
+        psi.form = O.NonCanonical()
+    else:
+        O.canonize(psi, start)
+    c = O.canonize(psi.copy(), target)
+    assert O.checkform(c)
+    for site, side in isos:
+        assert iso(c, site, side), (site, side)
+    for site, side in not_isos:
+        assert not iso(c, site, side), (site, side)
+    assert state_close(c, psi)
