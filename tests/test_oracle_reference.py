@@ -296,13 +296,20 @@ def test_mpo_evolution_direct_and_zipup_match_dense():
     assert max(zt.bondsizes()) <= 3
 
 
+def known_answers():
+    """The reference's own recorded DMRG answers (test/unit/dmrg.jl assertions and the
+    examples/dmrg.ipynb outputs), extracted by tests/golden/extract_known_answers.py."""
+    import json
+    import os
+
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference_known_answers.json")
+    with open(path) as f:
+        return json.load(f)
+
+
 # test/unit/dmrg.jl:5-39: n = 10, ising_1d_mpo(n, 1.0, 1.0), 10 sweeps, atol 1e-4 per site
-DMRG_CASES = [
-    ("product", "dmrg1", 128, -1.1902477482849715),
-    ("delta", "dmrg1", 128, -1.2372129315563634),
-    ("product", "dmrg2", 1, -1.1944098151375718),
-    ("product", "dmrg2", 32, -1.2381489999654788),
-]
+DMRG_CASES = [(c["start"], c["method"].lower(), c["maxdim"] or 128, c["energy_per_site"])
+              for c in known_answers()["dmrg_tests"]]
 
 
 def dmrg_start(kind, n=10):
@@ -430,3 +437,24 @@ def test_mpo_canonize_transitions(start, target, isos, not_isos):
     for site, side in not_isos:
         assert not iso(c, site, side), (site, side)
     assert state_close(c, psi)
+
+
+def test_dmrg_known_answers_fixture_matches_the_reference_tests():
+    cases = known_answers()["dmrg_tests"]
+    assert [c["source"] for c in cases] == ["test/unit/dmrg.jl:13", "test/unit/dmrg.jl:23", "test/unit/dmrg.jl:32",
+                                            "test/unit/dmrg.jl:38"]
+    assert [(c["start"], c["method"], c["maxdim"]) for c in cases] == [
+        ("product", "Dmrg1", None), ("delta", "Dmrg1", None), ("product", "Dmrg2", 1), ("product", "Dmrg2", 32)]
+
+
+def test_dmrg_oracle_reproduces_the_notebook_first_calls():
+    """examples/dmrg.ipynb cell 6: dmrg!(ψ, H, 1; Dmrg2, maxdim = 128) called repeatedly on
+    the 100-site Ising chain from |0…0⟩.  The first two calls (bonds ≤ 16) are cheap; the
+    oracle reproduces the printed energies to rounding."""
+    ref = known_answers()["dmrg_notebook"]["dmrg2_product"]["energies_per_call"]
+    n = 100
+    psi = O.OMPS([np.array([1.0, 0.0], dtype=np.complex128).reshape(1, 2, 1) for _ in range(n)])
+    H = O.ising_1d_mpo(n, 1.0, 1.0)
+    for call in range(2):
+        psi, E = O.dmrg(psi, H, 1, method="dmrg2", maxdim=128)
+        assert abs(E - ref[call]) < 1e-11, (call, E, ref[call])
