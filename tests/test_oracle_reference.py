@@ -458,3 +458,30 @@ def test_dmrg_oracle_reproduces_the_notebook_first_calls():
     for call in range(2):
         psi, E = O.dmrg(psi, H, 1, method="dmrg2", maxdim=128)
         assert abs(E - ref[call]) < 1e-11, (call, E, ref[call])
+
+
+def test_mps_notebook_forms_and_bond_sizes():
+    """examples/mps.ipynb (unseeded rand, so its printed forms and bond sizes are the
+    knowns): canonize! → MixedCanonical(1); norm on MixedCanonical(all) moves the centre
+    to site 1; simple_update! on sites (2, 3) leaves MixedCanonical([2, 3]); evolve! by a
+    rand(MPO; n=3, maxdim=4) gives bonds 8, 8; compress!(maxdim=4) then gives 2, 2."""
+    rng = np.random.default_rng(90)
+
+    def r(*s):
+        return rng.random(s) + 1j * rng.random(s)
+
+    psi = O.mps_from_arrays([r(2, 2), r(2, 2, 2), r(2, 2)])
+    assert psi.form == O.MixedCanonical([1, 2, 3])
+    O.canonize(psi, O.MixedCanonical(1))
+    assert psi.form == O.MixedCanonical(1)
+    O.normalize(psi)
+    assert abs(O.norm(psi) - 1.0) < 1e-14
+    O.canonize(psi, O.MixedCanonical([1, 2, 3]))
+    O.norm(psi)
+    assert psi.form == O.MixedCanonical(1)
+    O.simple_update(psi, r(2, 2, 2, 2), (2, 3))
+    assert psi.form == O.MixedCanonical([2, 3])
+    O.evolve_mpo_direct(psi, [r(1, 2, 2, 4), r(4, 2, 2, 4), r(4, 2, 2, 1)])
+    assert psi.bondsizes() == [8, 8]
+    O.compress(psi, maxdim=4)
+    assert psi.bondsizes() == [2, 2]
