@@ -238,6 +238,45 @@ end
 
 LinearAlgebra.normalize!(ψ::GB300MPS) = (check(ccall((:tn_mps_normalize, libtenetgb), Int32, (Ptr{Cvoid},), ψ.h), ψ.ctx.h); ψ)
 
+# evolve!(ψ, op::MPO) — src/Operations/evolve.jl:19-137 (algorithm :direct or :zipup); the
+# MPO as its (w_l, d_out, d_in, w_r) site arrays
+function evolve!(ψ::GB300MPS, H::Vector{Array{ComplexF64,4}}; algorithm::Symbol=:direct, maxdim::Integer=0,
+                 threshold::Real=0.0)
+    ptrs = Ptr{ComplexF64}[pointer(W) for W in H]
+    bonds = Int64[size(W, 4) for W in H[1:end-1]]
+    GC.@preserve H begin
+        check(ccall((:tn_mps_evolve_mpo, libtenetgb), Int32,
+                    (Ptr{Cvoid}, Ptr{Ptr{ComplexF64}}, Ptr{Int64}, Int32, Int64, Float64),
+                    ψ.h, ptrs, bonds, algorithm === :zipup ? 1 : 0, maxdim, threshold), ψ.ctx.h)
+    end
+    return ψ
+end
+
+# sample(ψ, nshots) — src/Operations/sample.jl:20-72; the caller's uniforms (nshots × L in
+# [0, 1)) make the draw reproducible; outcomes are 1-based like the reference's
+function sample(ψ::GB300MPS, nshots::Integer; uniforms::Matrix{Float64}=rand(ψ.L, nshots))
+    out = Matrix{Int32}(undef, ψ.L, nshots)
+    check(ccall((:tn_mps_sample, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int64, Ptr{Float64}, Ptr{Int32}),
+                ψ.h, 0, nshots, uniforms, out), ψ.ctx.h)
+    return permutedims(out)
+end
+
+# device MPS dump / load (raw column-major format, warm restarts)
+save(ψ::GB300MPS, path::AbstractString) =
+    check(ccall((:tn_mps_save, libtenetgb), Int32, (Ptr{Cvoid}, Cstring), ψ.h, path), ψ.ctx.h)
+
+function load(path::AbstractString; max_bond::Integer=0, ctx=default_context())
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:tn_mps_load, libtenetgb), Int32, (Ptr{Cvoid}, Cstring, Int64, Ref{Ptr{Cvoid}}), ctx.h, path, max_bond,
+                r), ctx.h)
+    L, d, B = Ref{Int32}(0), Ref{Int32}(0), Ref{Int32}(0)
+    check(ccall((:tn_mps_shape, libtenetgb), Int32, (Ptr{Cvoid}, Ref{Int32}, Ref{Int32}, Ref{Int32}), r[], L, d, B),
+          ctx.h)
+    mps = GB300MPS(r[], ctx, L[], d[])
+    finalizer(m -> ccall((:tn_mps_destroy, libtenetgb), Int32, (Ptr{Cvoid},), m.h), mps)
+    return mps
+end
+
 # dmrg!(ψ, H, nsweeps; method) — src/Algorithms/DMRG.jl:45-459.  H: the MPO's site arrays,
 # column-major (w_l, d_out, d_in, w_r) with w_0 = w_L = 1 (`MPO(arrays; order=(:l, :o, :i, :r))`).
 function dmrg!(ψ::GB300MPS, H::Vector{Array{ComplexF64,4}}, nsweeps::Integer=4; method::Symbol=:dmrg1,
