@@ -148,17 +148,18 @@ tn_status_t tn_svd_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int6
 
 /* Allocation-free thin SVD of a ComplexF64 matrix, m >= n (no counterpart in the
  * reference: it is an addition for callers that cannot allocate device memory where they
- * need the factorisation — inside someone else's stream capture, in loops whose memory is
- * fixed up front, or with only a stream and no allocator at hand).
+ * need the factorisation — loops whose memory is fixed up front, or hosts that have a
+ * stream but no allocator and no tn_ctx).
  * Same outputs as tn_svd_thin: U (m×n), S (n, FP64, descending), Vh (n×n), dense
  * column-major, all caller-owned device buffers; no context, no cudaMalloc/cudaFree.
  * Scratch lives in a 16 MiB file-scope device array that every GPU loading the library
  * holds until exit, so (m·n + n²)·16 + n·12 + ~1 KiB must fit in 16 MiB (e.g. 1024×512);
- * larger sizes return TN_EINVAL.  The first call on each device looks up the array's
- * device address and should come before any stream capture.  Every call shares the
- * array: calls that overlap on the GPU (two streams, two host threads) race.  Runs on
- * `stream` (a cudaStream_t; NULL = the legacy default stream) and returns after that work
- * has completed.  Errors: tn_last_error_string(NULL). */
+ * larger sizes return TN_EINVAL, and more than 4096 rows TN_EUNSUPPORTED.  The first call
+ * on each device looks up the array's device address.  Every call shares the array:
+ * calls that overlap on the GPU (two streams, two host threads) race.  Runs on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream), synchronises that stream once per
+ * Jacobi sweep to read the convergence flag, and returns after the work has completed.
+ * Errors: tn_last_error_string(NULL). */
 tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, const void* d_A, int64_t lda,
                                 void* d_U, double* d_S, void* d_Vh);
 

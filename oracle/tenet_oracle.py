@@ -188,10 +188,13 @@ def qr_thin(m):
     return q, r
 
 
-def svd_thin(m):
-    """tensor_svd_thin on a matrix: LAPACK gesdd; s descending; m = U diag(s) Vh."""
+def svd_thin(m, driver="gesdd"):
+    """tensor_svd_thin on a matrix: LAPACK gesdd; s descending; m = U diag(s) Vh.
+    ``driver="gesvd"`` selects LAPACK's QR-iteration SVD instead: the same
+    decomposition with different rounding, which the full-size parity tests use to
+    measure how far rounding alone moves a truncated TEBD run."""
     try:
-        u, s, vh = sla.svd(m, full_matrices=False, lapack_driver="gesdd")
+        u, s, vh = sla.svd(m, full_matrices=False, lapack_driver=driver)
     except np.linalg.LinAlgError:
         u, s, vh = sla.svd(m, full_matrices=False, lapack_driver="gesvd")
     return u, s, vh
@@ -411,7 +414,7 @@ def compress(psi: OMPS, bond=None, maxdim=None, threshold=None):
 # ----------------------------------------------------------------------------------
 
 
-def simple_update_tensors(A, B, G, maxdim=None, threshold=None):
+def simple_update_tensors(A, B, G, maxdim=None, threshold=None, driver="gesdd"):
     """Muscle.simple_update with AbsorbEqually: θ[l,a,b,r] = Σ G[a,b,a',b'] A[l,a',m]
     B[m,b',r]; SVD over (l,a)|(b,r); keep ≤ maxdim (then |s| > threshold, ≥ 1 kept);
     A' = U√S, B' = √S Vh.  Returns (A', B', s_kept, s_full)."""
@@ -419,7 +422,7 @@ def simple_update_tensors(A, B, G, maxdim=None, threshold=None):
     _, d2, chr_ = B.shape
     theta = np.tensordot(A, B, axes=(2, 0))  # l, a', b', r
     theta = np.einsum("abcd,lcdr->labr", G, theta, optimize=True)
-    u, s, vh = svd_thin(theta.reshape(chl * d1, d2 * chr_))
+    u, s, vh = svd_thin(theta.reshape(chl * d1, d2 * chr_), driver)
     k = s.size if maxdim is None else min(maxdim, s.size)
     if threshold is not None:
         k = max(1, int(np.count_nonzero(np.abs(s[:k]) > threshold)))
@@ -429,12 +432,13 @@ def simple_update_tensors(A, B, G, maxdim=None, threshold=None):
     return An, Bn, s[:k], s
 
 
-def simple_update(psi: OMPS, G, sites, maxdim=None, threshold=None):
+def simple_update(psi: OMPS, G, sites, maxdim=None, threshold=None, spectra=None, driver="gesdd"):
     """simple_update!(ψ::MPS, op) (simple_update.jl:82-92): move the centre onto the
     gate's sites, then apply; the 1-site shortcut is simple_update.jl:27-37.
 
     ``G`` is the gate array; for two sites its index order is
-    [plug a, plug b, plug a', plug b'] with a < b adjacent, primed = input."""
+    [plug a, plug b, plug a', plug b'] with a < b adjacent, primed = input.
+    ``spectra`` (a list) receives θ's full singular spectrum of a two-site gate."""
     sites = sorted(sites)
     canonize(psi, MixedCanonical(sites))
     if len(sites) == 1:
@@ -443,7 +447,9 @@ def simple_update(psi: OMPS, G, sites, maxdim=None, threshold=None):
         return psi
     a, b = sites
     assert b == a + 1
-    An, Bn, _, _ = simple_update_tensors(psi.site(a), psi.site(b), G, maxdim, threshold)
+    An, Bn, _, s_full = simple_update_tensors(psi.site(a), psi.site(b), G, maxdim, threshold, driver)
+    if spectra is not None:
+        spectra.append(s_full)
     psi.set_site(a, An)
     psi.set_site(b, Bn)
     return psi
@@ -661,13 +667,26 @@ def contract_state(psi: OMPS):
 # ----------------------------------------------------------------------------------
 
 
-def tebd(psi: OMPS, layers, maxdim, threshold):
-    """Apply brickwork layers [(bond_start, [G...]), ...] left→right."""
+def tebd(psi: OMPS, layers, maxdim, threshold, spectra=None, driver="gesdd"):
+    """Apply brickwork layers [(bond_start, [G...]), ...] left→right.  ``spectra`` (a
+    list) receives every gate's full θ spectrum, in order."""
     for start, gates in layers:
         for j, G in enumerate(gates):
             a = start + 2 * j
-            simple_update(psi, G, (a, a + 1), maxdim=maxdim, threshold=threshold)
+            simple_update(psi, G, (a, a + 1), maxdim=maxdim, threshold=threshold, spectra=spectra, driver=driver)
     return psi
+
+
+def truncation_gap(s, maxdim, threshold):
+    """Relative gap (σ_k − σ_{k+1}) / σ_k at a gate's cut, k the kept rank under the
+    maxdim cap and the absolute threshold; +inf when nothing above the threshold is
+    discarded (the cut then falls at the threshold, far below the kept values)."""
+    k = s.size if maxdim is None else min(maxdim, s.size)
+    if threshold is not None:
+        k = max(1, int(np.count_nonzero(np.abs(s[:k]) > threshold)))
+    if k >= s.size or s[k] <= (threshold or 0.0):
+        return float("inf")
+    return float((s[k - 1] - s[k]) / s[k - 1])
 
 
 # ----------------------------------------------------------------------------------

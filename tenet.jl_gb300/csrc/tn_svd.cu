@@ -1419,17 +1419,19 @@ tn_status_t svd_any(tn_ctx* ctx, tn_dtype_t dt, tn_precision_t prec, int64_t m, 
 // ---------------------------------------------------------------------------------
 // Allocation-free thin SVD.
 //
-// Some callers cannot allocate device memory at the point where they need an SVD: code
-// that runs while a CUDA graph is being captured by someone else, real-time loops whose
-// memory was fixed up front, or hosts that hand the library a stream but no allocator.
+// Some callers cannot allocate device memory at the point where they need an SVD:
+// real-time loops whose memory was fixed up front, or hosts that hand the library a
+// stream but no allocator (and no tn_ctx with its workspace arena).
 // tn_svd_thin_noalloc serves them: it takes only the caller's input and output buffers
 // and keeps its scratch (W, V, column norms, the sort order and two flag words) in one
 // file-scope device array of kNoAllocScratchBytes.  Every GPU that loads the library
-// holds that array until the process exits.
+// holds that array until the process exits.  The call waits on its stream once per
+// Jacobi sweep (to read the convergence flag), so it returns with the work complete.
 // ---------------------------------------------------------------------------------
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = size_t(16) << 20;  // 16 MiB per device
+constexpr int64_t kNoAllocMaxRows = 4096;                   // rows a Jacobi step holds
 __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_noalloc_mu;
@@ -1473,6 +1475,11 @@ extern "C" tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, c
     return tn_set_error(nullptr, TN_EINVAL, "tn_svd_thin_noalloc: need m >= n >= 1 (pass the adjoint for m < n)");
   if (lda < m) return tn_set_error(nullptr, TN_EINVAL, "tn_svd_thin_noalloc: lda < m");
   if (!d_A || !d_U || !d_S || !d_Vh) return tn_set_error(nullptr, TN_EINVAL, "tn_svd_thin_noalloc: null pointer");
+  // the Jacobi step keeps a column pair in registers, 16 rows per thread of a 256-thread
+  // CTA at most: taller matrices are refused here, as the context SVD refuses them
+  if (m > kNoAllocMaxRows)
+    return tn_set_error(nullptr, TN_EUNSUPPORTED, "tn_svd_thin_noalloc: %lld rows; at most %lld are supported",
+                        (long long)m, (long long)kNoAllocMaxRows);
   // scratch layout: W (m×n) | V (n×n) | column norms (n) | order (n) | active | rotated
   const size_t oW = 0, oV = oW + al256(sizeof(cxd) * (size_t)(m * n)), oN = oV + al256(sizeof(cxd) * (size_t)(n * n)),
                oO = oN + al256(sizeof(double) * (size_t)(n + 1)), oF = oO + al256(sizeof(int) * (size_t)n),
@@ -1527,7 +1534,7 @@ extern "C" tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, c
       else if (m <= 2048)
         k_jacobi_step_reg<double, 256, 8, false><<<grid, 256, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
                                                                         rotated, tol, nullptr);
-      else
+      else  // m <= kNoAllocMaxRows = 256 threads x 16 rows
         k_jacobi_step_reg<double, 256, 16, false><<<grid, 256, 0, st>>>(m, n, N, r, W, m * n, V, n * n, nrm, active,
                                                                          rotated, tol, nullptr);
       NA_CHECK(cudaGetLastError());

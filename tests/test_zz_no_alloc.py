@@ -1,8 +1,8 @@
 """The allocation-free SVD entry point (tn_svd_thin_noalloc).
 
 It exists for callers that cannot allocate device memory at the point where they need an
-SVD (someone else's stream capture, fixed-memory loops, a bare stream without an
-allocator).  It keeps its scratch in a file-scope device array instead of calling
+SVD (loops whose memory is fixed up front, a bare stream without an allocator or a
+context).  It keeps its scratch in a file-scope device array instead of calling
 cudaMalloc.  This test calls it through the C ABI twice in a row on the same inputs and
 checks its outputs against tn_svd_thin, within the FP64 tolerance the other SVD tests use
 (1e-12 relative).  The second call shows that whatever the first left in the shared
@@ -22,7 +22,7 @@ def _cgauss(rng, shape):
     return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2)
 
 
-@pytest.mark.parametrize("m,n", [(200, 120), (512, 512), (96, 96), (1024, 512)])
+@pytest.mark.parametrize("m,n", [(200, 120), (512, 512), (96, 96), (1024, 512), (3000, 40), (4096, 64)])
 def test_noalloc_svd_matches_tn_svd_thin_twice(m, n):
     import tenetgb
 
@@ -68,3 +68,8 @@ def test_noalloc_svd_rejects_sizes_beyond_its_scratch():
     assert b"16 MiB" in lib.tn_last_error_string(None)
     st = lib.tn_svd_thin_noalloc(None, 10, 20, C.c_void_p(16), 10, C.c_void_p(16), C.c_void_p(16), C.c_void_p(16))
     assert st == tenetgb._lib.TN_EINVAL
+    # 8192 x 64 fits the scratch (8.4 MB) but the Jacobi step holds at most 4096 rows
+    st = lib.tn_svd_thin_noalloc(None, 8192, 64, C.c_void_p(16), 8192, C.c_void_p(16), C.c_void_p(16),
+                                 C.c_void_p(16))
+    assert st == tenetgb._lib.TN_EUNSUPPORTED
+    assert b"4096" in lib.tn_last_error_string(None)
