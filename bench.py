@@ -35,6 +35,9 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 SAT_LAYERS = 5
+# DRAM bytes per launch of the step's dominant kernels from one ncu capture (dram__bytes_read.sum
+# + dram__bytes_write.sum, profiles/), by profiler class; None where not captured
+DOMINANT_TRAFFIC = {}
 L_SITES, CHI0, CHI_MAX, CUTOFF = 64, 16, 256, 1e-12
 METRIC = "tebd_gate_layers_per_s_chi256"
 UNIT = "layers/s"
@@ -142,6 +145,129 @@ def flush_l2(torch, buf):
     buf.add_(1.0)
 
 
+def bench_config(ws, batch):
+    """The workload description both arms print (identical dicts)."""
+    return dict(CONFIG, parallelism=f"replicas{ws}", batch_instances=batch,
+                l2="flushed between steps (256 MB write)")
+
+
+def _timed_layers(ctx, torch, stream, dev, l2buf, psi, layers, warm):
+    """Apply `layers` to psi one at a time; the first `warm` untimed, the rest each timed
+    with CUDA events on the library's stream, L2 flushed before each."""
+    for ly in layers[:warm]:
+        psi.evolve_brickwork_([ly], maxdim=CHI_MAX, threshold=CUTOFF)
+    ctx.sync()
+    times = []
+    for ly in layers[warm:]:
+        flush_l2(torch, l2buf)
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        psi.evolve_brickwork_([ly], maxdim=CHI_MAX, threshold=CUTOFF)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    return times
+
+
+def pipe_peaks(ctx):
+    """Roofline denominators: HBM copy rate and BF16 dense rate from MEASURED_PEAKS.json
+    (measured on this machine), the CUDA cores' FP32 and FP64 FMA rates measured here
+    (tn_pipe_peak: a register-resident FMA loop over every SM)."""
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        mp = json.load(open(path))
+        hbm, bf16, src = mp["hbm_gbs"], mp["bf16_tflops"], "MEASURED_PEAKS.json"
+    else:
+        hbm, bf16, src = 6800.0, 1900.0, "fallback (6.8 TB/s, 1.9 PFLOP/s bf16)"
+    return {"hbm_gbs": hbm, "bf16_tflops": bf16, "fp32_tflops": ctx.pipe_peak("fp32"),
+            "fp64_tflops": ctx.pipe_peak("fp64"),
+            "source": f"HBM and BF16: {src} (measured); FP32 / FP64 CUDA-core FMA rate: measured in this run"}
+
+
+# per profiled class: the pipe whose peak bounds its arithmetic
+_PIPE = {"jacobi_fp32": ("fp32_tflops", "fp32_cuda_cores"), "jacobi_fp64": ("fp64_tflops", "fp64_cuda_cores"),
+         "gemm_fp64": ("fp64_tflops", "fp64_cuda_cores"), "gemm_split_bf16": ("bf16_tflops", "tensor"),
+         "split_prep": (None, "hbm"), "qr": ("fp64_tflops", "fp64_cuda_cores"),
+         "jacobi_coop": ("fp64_tflops", "fp64_cuda_cores")}
+_KERNEL = {"jacobi_fp32": "k_jacobi_step_reg<float>", "jacobi_fp64": "k_jacobi_step_reg<double>",
+           "gemm_fp64": "k_gemm_cx<double>", "gemm_split_bf16": "k_gemm_oz (tcgen05 kind::f16)",
+           "split_prep": "k_oz_scales + k_oz_split", "qr": "k_qr_panel + k_apply_block_reflector",
+           "jacobi_coop": "k_jacobi_coop<double>"}
+
+
+def kernel_rooflines(prof, peaks):
+    """Per profiled class (event-timed inside the step): launches, ms, the algorithmic
+    flops and bytes per launch, achieved rates and their fractions of the class's pipe
+    peak and of HBM; 'bound' is the roof nearer to being reached."""
+    total = sum(v["ms"] for v in prof.values()) or 1.0
+    out = {}
+    for name, v in prof.items():
+        if v["launches"] == 0 or v["ms"] <= 0:
+            continue
+        s = v["ms"] * 1e-3
+        peak_key, pipe = _PIPE[name]
+        tfl = v["flops"] / s / 1e12
+        gbs = v["bytes"] / s / 1e9
+        e = {"kernel": _KERNEL[name], "launches": v["launches"], "ms": v["ms"], "share_of_profiled": v["ms"] / total,
+             "launch_avg_ms": v["ms"] / v["launches"], "flops_per_launch": v["flops"] / v["launches"],
+             "bytes_per_launch": v["bytes"] / v["launches"], "achieved_tflops": tfl, "achieved_gbs": gbs,
+             "frac_hbm": gbs / peaks["hbm_gbs"]}
+        if peak_key:
+            e["pipe"] = pipe
+            e["pipe_peak_tflops"] = peaks[peak_key]
+            e["frac_pipe"] = tfl / peaks[peak_key]
+        e["bound"] = pipe if peak_key and e["frac_pipe"] >= e["frac_hbm"] else "hbm"
+        out[name] = e
+    return out
+
+
+def roofline_entry(rooflines, peaks, traffic=None):
+    """The dominant kernel of the step (largest event-timed share) in the bench schema."""
+    name, e = max(rooflines.items(), key=lambda kv: kv[1]["ms"])
+    if e["bound"] == "hbm":
+        achieved, peak, unit, frac = e["achieved_gbs"], peaks["hbm_gbs"], "GB/s", e["frac_hbm"]
+    else:
+        achieved, peak, unit, frac = e["achieved_tflops"], e["pipe_peak_tflops"], "TFLOP/s", e["frac_pipe"]
+    return {"bound": e["bound"], "kernel": e["kernel"], "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": frac, "traffic": traffic, "launch_avg_ms": e["launch_avg_ms"],
+            "flops_per_launch": e["flops_per_launch"], "bytes_per_launch": e["bytes_per_launch"],
+            "share_of_step": e["share_of_profiled"],
+            "timing": "CUDA events on the library stream around each launch / sweep graph inside one mixed B=16 layer",
+            "peak_source": peaks["source"]}
+
+
+def parity_vs_oracle(ctx, n_layers=10):
+    """Plain FP64 GPU against the oracle over the workload's first ten layers from the
+    initial state: ⟨ψ|ψ⟩ relative error, max |Δ⟨Z_i⟩|, equal bonds, and the smallest
+    relative gap (σ_χ − σ_χ+1)/σ_χ over the layer's truncated cuts."""
+    import tenetgb
+    from oracle import tenet_oracle as O
+    from tenetgb import workloads as W
+
+    sites, layers = W.tebd_workload(L=L_SITES, chi0=CHI0, n_layers=n_layers)
+    Z = W.pauli_z()
+    psi = tenetgb.MPS(sites, ctx=ctx, max_bond=CHI_MAX, precision="native")
+    ref = O.OMPS([a.copy() for a in sites])
+    rows = []
+    t0 = time.perf_counter()
+    for ell, ly in enumerate(layers):
+        psi.evolve_brickwork_([ly], maxdim=CHI_MAX, threshold=CUTOFF)
+        spectra = []
+        O.tebd(ref, [ly], CHI_MAX, CUTOFF, spectra=spectra)
+        ov, ov_o = psi.overlap(psi), O.overlap(ref, ref)
+        z_o, _ = O.local_expectations(ref, Z)
+        gaps = [g for g in (O.truncation_gap(x, CHI_MAX, CUTOFF) for x in spectra) if np.isfinite(g)]
+        rows.append({"layer": ell + 1, "overlap_rel_err": abs(ov - ov_o) / abs(ov_o),
+                     "z_max_abs_err": float(np.abs(psi.local_expectations(Z) - z_o).max()),
+                     "bonds_equal": psi.bondsizes() == ref.bondsizes(), "truncated_cuts": len(gaps),
+                     "min_relative_gap": min(gaps) if gaps else None})
+    return {"layers": rows, "max_overlap_rel_err": max(r["overlap_rel_err"] for r in rows),
+            "max_z_abs_err": max(r["z_max_abs_err"] for r in rows),
+            "all_bonds_equal": all(r["bonds_equal"] for r in rows), "seconds": time.perf_counter() - t0,
+            "oracle": "numpy/LAPACK restatement (zgesdd), all host cores"}
+
+
 def run_ours(args):
     import torch
 
@@ -161,7 +287,7 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     l2buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)  # 256 MB > L2
 
-    n_layers = SAT_LAYERS + args.warmup + args.steps
+    n_layers = SAT_LAYERS + args.warmup + args.steps + 1
     all_layers = layers_for(n_layers)
     Bt = args.batch
     insts = [W.random_mps_arrays(L_SITES, 2, CHI0, seed=2 + 1000 * b) for b in range(Bt)]
@@ -170,23 +296,11 @@ def run_ours(args):
     ctx.sync()
     host_states = [base.sites(b) for b in range(Bt)]
     host_state = host_states[0]
-    run_layers = all_layers[SAT_LAYERS:]
+    run_layers = all_layers[SAT_LAYERS:SAT_LAYERS + args.warmup + args.steps]
+    prof_layer = all_layers[-1]
 
     def timed(psi, layers, warm):
-        for ly in layers[:warm]:
-            psi.evolve_brickwork_([ly], maxdim=CHI_MAX, threshold=CUTOFF)
-        ctx.sync()
-        times = []
-        for ly in layers[warm:]:
-            flush_l2(torch, l2buf)
-            torch.cuda.synchronize(dev)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            psi.evolve_brickwork_([ly], maxdim=CHI_MAX, threshold=CUTOFF)
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) / 1e3)
-        return times
+        return _timed_layers(ctx, torch, stream, dev, l2buf, psi, layers, warm)
 
     # mixed (headline) on a device copy of the saturated state
     psi_mixed = base.copy()
@@ -200,9 +314,24 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
     launches_total = ctx.launches() - launches0
     launches_per_step = launches_total / max(1, len(run_layers))
-    # plain FP64 on one instance (instance 0's saturated state)
+    # one more mixed layer with the phase profiler on: each Jacobi sweep graph, GEMM and QR
+    # of the step bracketed by CUDA events on the library stream (outside the timed region)
+    peaks = pipe_peaks(ctx)
+    prof_psi = psi_mixed.copy()
+    ctx.profile(True)
+    prof_psi.evolve_brickwork_([prof_layer], maxdim=CHI_MAX, threshold=CUTOFF)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    del prof_psi
+    rooflines = kernel_rooflines(prof, peaks)
+    # plain FP64, one instance (instance 0's saturated state), the same layers
     psi_fp64 = tenetgb.MPS(host_state, ctx=ctx, max_bond=CHI_MAX, precision="native")
     t_fp64 = timed(psi_fp64, run_layers, args.warmup)
+    # plain FP64 with the B instances batched (1 warm-up layer, 2 timed): the batching
+    # share of the mixed-batched speed-up
+    psi_fp64b = base.copy()
+    t_fp64b = timed(psi_fp64b, run_layers[:3], 1)
+    del psi_fp64b
     # accuracy of mixed vs FP64 after the same layers (instance 0)
     m0 = tenetgb.MPS(psi_mixed.sites(0), ctx=ctx, max_bond=CHI_MAX)
     ov_m, ov_f = m0.overlap(m0), psi_fp64.overlap(psi_fp64)
@@ -229,7 +358,8 @@ def run_ours(args):
             v[...] = a
             row.append(v)
         states.append(row)
-    for k, ly in enumerate(run_layers):
+    e2e_layers = run_layers[: 1 + min(args.steps, 4)]
+    for k, ly in enumerate(e2e_layers):
         dst = bufs[(k + 1) % 2]
         torch.cuda.synchronize(dev)
         t0 = time.perf_counter()
@@ -238,15 +368,18 @@ def run_ours(args):
         new_states = [psi.sites(b, out=dst[b]) for b in range(Bt)]
         dt = time.perf_counter() - t0
         del psi
-        if k >= args.warmup:
+        if k >= 1:
             t_e2e.append(dt)
             h2d = sum(s.nbytes for st in states for s in st) + sum(np.asarray(g).nbytes for g in ly[1])
             d2h = sum(s.nbytes for st in new_states for s in st)
         states = new_states
     # max over ranks
-    tm, tf, te = max_over_ranks([sum(t_mixed), sum(t_fp64), sum(t_e2e)], ws)
     K = args.steps
+    tm, tf, tfb, te = max_over_ranks([sum(t_mixed), sum(t_fp64) / len(t_fp64) * K,
+                                      sum(t_fp64b) / len(t_fp64b) * K, sum(t_e2e) / len(t_e2e) * K], ws)
     value = replica_throughput(ws, Bt, K, tm)
+    fp64_value = replica_throughput(ws, 1, K, tf)
+    fp64b_value = replica_throughput(ws, Bt, K, tfb)
     out = {
         "metric": METRIC,
         "value": value,
@@ -258,148 +391,164 @@ def run_ours(args):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "c64 (FP32 Jacobi pre-pass, FP64 rotations/truncation/overlaps)",
+        "dtype": "c64 (FP32 Jacobi pre-pass; split-BF16 tensor-core GEMMs; FP64 rotations/truncation/overlaps)",
         "data": "synthetic (seeded Gaussian MPS, Haar gates)",
-        "config": dict(CONFIG, parallelism=f"replicas{ws}", batch_instances=Bt,
-                       l2="flushed between steps (256 MB write)"),
-        "fp64": {"value": replica_throughput(ws, 1, K, tf), "unit": UNIT, "ms_per_step": 1e3 * tf / K, "instances": 1,
-                 "speedup_of_value": (Bt * tf) / tm},
+        "config": bench_config(ws, Bt),
+        "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": 1e3 * tf / K, "instances": 1,
+                 "speedup_of_value": value / fp64_value},
+        "fp64_batched": {"value": fp64b_value, "unit": UNIT, "ms_per_step": 1e3 * tfb / K, "instances": Bt,
+                         "layers_timed": len(t_fp64b),
+                         "speedup_batching": fp64b_value / fp64_value, "speedup_precision": value / fp64b_value},
         "accuracy_mixed_vs_fp64": {
             "overlap_rel_err": abs(ov_m - ov_f) / abs(ov_f),
             "fidelity_1_minus": float(1 - abs(cross) ** 2 / (abs(ov_m) * abs(ov_f))),
             "z_max_abs_err": float(np.abs(z_m - z_f).max()),
             "layers_compared": len(run_layers),
         },
-        "e2e": {"value": replica_throughput(ws, Bt, K, te), "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "e2e": {"value": replica_throughput(ws, Bt, K, te), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "layers_timed": len(t_e2e)},
         "gpu_launches": int(round(launches_per_step * K)),
         "clocks": clk.summary(),
+        "roofline": roofline_entry(rooflines, peaks, traffic=DOMINANT_TRAFFIC.get(max(rooflines, key=lambda k: rooflines[k]["ms"]))),
+        "kernel_rooflines": rooflines,
+        "peaks": peaks,
     }
-    out["roofline"] = roofline_entry(ctx, stream, dev)
     if rank == 0:
+        if not args.quick:
+            out["parity_fp64_vs_oracle"] = parity_vs_oracle(ctx)
         out["cpu_baseline"] = cpu_sample(host_state, run_layers[0])
+        if not args.quick:
+            out["configs"] = other_configs(args, ctx, torch, stream, peaks)
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
 
 
-def fp64_peak(ctx, stream, dev):
-    """The FP64 pipe rate (TFLOP/s) measured with the library's own complex FP64 GEMM at
-    2048³ (MEASURED_PEAKS.json carries no FP64 rate)."""
-    import ctypes as C
-
-    import torch
-
-    import tenetgb
-
-    rng = np.random.default_rng(1)
-    N = 2048
-    X = tenetgb.DeviceTensor.from_numpy(ctx, rng.standard_normal((N, N)) + 1j * rng.standard_normal((N, N)))
-    Y = tenetgb.DeviceTensor(ctx, (N, N), np.complex128)
-    one, zero = (C.c_double * 2)(1, 0), (C.c_double * 2)(0, 0)
-
-    def g():
-        ctx.check(ctx.lib.tn_gemm(ctx.h, 3, 0, b"N", b"N", N, N, N, one, C.c_void_p(X.ptr), N, 0, C.c_void_p(X.ptr), N,
-                                  0, zero, C.c_void_p(Y.ptr), N, 0, 1))
-
-    g()
-    torch.cuda.synchronize(dev)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    g()
-    e1.record(stream)
-    e1.synchronize()
-    return 8 * N**3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
-
-
-def roofline_entry(ctx, stream, dev):
-    """Dominant kernel: the FP64 Jacobi rotation step (k_jacobi_step_reg) on the 512×512
-    θ of a saturated gate.  Algorithmic flops per launch = 256 pairs × (8m for wᵢᴴwⱼ +
-    24m for the two rotated columns of W + 24n for V).  Peak: the FP64 pipe measured here
-    with the library's own FP64 complex GEMM (MEASURED_PEAKS.json carries no FP64 rate)."""
-    import torch
-
-    import tenetgb
-
-    rng = np.random.default_rng(0)
-    m = n = 512
-    A = tenetgb.DeviceTensor.from_numpy(ctx, (rng.standard_normal((m, n)) + 1j * rng.standard_normal((m, n))), ["r", "c"])
-    l0 = ctx.launches()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    tenetgb.tensor_svd_thin(A, ["r"], ["c"], "s")  # warm (graph instantiation)
-    torch.cuda.synchronize(dev)
-    l0 = ctx.launches()
-    e0.record(stream)
-    tenetgb.tensor_svd_thin(A, ["r"], ["c"], "s")
-    e1.record(stream)
-    e1.synchronize()
-    svd_ms = e0.elapsed_time(e1)
-    n_launch = ctx.launches() - l0
-    # the step kernels are all but ~6 of the launches
-    steps = max(1, n_launch - 6)
-    per_launch_ms = svd_ms / steps
-    flops = (n // 2) * (8 * m + 24 * m + 24 * n)
-    achieved = flops / (per_launch_ms * 1e-3) / 1e12
-    peak = fp64_peak(ctx, stream, dev)
-    # DRAM bytes of one launch of this kernel in this configuration, from one ncu capture
-    # (bench.py --profile-svd; cold cache, so W and V are read once: 8.43 MB), per launch
-    traffic = 8.428032e6
-    return {"bound": "tensor", "kernel": "k_jacobi_step_reg<double> (FP64 pipe)", "achieved": achieved,
-            "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": traffic,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, profiles/jacobi_fp64_step_svd512_b1.md",
-            "peak_source": "FP64 pipe measured in this run (own zgemm 2048^3); MEASURED_PEAKS.json has no FP64 entry",
-            "flops_per_launch": flops, "svd_512_ms": svd_ms, "launch_avg_ms": per_launch_ms}
-
-
-def cpu_sample(host_state, layer, budget_gates=None):
-    """Oracle (numpy/LAPACK restatement) on the host cores: the first gates of one
-    saturated layer applied to the same input state; extrapolated to layers/s."""
+def cpu_sample(host_state, layer):
+    """Oracle (numpy/LAPACK restatement, all host cores) on one whole saturated layer
+    applied to the same input state."""
     from oracle import tenet_oracle as O
 
     start, gates = layer
-    n = len(gates) if budget_gates is None else min(budget_gates, len(gates))
     psi = O.OMPS([np.ascontiguousarray(s) for s in host_state])
     t0 = time.perf_counter()
-    O.tebd(psi, [(start, gates[:n])], maxdim=CHI_MAX, threshold=CUTOFF)
+    O.tebd(psi, [(start, gates)], maxdim=CHI_MAX, threshold=CUTOFF)
     dt = time.perf_counter() - t0
-    per_layer = dt * len(gates) / n
-    return {"value": 1.0 / per_layer, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-            "sample": f"{n} of {len(gates)} gates of one saturated layer (same input MPS), numpy/LAPACK, "
+    return {"value": 1.0 / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"all {len(gates)} gates of one saturated layer (same input MPS), numpy/LAPACK, "
                       f"{os.cpu_count()} threads"}
 
 
 def run_reference(args):
+    """The reference algorithm's CPU path (the oracle restatement: numpy/LAPACK on all
+    host cores) on the same workload: after the five saturating layers, every step
+    applies one whole brickwork layer (31-32 gates), as a step of the GPU arm does."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     from oracle import tenet_oracle as O
     from tenetgb import workloads as W
 
-    n_layers = SAT_LAYERS + 1
-    all_layers = layers_for(n_layers)
+    all_layers = layers_for(SAT_LAYERS + args.warmup + args.steps)
     psi = O.OMPS(W.random_mps_arrays(L_SITES, 2, CHI0, seed=2))
     O.tebd(psi, all_layers[:SAT_LAYERS], maxdim=CHI_MAX, threshold=CUTOFF)
-    start, gates = all_layers[SAT_LAYERS]
-    per_step = 8  # gates per step: a quarter layer keeps the run within minutes
     times = []
-    for k in range(args.warmup + args.steps):
-        p = psi.copy()
+    for k, ly in enumerate(all_layers[SAT_LAYERS:]):
         t0 = time.perf_counter()
-        O.tebd(p, [(start, gates[:per_step])], maxdim=CHI_MAX, threshold=CUTOFF)
+        O.tebd(psi, [ly], maxdim=CHI_MAX, threshold=CUTOFF)
         if k >= args.warmup:
             times.append(time.perf_counter() - t0)
     t = sum(times)
-    frac = per_step / len(gates)
-    value = args.steps * frac / t
+    value = args.steps / t
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1e3 * t / args.steps / frac, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c64 (FP64)", "data": "synthetic (seeded Gaussian MPS, Haar gates)", "impl": "reference",
-        "config": dict(CONFIG, parallelism="cpu"),
+        "config": bench_config(ws, args.batch),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{per_step} of {len(gates)} gates of one saturated layer per step"},
+                         "sample": "whole saturated brickwork layers (31-32 gates) per step, one MPS, numpy/LAPACK "
+                                   f"on {os.cpu_count()} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
+
+
+def run_plain_small(args, ctx=None):
+    """Config 1 (plain FP64, small): L=32, d=2, χ=64 Gaussian MPS (seed 1, not
+    orthogonalised): the QR left-canonize sweep canonize!(ψ, site 32), overlap(ψ, ψ) and
+    ⟨ψ|Z₁₆|ψ⟩ = overlap(ψ, Z₁₆ψ) with Z₁₆ψ from the one-site simple_update!.  Latency-bound:
+    median µs per operation over 20 repetitions and kernel launches per operation, with
+    the values checked against the oracle."""
+    import tenetgb
+    from oracle import tenet_oracle as O
+    from tenetgb import workloads as W
+
+    if ctx is None:
+        ctx = tenetgb.Context(0)
+    sites = W.plain_small_workload()
+    Z = W.pauli_z()
+
+    def op_canonize():
+        p = tenetgb.MPS(sites, ctx=ctx)
+        ctx.sync()
+        l0, t0 = ctx.launches(), time.perf_counter()
+        p.canonize_(32)
+        ctx.sync()
+        return time.perf_counter() - t0, ctx.launches() - l0, p
+
+    res, psi = {}, None
+    for name in ("canonize", "overlap", "z16"):
+        ts, ls = [], []
+        for _ in range(21):
+            if name == "canonize":
+                dt, nl, psi = op_canonize()
+            elif name == "overlap":
+                l0, t0 = ctx.launches(), time.perf_counter()
+                ov = psi.overlap(psi)
+                dt, nl = time.perf_counter() - t0, ctx.launches() - l0
+            else:
+                l0, t0 = ctx.launches(), time.perf_counter()
+                zp = psi.copy()
+                zp.simple_update_(Z, [16])
+                z = psi.overlap(zp)
+                dt, nl = time.perf_counter() - t0, ctx.launches() - l0
+            ts.append(dt)
+            ls.append(nl)
+        res[name] = {"us": 1e6 * float(np.median(ts[1:])), "launches": int(np.median(ls[1:]))}
+    ref = O.OMPS([a.copy() for a in sites])
+    O.canonize(ref, 32)
+    ov_o = O.overlap(ref, ref)
+    pz = ref.copy()
+    O.simple_update(pz, Z, [16])
+    z_o = O.overlap(ref, pz)
+    return {"metric": "plain_small_latency_us", "config": {"workload": "plain_L32_d2_chi64_seed1", "L": 32, "chi": 64},
+            "ops": res, "overlap_rel_err_vs_oracle": abs(ov - ov_o) / abs(ov_o),
+            "z16_rel_err_vs_oracle": abs(z - z_o) / abs(ov_o), "dtype": "c128 (FP64)",
+            "note": "latency-bound (tiny): µs and launches per operation, no roofline claim"}
+
+
+def other_configs(args, ctx, torch, stream, peaks):
+    """Configs 1, 3, 4 and 5 and the standalone kernel rooflines, each compact, for the
+    one bench line (each is also a --workload of its own)."""
+    out = {}
+    for name, fn in [("plain_small", lambda: run_plain_small(args, ctx)),
+                     ("lattice_8x8", lambda: run_lattice(args, ctx, stream)),
+                     ("kernels", lambda: run_kernels(args, ctx, stream)),
+                     ("batched_512", lambda: run_batched(args, ctx)),
+                     ("serving", lambda: run_serving(args, rates=(1000, 5000)))]:
+        t0 = time.perf_counter()
+        try:
+            r = fn()
+        except Exception as e:  # a failing secondary config is reported, not fatal to the headline
+            r = {"error": f"{type(e).__name__}: {e}"}
+        r["seconds"] = time.perf_counter() - t0
+        if name == "batched_512":
+            for k in ("config",):
+                r[k] = {kk: vv for kk, vv in r.get(k, {}).items() if kk not in ("Ls", "chis")}
+        if name == "serving":
+            r.pop("config", None)
+        out[name] = r
+    return out
 
 
 def profile_gate(args):
@@ -484,18 +633,19 @@ def profile_dmrg(args):
                       "bond_max": max(psi.bondsizes())}))
 
 
-def run_lattice(args):
+def run_lattice(args, ctx=None, stream=None):
     """Closed 8×8 lattice, bond 8, ComplexF32 (seed 4): contraction to a scalar along the
     planner's path, in 3×TF32 (tensor pipe), TF32, FP32 (CUDA cores) and FP64; errors
-    against the FP64 run.  Prints one JSON line (a secondary workload)."""
+    against the FP64 run.  Returns one JSON-able dict (a secondary workload)."""
     import torch
 
     import tenetgb
     from tenetgb import network as N
 
-    ctx = tenetgb.Context(0)
-    stream = torch.cuda.Stream()
-    ctx.set_stream(stream.cuda_stream)
+    if ctx is None:
+        ctx = tenetgb.Context(0)
+        stream = torch.cuda.Stream()
+        ctx.set_stream(stream.cuda_stream)
     net = N.lattice_2d(8, 8, 8, seed=4)
     path = N.greedy_path(net.labels, net.dims)
     steps, peak = N.path_flops(net.labels, net.dims, path)
@@ -516,12 +666,12 @@ def run_lattice(args):
     for mode in res:
         res[mode]["rel_err_vs_fp64"] = abs(res[mode]["value"] - ref) / abs(ref)
         res[mode]["value"] = [res[mode]["value"].real, res[mode]["value"].imag]
-    print(json.dumps({"metric": "lattice_8x8_bond8_contraction_tflops", "value": res["3xtf32"]["tflops"],
-                      "unit": "TFLOP/s (complex-algorithmic)", "steps": len(path), "peak_elements": peak,
-                      "path_flops": flops, "modes": res, "data": "synthetic (seeded Gaussian C32, seed 4)"}))
+    return {"metric": "lattice_8x8_bond8_contraction_tflops", "value": res["3xtf32"]["tflops"],
+            "unit": "TFLOP/s (complex-algorithmic)", "steps": len(path), "peak_elements": peak,
+            "path_flops": flops, "modes": res, "data": "synthetic (seeded Gaussian C32, seed 4)"}
 
 
-def run_kernels(args):
+def run_kernels(args, ctx=None, stream=None):
     """Kernel rooflines outside the TEBD step: the permutation kernel on 1 GiB ComplexF64
     tensors (bytes = 2·numel·16, against the measured HBM copy rate) and the contraction
     GEMMs at 4096³ (C32 on the tcgen05 tensor pipe in TF32 and 3×TF32, counted as real
@@ -537,9 +687,10 @@ def run_kernels(args):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
     hbm, tf32 = peaks["hbm_gbs"], peaks["bf16_tflops"] / 2
-    ctx = tenetgb.Context(0)
-    stream = torch.cuda.Stream()
-    ctx.set_stream(stream.cuda_stream)
+    if ctx is None:
+        ctx = tenetgb.Context(0)
+        stream = torch.cuda.Stream()
+        ctx.set_stream(stream.cuda_stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def best(fn, reps=5):
@@ -599,8 +750,9 @@ def run_kernels(args):
             e.update({"tensor_tflops": real, "frac_tf32_peak": real / tf32})
         out["gemm"].append(e)
         del A, B, Cc
-    print(json.dumps({"metric": "kernel_rooflines", "hbm_peak_gbs": hbm, "tf32_dense_peak_tflops": tf32,
-                      "peak_source": "MEASURED_PEAKS.json (TF32 dense = BF16 / 2)", **out}))
+    return {"metric": "kernel_rooflines", "hbm_peak_gbs": hbm, "tf32_dense_peak_tflops": tf32,
+            "bf16_dense_peak_tflops": peaks["bf16_tflops"],
+            "peak_source": "MEASURED_PEAKS.json (TF32 dense = BF16 / 2)", **out}
 
 
 def batched_flops(Ls, chis, maxdims, d=2):
@@ -631,13 +783,13 @@ def batched_flops(Ls, chis, maxdims, d=2):
     return tot
 
 
-def run_batched(args):
+def run_batched(args, ctx=None):
     """Config 4: ragged batch of random MPS (L uniform in [16, 128], χ log-uniform in
     [16, 512], d=2, seed 5; the first --batched-sample of the 512-MPS population), each
     canonize!(ψ, MixedCanonical(L)) → compress!(ψ; maxdim = χ÷2) → norm(ψ), FP64.  The
     grouped path (one launch per kernel per sweep step over all instances) against the
-    per-instance device loop on the same data.  Prints one JSON line (a secondary
-    workload)."""
+    per-instance device loop on the first --batched-loop instances of the sample.
+    Returns one JSON-able dict (a secondary workload)."""
     import torch
 
     import tenetgb
@@ -648,8 +800,9 @@ def run_batched(args):
     n = args.batched_sample
     Ls, chis = Ls_all[:n], chis_all[:n]
     maxdim = [max(1, c // 2) for c in chis]
-    ctx = tenetgb.Context(0)
-    ctx.set_autotune(True)
+    if ctx is None:
+        ctx = tenetgb.Context(0)
+        ctx.set_autotune(True)
     g = MPSGroup.random(Ls, chis, seed=5, ctx=ctx)
     ctx.sync()
     init = [g.sites(b) for b in range(n)]
@@ -663,8 +816,9 @@ def run_batched(args):
             t0 = time.perf_counter()
             norms_g = g.canonize_compress_norm(maxdim)
             times_g.append(time.perf_counter() - t0)
+        nl = min(n, args.batched_loop)
         for rep in range(2):
-            psis = [tenetgb.MPS([a.copy() for a in init[b]], ctx=ctx) for b in range(n)]
+            psis = [tenetgb.MPS([a.copy() for a in init[b]], ctx=ctx) for b in range(nl)]
             ctx.sync()
             t0 = time.perf_counter()
             norms_p = []
@@ -676,6 +830,8 @@ def run_batched(args):
             del psis
     tg, tp = times_g[-1], times_p[-1]
     norms_p = np.array(norms_p)
+    # the grouped path restricted to the loop's instances, for a like-for-like speed-up
+    fl_loop = batched_flops(Ls[:nl], chis[:nl], maxdim[:nl])
     # CPU oracle on the smallest instances of the sample, ~20 s
     from oracle import tenet_oracle as O
 
@@ -690,23 +846,24 @@ def run_batched(args):
         spent += time.perf_counter() - t0
         done += 1
         fl_cpu += batched_flops([Ls[b]], [chis[b]], [maxdim[b]])
-        if spent > 20:
+        if spent > args.batched_cpu_s:
             break
-    print(json.dumps({
+    return {
         "metric": "batched_canonize_compress_norm_mps_per_s", "value": n / tg, "unit": "MPS/s",
         "higher_is_better": True, "dtype": "c128 (FP64)",
         "data": "synthetic (seeded Gaussian MPS generated on the device, seed 5)",
         "config": {"workload": "ragged_mps_L16to128_chi16to512_canonize_compress_half_norm",
                    "population": 512, "sample": n, "Ls": Ls, "chis": chis, "maxdim": "chi // 2"},
         "grouped": {"s": tg, "mps_per_s": n / tg, "tflops_algorithmic": flops / tg / 1e12},
-        "per_instance_loop": {"s": tp, "mps_per_s": n / tp, "tflops_algorithmic": flops / tp / 1e12},
-        "speedup_grouped_vs_loop": tp / tg,
-        "norm_max_rel_diff_grouped_vs_loop": float(np.max(np.abs(norms_g - norms_p) / norms_p)),
+        "per_instance_loop": {"instances": nl, "s": tp, "mps_per_s": nl / tp,
+                              "tflops_algorithmic": fl_loop / tp / 1e12},
+        "speedup_grouped_vs_loop_per_flop": (flops / tg) / (fl_loop / tp),
+        "norm_max_rel_diff_grouped_vs_loop": float(np.max(np.abs(norms_g[:nl] - norms_p) / norms_p)),
         "algorithmic_flops": flops, "clocks": sampler.summary(),
         "cpu_baseline": {"value": fl_cpu / spent / 1e12, "unit": "TFLOP/s (algorithmic)", "cores": os.cpu_count(),
                          "kind": "port", "sample": f"{done} smallest MPS of the sample through the oracle, "
                                                    f"{spent:.1f} s"},
-    }))
+    }
 
 
 SERVING_RATES = (100, 300, 1000, 3000, 5000)
@@ -743,7 +900,7 @@ def _serving_oracle_sample(srv, ids, spec, trace, budget_s=20.0):
     return done, spent
 
 
-def run_serving(args):
+def run_serving(args, rates=None):
     """Query serving on a device-resident pool: 16 random MPS (L in [8, 256], χ in
     {32, …, 1024}, d=2, seed 6), Poisson arrivals at each rate of SERVING_RATES (seed
     7+rate), 60 % amplitudes / 30 % ⟨O_i⟩ / 10 % overlaps, FP64.  For each rate: queries/s
@@ -774,7 +931,7 @@ def run_serving(args):
     per_rate = []
     sampler = ClockSampler(torch.cuda.current_device() if torch.cuda.is_available() else 0)
     with sampler:
-        for rate in SERVING_RATES:
+        for rate in (rates or SERVING_RATES):
             trace = W.serving_trace(pool_L, rate, args.queries, seed=7 + rate)
             tickets, t_sub = [], []
             start = time.perf_counter()
@@ -804,7 +961,7 @@ def run_serving(args):
     done, spent = _serving_oracle_sample(srv, ids, spec, cpu_trace)
     srv.close()
     best = max(per_rate, key=lambda e: e["qps"])
-    print(json.dumps({
+    return {
         "metric": "serving_queries_per_s", "value": best["qps"], "unit": "queries/s", "higher_is_better": True,
         "dtype": "c128 (FP64)" if args.serve_precision == "native" else
                  "c128 data; FP32 amplitude/overlap sweeps, FP64 <O_i> and results",
@@ -817,7 +974,7 @@ def run_serving(args):
         "cpu_baseline": {"value": done / spent, "unit": "queries/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": f"first {done} queries of the rate-100 trace, the reference's per-query "
                                    f"algorithms in numpy/LAPACK, {spent:.1f} s"},
-    }))
+    }
 
 
 def run_dmrg(args):
@@ -869,11 +1026,11 @@ def run_dmrg(args):
     sweeps_per_split = stats["svd_sweeps"] / max(1, stats["updates"])
     flops = sweeps_per_split * 255 * 128 * 32 * 256
     split_ms = stats["split_ms"] / max(1, stats["updates"])
-    peak = fp64_peak(ctx, stream, torch.device("cuda", 0))
+    peak = ctx.pipe_peak("fp64")
     achieved = flops / (split_ms * 1e-3) / 1e12
-    roofline = {"bound": "tensor", "kernel": "k_jacobi_coop<double> (FP64 pipe; latency-bound rounds)",
+    roofline = {"bound": "fp64_cuda_cores", "kernel": "k_jacobi_coop<double> (FP64 pipe; latency-bound rounds)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
-                "peak_source": "FP64 pipe measured in this run (own zgemm 2048^3); MEASURED_PEAKS.json has no FP64 entry",
+                "peak_source": "FP64 FMA rate of the CUDA cores measured in this run (tn_pipe_peak)",
                 "flops_per_launch": flops, "sweeps_per_split": sweeps_per_split, "launch_avg_ms": split_ms,
                 "phases_ms_per_step": {k: stats[k] for k in ("canonize_ms", "environments_ms", "eigsolve_ms",
                                                              "split_ms")}}
@@ -930,7 +1087,7 @@ def run_dmrg(args):
             per_call = json.load(f)["dmrg_notebook"]["dmrg2_product"]["energies_per_call"]
     except (OSError, KeyError, ValueError):
         per_call = None
-    print(json.dumps({
+    return {
         "metric": "dmrg2_sweeps_per_s_ising_n100_chi128", "value": 1e3 / ms, "unit": "sweeps/s", "n_gpus": 1,
         "steps": args.steps, "warmup": total - args.steps, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "replicas", "vs_baseline": None, "dtype": "c128 (FP64 GEMMs, Lanczos and Jacobi SVD)",
@@ -949,13 +1106,16 @@ def run_dmrg(args):
         "cpu_baseline": {"value": 1.0 / cpu_s, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": "oracle (numpy/LAPACK) on the same saturated MPS: environments + 40 of the 198 "
                                    "local updates of one dmrg!(ψ, H, 1) call, scaled to the call"},
-    }))
+    }
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--workload", default="tebd", choices=["tebd", "lattice", "serving", "kernels", "batched", "dmrg"])
-    ap.add_argument("--batched-sample", type=int, default=32, help="instances of the 512-MPS population (batched)")
+    ap.add_argument("--workload", default="tebd", choices=["tebd", "lattice", "serving", "kernels", "batched", "dmrg", "plain"])
+    ap.add_argument("--batched-sample", type=int, default=512, help="instances of the 512-MPS population (batched)")
+    ap.add_argument("--batched-loop", type=int, default=32, help="instances of the per-instance device loop (batched)")
+    ap.add_argument("--batched-cpu-s", type=float, default=20.0, help="oracle seconds on the smallest instances")
+    ap.add_argument("--quick", action="store_true", help="TEBD line only (no parity / secondary configs)")
     ap.add_argument("--queries", type=int, default=200, help="queries per arrival rate (serving)")
     ap.add_argument("--serve-budget-gb", type=float, default=200.0, help="HBM budget of the server (serving)")
     ap.add_argument("--serve-precision", default="native", choices=["native", "mixed"], help="serving arithmetic")
@@ -979,15 +1139,17 @@ def main():
     elif args.profile_dmrg:
         profile_dmrg(args)
     elif args.workload == "lattice":
-        run_lattice(args)
+        print(json.dumps(run_lattice(args)))
     elif args.workload == "serving":
-        run_serving(args)
+        print(json.dumps(run_serving(args)))
     elif args.workload == "kernels":
-        run_kernels(args)
+        print(json.dumps(run_kernels(args)))
     elif args.workload == "batched":
-        run_batched(args)
+        print(json.dumps(run_batched(args)))
     elif args.workload == "dmrg":
-        run_dmrg(args)
+        print(json.dumps(run_dmrg(args)))
+    elif args.workload == "plain":
+        print(json.dumps(run_plain_small(args)))
     elif args.impl == "reference":
         run_reference(args)
     else:

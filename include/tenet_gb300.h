@@ -51,8 +51,11 @@ typedef enum { TN_F32 = 0, TN_F64 = 1, TN_C32 = 2, TN_C64 = 3 } tn_dtype_t;
  *   (FP32-grade); C64 SVDs as an FP32 Jacobi pre-pass followed by FP64 Jacobi sweeps
  *   (FP64 is kept for the rotations, the truncation decision and norm/overlap
  *   accumulation); C64 GEMMs stay FP64.
- * TN_PREC_TF32: C32/F32 GEMMs as single-pass TF32 tensor-core products. */
-typedef enum { TN_PREC_NATIVE = 0, TN_PREC_MIXED = 1, TN_PREC_TF32 = 2 } tn_precision_t;
+ * TN_PREC_TF32: C32/F32 GEMMs as single-pass TF32 tensor-core products.
+ * TN_PREC_SPLIT_BF16: C64 GEMMs from exact BF16 digit planes on the tcgen05 tensor pipe
+ *   (tn_set_split_slices planes of 7 bits per operand, default 8: FP64-grade products);
+ *   factorisations as TN_PREC_NATIVE. */
+typedef enum { TN_PREC_NATIVE = 0, TN_PREC_MIXED = 1, TN_PREC_TF32 = 2, TN_PREC_SPLIT_BF16 = 3 } tn_precision_t;
 
 #define TN_MAX_RANK 16
 
@@ -79,6 +82,20 @@ tn_status_t tn_hbm_in_use(tn_ctx* ctx, size_t* bytes);
 tn_status_t tn_kernel_launches(tn_ctx* ctx, int64_t* count);
 const char* tn_last_error_string(tn_ctx* ctx);
 const char* tn_version(void);
+/* phase profiler: with enable != 0 the hot path brackets its phases by CUDA events on
+ * the context's stream (each Jacobi sweep, each GEMM launch, each QR factorisation) and
+ * tn_profile_read returns per class, since enabling: the kernel launches, the device
+ * time (ms) and the algorithmic flops and bytes.  Classes: 0 Jacobi sweeps FP32, 1 Jacobi
+ * sweeps FP64, 2 complex FP64 GEMM, 3 split-BF16 tensor-core GEMM (flops = the BF16
+ * tensor-pipe products it issues), 4 its digit-plane preparation, 5 Householder QR,
+ * 6 cooperative small-matrix Jacobi.  Enabling (or disabling) resets the totals. */
+tn_status_t tn_profile_enable(tn_ctx* ctx, int32_t enable);
+tn_status_t tn_profile_read(tn_ctx* ctx, int32_t cls, int64_t* launches, double* ms, double* flops,
+                            double* bytes);
+/* measured fused multiply-add rate of the CUDA cores (TFLOP/s): which 0 = FP32, 1 = FP64
+ * (a register-resident FMA loop over every SM; the roofline denominator of CUDA-core
+ * kernels) */
+tn_status_t tn_pipe_peak(tn_ctx* ctx, int32_t which, double* tflops);
 /* autotuner: with enable != 0 the first call of an unseen shape bucket times the
  * candidate launch configurations (QR panel and slab widths) and records the fastest.
  * tn_tuning_dump writes the table as text ("key v1 v2" lines; *needed = bytes incl. the
@@ -108,6 +125,12 @@ tn_status_t tn_gemm(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, char opa
                     int64_t lda, int64_t strideA, const void* d_B, int64_t ldb,
                     int64_t strideB, const double* beta, void* d_C, int64_t ldc,
                     int64_t strideC, int64_t batch);
+
+/* digit planes per operand of the TN_PREC_SPLIT_BF16 (and mixed C64) GEMMs, 2..8
+ * (default 8): each plane carries 7 bits (8 for short contractions), so the products'
+ * relative error is ~2^(-7·slices), and the tensor-pipe work grows as slices·(slices+1)/2
+ * BF16 products.  Contractions longer than 4096/slices real terms run in chunks. */
+tn_status_t tn_set_split_slices(tn_ctx* ctx, int32_t slices);
 
 /* ------------------------------------------------------------------------------------
  * Muscle.binary_einsum(a, b; dims) on dense column-major tensors with integer mode
@@ -162,6 +185,32 @@ tn_status_t tn_svd_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int6
  * Errors: tn_last_error_string(NULL). */
 tn_status_t tn_svd_thin_noalloc(void* stream, int64_t m, int64_t n, const void* d_A, int64_t lda,
                                 void* d_U, double* d_S, void* d_Vh);
+
+/* ------------------------------------------------------------------------------------
+ * Mode-labelled factorisations, the form the Julia binding of Muscle calls:
+ *
+ * Muscle.tensor_qr_thin(A; inds_q, inds_r, ind_virtual) (src/Operations/canonize.jl:58):
+ * A is matricised as (q_modes…) × (its other modes, in A's order), factorised, and Q, R
+ * come back as labelled tensors Q (q_modes…, virtual_mode), R (virtual_mode, others…).
+ * Q->data / R->data are caller buffers of ≥ m·k and k·n elements (k = min(m, n)); the
+ * library fills rank, dims and modes.
+ *
+ * Muscle.tensor_svd_thin(A; inds_u, inds_v, ind_s) (src/Operations/canonize.jl:41,97),
+ * with compress!'s truncation (src/Operations/compress.jl:47-59) applied to the result:
+ * keep min(maxdim, k) values (maxdim <= 0: no cap), then those with |s| > abs_threshold
+ * (abs_threshold <= 0: none), at least one; *rank_out = the kept rank r.  U (u_modes…,
+ * s_mode) holds the first r left vectors, d_S the r values (FP64, descending), Vh
+ * (s_mode, others…) the first r right vectors, compacted (leading dimension r).  Buffers
+ * as for the QR with k columns / rows.  Both: C64 or C32; TN_EINVAL when a label is
+ * missing, repeated or the new mode is already used.
+ * ---------------------------------------------------------------------------------- */
+tn_status_t tn_tensor_qr_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, const tn_tensor* A,
+                              int32_t n_q, const int32_t* q_modes, int32_t virtual_mode, tn_tensor* Q,
+                              tn_tensor* R);
+tn_status_t tn_tensor_svd_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, const tn_tensor* A,
+                               int32_t n_u, const int32_t* u_modes, int32_t s_mode, int64_t maxdim,
+                               double abs_threshold, tn_tensor* U, double* d_S, tn_tensor* Vh,
+                               int64_t* rank_out);
 
 /* diagnostics of the last SVD on this context: Jacobi sweeps run in FP32 (mixed
  * pre-pass) and in FP64 (-1: the one-CTA shared-memory kernel ran all sweeps), and the

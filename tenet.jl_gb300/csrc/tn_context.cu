@@ -62,6 +62,11 @@ tn_status_t ws_reserve(tn_ctx* ctx, size_t bytes) {
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
   ctx->graphs.clear();
+  for (auto& r : ctx->prof_recs) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
   if (ctx->ws) TN_RETURN_IF(tn_dev_free(ctx, ctx->ws));
   ctx->ws = nullptr;
   ctx->ws_cap = 0;
@@ -137,6 +142,11 @@ void ctx_release(tn_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
   ctx->graphs.clear();
+  for (auto& r : ctx->prof_recs) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
   for (auto& kv : ctx->allocs) cudaFree(kv.first);
   ctx->allocs.clear();
   if (ctx->pinned) cudaFreeHost(ctx->pinned);

@@ -113,9 +113,15 @@ tn_status_t launch(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64_
                    cx<T> beta, cx<T>* C, int64_t ldc, int64_t sC, int64_t batch, bool upper = false) {
   dim3 grid(cdiv(m, BM), cdiv(n, BN), (unsigned)(batch < 65535 ? batch : 65535));
   if (grid.x > 0x7fffffffu || grid.y > 65535u) return tn_set_error(ctx, TN_EINVAL, "gemm: grid too large");
+  const int slot = sizeof(T) == 8 ? prof_begin(ctx) : -1;
   k_gemm_cx<T, BM, BN, BK, TM, TN><<<grid, (BM / TM) * (BN / TN), 0, ctx->stream>>>(
       opa, opb, m, n, k, alpha, A, lda, sA, B, ldb, sB, beta, C, ldc, sC, batch, upper);
   TN_LAUNCHED(ctx);
+  if (slot >= 0) {
+    const bool b0 = beta.x == T(0) && beta.y == T(0);
+    prof_end(ctx, slot, TN_PROF_GEMM_F64, 1, 8.0 * m * n * k * batch,
+             sizeof(cx<T>) * ((double)m * k + (double)k * n + (double)m * n * (b0 ? 1 : 2)) * batch);
+  }
   return TN_OK;
 }
 
@@ -252,12 +258,6 @@ static tn_status_t gemm_re(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n
   return TN_OK;
 }
 
-// split-precision tensor-core path (defined in tn_gemm_tc.cu)
-tn_status_t gemm_mixed_c64(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64_t k,
-                           cxd alpha, const cxd* A, int64_t lda, int64_t sA, const cxd* B,
-                           int64_t ldb, int64_t sB, cxd beta, cxd* C, int64_t ldc, int64_t sC,
-                           int64_t batch);
-
 static bool valid_op(char c) { return c == 'N' || c == 'T' || c == 'C'; }
 
 // The tensor path pays an operand-preparation pass (split + 4M expansion) and 128×128
@@ -295,11 +295,8 @@ tn_status_t gemm_any(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, char op
   switch (dtype) {
     case TN_C64: {
       cxd a = mkcx(alpha[0], alpha[1]), b = mkcx(beta[0], beta[1]);
-      if (prec == TN_PREC_MIXED)
-        return gemm_mixed_c64(ctx, opa, opb, m, n, k, a, (const cxd*)A, lda, strideA, (const cxd*)B, ldb, strideB, b,
-                              (cxd*)C, ldc, strideC, batch);
-      return gemm_cx<double>(ctx, opa, opb, m, n, k, a, (const cxd*)A, lda, strideA, (const cxd*)B, ldb, strideB, b,
-                             (cxd*)C, ldc, strideC, batch);
+      return gemm_c64(ctx, prec, opa, opb, m, n, k, a, (const cxd*)A, lda, strideA, (const cxd*)B, ldb, strideB, b,
+                      (cxd*)C, ldc, strideC, batch);
     }
     case TN_C32: {
       cxf a = mkcx((float)alpha[0], (float)alpha[1]), b = mkcx((float)beta[0], (float)beta[1]);
@@ -331,6 +328,7 @@ extern "C" tn_status_t tn_gemm(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t pre
   TN_ARG(ctx, lda >= (ra > 1 ? ra : 1) && ldb >= (rb > 1 ? rb : 1) && ldc >= (m > 1 ? m : 1),
          "tn_gemm: leading dimension too small");
   TN_RETURN_IF(ws_reserve(ctx, gemm_any_workspace(dtype, prec, m, n, k)));
-  return gemm_any(ctx, dtype, prec, opa, opb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc, strideC,
-                  batch);
+  TN_RETURN_IF(gemm_any(ctx, dtype, prec, opa, opb, m, n, k, alpha, A, lda, strideA, B, ldb, strideB, beta, C, ldc,
+                        strideC, batch));
+  return split_gemm_check(ctx);
 }

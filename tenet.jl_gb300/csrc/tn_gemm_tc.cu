@@ -304,23 +304,7 @@ __global__ void k_prep_re(int64_t R, int64_t K, int64_t Kp, const float* X, int6
   }
 }
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn(tn_ctx* ctx) {
-  static EncodeTiledFn fn = nullptr;
-  if (fn) return fn;
-  void* p = nullptr;
-  cudaDriverEntryPointQueryResult q;
-  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-      q != cudaDriverEntryPointSuccess || !p) {
-    tn_set_error(ctx, TN_ECUDA, "cuTensorMapEncodeTiled unavailable");
-    return nullptr;
-  }
-  fn = (EncodeTiledFn)p;
-  return fn;
-}
+EncodeTiledFn encode_fn(tn_ctx* ctx) { return tn_encode_tiled_fn(ctx); }
 
 // K-major operand: rows × Kp floats, row pitch Kp·4 bytes; box 32 floats × box_rows
 tn_status_t make_map(tn_ctx* ctx, CUtensorMap* map, const float* base, int64_t rows, int64_t Kp, uint32_t box_rows) {
@@ -344,6 +328,21 @@ unsigned blocks_for(tn_ctx* ctx, int64_t n) {
 }
 
 }  // namespace
+
+// the driver's cuTensorMapEncodeTiled, looked up once through the runtime
+EncodeTiledFn tn_encode_tiled_fn(tn_ctx* ctx) {
+  static EncodeTiledFn fn = nullptr;
+  if (fn) return fn;
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !p) {
+    tn_set_error(ctx, TN_ECUDA, "cuTensorMapEncodeTiled unavailable");
+    return nullptr;
+  }
+  fn = (EncodeTiledFn)p;
+  return fn;
+}
 
 // Workspace (bytes) for tc_gemm on the given shape.
 // K-major operands are stored with K padded to a multiple of 4 floats (the 16-byte TMA
@@ -427,13 +426,4 @@ tn_status_t tc_gemm(tn_ctx* ctx, bool complex_in, int passes, char opa, char opb
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (hp[0]) return tn_set_error(ctx, TN_ETIMEOUT, "tc_gemm: a pipeline wait timed out");
   return TN_OK;
-}
-
-tn_status_t gemm_mixed_c64(tn_ctx* ctx, char opa, char opb, int64_t m, int64_t n, int64_t k, cxd alpha, const cxd* A,
-                           int64_t lda, int64_t sA, const cxd* B, int64_t ldb, int64_t sB, cxd beta, cxd* C,
-                           int64_t ldc, int64_t sC, int64_t batch) {
-  (void)opa; (void)opb; (void)m; (void)n; (void)k; (void)alpha; (void)A; (void)lda; (void)sA; (void)B; (void)ldb;
-  (void)sB; (void)beta; (void)C; (void)ldc; (void)sC; (void)batch;
-  return tn_set_error(ctx, TN_EUNSUPPORTED,
-                      "C64 contractions stay FP64: split-TF32 products are FP32-grade (use C32 data for the tensor path)");
 }

@@ -179,11 +179,46 @@ struct tn_ctx {
   double dmrg_ms[4] = {0, 0, 0, 0};
   int64_t dmrg_updates = 0;
   int64_t dmrg_svd_sweeps = 0;  // Jacobi sweeps summed over the pair splits
+  // phase profiler (tn_profile_*): event pairs around hot-path phases, resolved on read
+  bool prof_on = false;
+  struct prof_rec {
+    int cls;
+    cudaEvent_t a, b;
+    int64_t launches;
+    double flops, bytes;
+  };
+  std::vector<prof_rec> prof_recs;
+  std::vector<cudaEvent_t> prof_pool;
+  int64_t prof_launches[16] = {0};
+  double prof_ms[16] = {0}, prof_flops[16] = {0}, prof_bytes[16] = {0};
+  // split-BF16 GEMM: digit planes per operand, its operand-plane scratch and error word
+  int split_slices = 8;
+  char* oz_ws = nullptr;
+  size_t oz_cap = 0;
+  int* oz_err = nullptr;
   // autotuned launch parameters, keyed by kernel family + shape bucket
   bool autotune = false;
   std::unordered_map<std::string, std::pair<int, int>> tuning;
 };
 void ctx_release(tn_ctx* ctx);  // frees the context (called when refs drop to 0)
+
+// ---------------------------------------------------------------------------------
+// phase profiler: classes of hot-path work timed by CUDA events on the context stream
+// (tn_profile_enable / tn_profile_read).  prof_begin returns a slot (-1 when profiling
+// is off); prof_end records the closing event with the work done in between.
+// ---------------------------------------------------------------------------------
+enum {
+  TN_PROF_JACOBI_F32 = 0,   // one-sided Jacobi sweeps, FP32 (k_jacobi_step_reg<float>)
+  TN_PROF_JACOBI_F64 = 1,   // one-sided Jacobi sweeps, FP64 (k_jacobi_step_reg<double>)
+  TN_PROF_GEMM_F64 = 2,     // complex FP64 CUDA-core GEMM (k_gemm_cx<double>)
+  TN_PROF_GEMM_SPLIT = 3,   // split-BF16 tensor-core GEMM kernel (k_gemm_oz)
+  TN_PROF_SPLIT_PREP = 4,   // its digit-plane preparation
+  TN_PROF_QR = 5,           // blocked Householder QR (panel + block reflector)
+  TN_PROF_JACOBI_COOP = 6,  // cooperative small-matrix Jacobi (whole iteration)
+  TN_PROF_NCLASS = 7
+};
+int prof_begin(tn_ctx* ctx);
+void prof_end(tn_ctx* ctx, int slot, int cls, int64_t launches, double flops, double bytes);
 
 tn_status_t tn_set_error(tn_ctx* ctx, tn_status_t st, const char* fmt, ...);
 
@@ -319,6 +354,31 @@ size_t gemm_any_workspace(tn_dtype_t dt, tn_precision_t prec, int64_t m, int64_t
 tn_status_t gemm_any(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, char opa, char opb, int64_t m, int64_t n,
                      int64_t k, const double* alpha, const void* A, int64_t lda, int64_t sA, const void* B, int64_t ldb,
                      int64_t sB, const double* beta, void* C, int64_t ldc, int64_t sC, int64_t batch);
+// the driver's cuTensorMapEncodeTiled (resolved once through the runtime; null with the
+// context's error set when unavailable).  Needs <cuda.h> for the CUtensorMap types.
+#ifdef CUDA_VERSION
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn tn_encode_tiled_fn(tn_ctx* ctx);
+#endif
+// Ozaki-style split-BF16 complex FP64 GEMM on the tcgen05 tensor pipe (tn_gemm_oz.cu):
+// C = alpha op(A) op(B) + beta C with every operand cut into `slices` exact BF16 digit
+// planes; FP64-grade (the error is set by the slice count).  Its operand planes live in
+// a context scratch of their own (grown between calls), so callers reserve nothing.
+constexpr int kSplitSlicesDefault = 8;
+tn_status_t gemm_c64_split(tn_ctx* ctx, int slices, char opa, char opb, int64_t m, int64_t n, int64_t k, cxd alpha,
+                           const cxd* A, int64_t lda, int64_t sA, const cxd* B, int64_t ldb, int64_t sB, cxd beta,
+                           cxd* C, int64_t ldc, int64_t sC, int64_t batch);
+// reads (and clears) the split GEMMs' error word after draining the stream: TN_ETIMEOUT
+// when a pipeline wait ran out since the last check
+tn_status_t split_gemm_check(tn_ctx* ctx);
+// ComplexF64 GEMM in the arithmetic `prec` asks for: the split-BF16 tensor path for
+// TN_PREC_MIXED / TN_PREC_SPLIT_BF16 on shapes large enough to pay for it, else the FP64
+// CUDA-core kernel
+tn_status_t gemm_c64(tn_ctx* ctx, tn_precision_t prec, char opa, char opb, int64_t m, int64_t n, int64_t k, cxd alpha,
+                     const cxd* A, int64_t lda, int64_t sA, const cxd* B, int64_t ldb, int64_t sB, cxd beta, cxd* C,
+                     int64_t ldc, int64_t sC, int64_t batch);
 // tcgen05 TF32 GEMM (tn_gemm_tc.cu)
 size_t tc_gemm_workspace(bool complex_in, int passes, int64_t m, int64_t n, int64_t k);
 tn_status_t tc_gemm(tn_ctx* ctx, bool complex_in, int passes, char opa, char opb, int64_t m, int64_t n, int64_t k,

@@ -122,8 +122,8 @@ tn_status_t gauge_right(tn_mps* p, int i, bool svd_lambda) {
   } else {
     TN_RETURN_IF(qr_cx<double>(ctx, m, n, p->site[i], m, p->cap[i], p->site[i], p->cap[i], R, k * n, B));
   }
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k, nbc, n, kOne, R, k, k * n, p->site[i + 1], n, p->cap[i + 1], kZero, tmp,
-                               k, k * nbc, B));
+  TN_RETURN_IF(gemm_c64(ctx, p->prec, 'N', 'N', k, nbc, n, kOne, R, k, k * n, p->site[i + 1], n, p->cap[i + 1], kZero,
+                        tmp, k, k * nbc, B));
   TN_RETURN_IF(ensure_site(p, i + 1, (size_t)(k * nbc)));
   TN_RETURN_IF(copy_instances(ctx, p->site[i + 1], p->cap[i + 1], tmp, k * nbc, k * nbc, B));
   p->bond[i] = k;
@@ -157,8 +157,8 @@ tn_status_t gauge_left(tn_mps* p, int i, bool svd_lambda) {
   // new site i = Qᴴ (k × d χ_r)
   TN_RETURN_IF(transpose_cx<double>(ctx, m, k, Q, m, m * n, p->site[i], k, p->cap[i], B, true));
   // site i-1 ← B · Rᴴ
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'C', rows_b, k, n, kOne, p->site[i - 1], rows_b, p->cap[i - 1], R, k, k * n,
-                               kZero, tmp, rows_b, rows_b * k, B));
+  TN_RETURN_IF(gemm_c64(ctx, p->prec, 'N', 'C', rows_b, k, n, kOne, p->site[i - 1], rows_b, p->cap[i - 1], R, k, k * n,
+                        kZero, tmp, rows_b, rows_b * k, B));
   TN_RETURN_IF(ensure_site(p, i - 1, (size_t)(rows_b * k)));
   TN_RETURN_IF(copy_instances(ctx, p->site[i - 1], p->cap[i - 1], tmp, rows_b * k, rows_b * k, B));
   p->bond[i - 1] = k;
@@ -300,7 +300,7 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
   double* S = ws_take<double>(ctx, (size_t)(batch * k));
   cxd* Vh = ws_take<cxd>(ctx, (size_t)(batch * k * n));
   // θ0 = A (χl d1 × χm) · B (χm × d2 χr)
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, chm, kOne, A, m, sA, Bm, chm, sB, kZero, th0, m, m * n, batch));
+  TN_RETURN_IF(gemm_c64(ctx, prec, 'N', 'N', m, n, chm, kOne, A, m, sA, Bm, chm, sB, kZero, th0, m, m * n, batch));
   // θ[l, (a b), r] = Σ G[(a b), (a' b')] θ0[l, (a' b'), r] — batched over (r, instance),
   // which are contiguous blocks of chl·dd elements
   TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, dd, dd, kOne, th0, chl, chl * dd, dG, dd, 0, kZero, th, chl,
@@ -311,6 +311,7 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
     TN_RETURN_IF(svd_any(ctx, TN_C64, prec, m, n, th, m, m * n, U, m * k, S, k, Vh, k * n, batch));
   int64_t r = 0;
   TN_RETURN_IF(rank_select_batched(ctx, S, k, k, batch, maxdim, threshold, &r, nullptr));
+  if (prec != TN_PREC_NATIVE) TN_RETURN_IF(split_gemm_check(ctx));  // the stream has drained: one word
   cxd *Aout = nullptr, *Bout = nullptr;
   int64_t sAo = 0, sBo = 0;
   TN_RETURN_IF(out_fn(out_arg, r, &Aout, &sAo, &Bout, &sBo));
@@ -319,7 +320,7 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
   TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
   if (left_only) {
     // B' = diag(1/√s) U[:, :r]ᴴ θ
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
+    TN_RETURN_IF(gemm_c64(ctx, prec, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
     TN_RETURN_IF(scale_rows_invsqrt(ctx, Bout, r, n, r, S, sBo, k, batch));
   } else {
     // B' = √S Vh[:r, :]

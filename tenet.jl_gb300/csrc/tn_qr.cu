@@ -363,7 +363,16 @@ tn_status_t qr_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda
     cudaEventDestroy(e1);
     ctx->tuning[key] = {nb, slab};
   }
-  return qr_run<T>(ctx, nb, slab, m, n, A, lda, sA, Q, sQ, R, sR, batch, W, tau, Tm);
+  const int slot = prof_begin(ctx);
+  const int64_t l0 = ctx->launches;
+  TN_RETURN_IF(qr_run<T>(ctx, nb, slab, m, n, A, lda, sA, Q, sQ, R, sR, batch, W, tau, Tm));
+  if (slot >= 0) {
+    // geqrf + forming Q: 2 × 4·(2mk² − ⅔k³)·… (LAWN 41, ×4 complex); A read, Q and R written
+    const double kk = (double)k, f = 4.0 * (2.0 * m * kk * kk - 2.0 / 3.0 * kk * kk * kk);
+    prof_end(ctx, slot, TN_PROF_QR, ctx->launches - l0, 2.0 * f * batch,
+             sizeof(cx<T>) * ((double)m * n + (double)m * k + (double)k * n) * batch);
+  }
+  return TN_OK;
 }
 template tn_status_t qr_cx<double>(tn_ctx*, int64_t, int64_t, const cxd*, int64_t, int64_t, cxd*, int64_t, cxd*,
                                    int64_t, int64_t);

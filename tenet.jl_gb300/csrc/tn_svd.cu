@@ -1051,7 +1051,16 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
     const int64_t min_rot = (int64_t)(min_rot_frac * (double)pairs);
     int n_active = (int)batch;
     for (sweeps = 0; sweeps < max_sweeps && n_active > 0; ++sweeps) {
+      const int slot = prof_begin(ctx);
       TN_CHECK_CUDA(ctx, cudaGraphLaunch(ge, ctx->stream));
+      if (slot >= 0) {
+        // per round, every pair of every active matrix: wᵢᴴwⱼ (8m) + the two rotated
+        // columns of W (24m) [+ of V (24n)]; W [and V] read and written once
+        const double rounds = (double)(N - 1), act = (double)n_active;
+        const double flops = rounds * act * (N / 2) * (32.0 * m + (V ? 24.0 * n : 0.0));
+        const double bytes = rounds * act * 2.0 * sizeof(cx<T>) * ((double)m * n + (V ? (double)n * n : 0.0));
+        prof_end(ctx, slot, sizeof(T) == 4 ? TN_PROF_JACOBI_F32 : TN_PROF_JACOBI_F64, N - 1, flops, bytes);
+      }
       ctx->launches += N + 1;  // norm refresh, ‖A‖_F, N-1 steps
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * 2 * batch, cudaMemcpyDeviceToHost,
                                          ctx->stream));
@@ -1286,7 +1295,10 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   //   V ← V (I − E/2 + 3E²/8 − 5E³/16)   (the (I + E)^{-1/2} series; residual ~ (35/128)E⁴)
   // FP32 rotation accumulation leaves |E| ~ 1e-4, so E² and E³ need only ~1e-4 relative
   // accuracy: both are FP32 GEMMs.
-  TN_RETURN_IF(herk_cx<double>(ctx, n, n, V64, n, n * n, G, n, n * n, batch));
+  // the Gram matrix, V·(…) and W = A·V below are split-BF16 tensor-core GEMMs
+  // (FP64-grade products; rotations, norms and the stop test stay FP64)
+  TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'C', 'N', n, n, n, mkcx(1.0, 0.0), V64, n, n * n, V64, n, n * n,
+                        mkcx(0.0, 0.0), G, n, n * n, batch));
   {
     const int64_t cnt = n * n * batch;
     const unsigned blocks = (unsigned)std::min<int64_t>((cnt + 255) / 256, 4096);
@@ -1307,14 +1319,14 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
     k_ortho_poly<<<blocks, 256, 0, ctx->stream>>>(n, batch, G, E2, E3, (E3 == W32 + n * n) ? sE : n * n);
     TN_LAUNCHED(ctx);
   }
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', n, n, n, mkcx(1.0, 0.0), V64, n, n * n, G, n, n * n, mkcx(0.0, 0.0), V,
-                               n, sV, batch));
+  TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', n, n, n, mkcx(1.0, 0.0), V64, n, n * n, G, n, n * n,
+                        mkcx(0.0, 0.0), V, n, sV, batch));
   for (int64_t b = 0; b < batch; ++b)
     TN_CHECK_CUDA(ctx, cudaMemcpyAsync(V64 + b * n * n, V + b * sV, sizeof(cxd) * n * n, cudaMemcpyDeviceToDevice,
                                        ctx->stream));
   // W = A V  (FP64)
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', m, n, n, mkcx(1.0, 0.0), A, lda, sA, V64, n, n * n, mkcx(0.0, 0.0), W64,
-                               m, m * n, batch));
+  TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, mkcx(1.0, 0.0), A, lda, sA, V64, n, n * n,
+                        mkcx(0.0, 0.0), W64, m, m * n, batch));
   TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W64, want_v ? V64 : nullptr, batch, true, active, rotated, nrm64,
                                     kMaxSweeps, nullptr, &noconv, (keep_m > 0 && keep_m < n) ? tail : nullptr, keep_m,
                                     true));

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libtenetgb.so")
 
 TN_OK, TN_EINVAL, TN_ENOMEM, TN_ENOCONV, TN_ETIMEOUT, TN_ECUDA, TN_EUNSUPPORTED = range(7)
 TN_F32, TN_F64, TN_C32, TN_C64 = range(4)
-TN_PREC_NATIVE, TN_PREC_MIXED, TN_PREC_TF32 = 0, 1, 2
+TN_PREC_NATIVE, TN_PREC_MIXED, TN_PREC_TF32, TN_PREC_SPLIT_BF16 = 0, 1, 2, 3
 TN_FORM_NONCANONICAL, TN_FORM_MIXED, TN_FORM_BOND = 0, 1, 2
 TN_MAX_RANK = 16
 
@@ -83,6 +83,12 @@ SIGNATURES = {
     "tn_last_error_string": (C.c_char_p, [_vp]),
     "tn_version": (C.c_char_p, []),
     "tn_set_autotune": (_st, [_vp, _i32]),
+    "tn_set_split_slices": (_st, [_vp, _i32]),
+    "tn_tensor_qr_thin": (_st, [_vp, _i32, _i32, _vp, _i32, _vp, _i32, _vp, _vp]),
+    "tn_tensor_svd_thin": (_st, [_vp, _i32, _i32, _vp, _i32, _vp, _i32, _i64, C.c_double, _vp, _vp, _vp, _vp]),
+    "tn_profile_enable": (_st, [_vp, _i32]),
+    "tn_profile_read": (_st, [_vp, _i32, _vp, _vp, _vp, _vp]),
+    "tn_pipe_peak": (_st, [_vp, _i32, _vp]),
     "tn_tuning_dump": (_st, [_vp, C.c_char_p, _sz, C.POINTER(_sz)]),
     "tn_tuning_load": (_st, [_vp, C.c_char_p]),
     "tn_permute": (_st, [_vp, C.c_int, _i32, _pi64, _pi64, _pi32, _vp, _vp, _i32]),

@@ -34,7 +34,7 @@ _DT = {
     np.dtype(np.float32): L.TN_F32,
 }
 _PREC = {"native": L.TN_PREC_NATIVE, "fp64": L.TN_PREC_NATIVE, "fp32": L.TN_PREC_NATIVE, "mixed": L.TN_PREC_MIXED,
-         "3xtf32": L.TN_PREC_MIXED, "tf32": L.TN_PREC_TF32}
+         "3xtf32": L.TN_PREC_MIXED, "tf32": L.TN_PREC_TF32, "split_bf16": L.TN_PREC_SPLIT_BF16}
 
 
 def precision_code(p):
@@ -43,7 +43,7 @@ def precision_code(p):
     try:
         return _PREC[p]
     except KeyError:
-        raise ValueError(f"unknown precision {p!r}; use 'native' or 'mixed'") from None
+        raise ValueError(f"unknown precision {p!r}; use 'native', 'mixed' or 'split_bf16'") from None
 
 
 class Context:
@@ -130,6 +130,32 @@ class Context:
     def launches(self):
         v = C.c_int64()
         self.check(self.lib.tn_kernel_launches(self.h, C.byref(v)))
+        return v.value
+
+    def set_split_slices(self, slices):
+        """Digit planes per operand of the split-BF16 C64 GEMMs (2…8, default 8)."""
+        self.check(self.lib.tn_set_split_slices(self.h, int(slices)))
+
+    PROFILE_CLASSES = ("jacobi_fp32", "jacobi_fp64", "gemm_fp64", "gemm_split_bf16", "split_prep", "qr",
+                       "jacobi_coop")
+
+    def profile(self, enable=True):
+        """Time the hot-path phases by CUDA events on the context stream (resets the totals)."""
+        self.check(self.lib.tn_profile_enable(self.h, int(bool(enable))))
+
+    def profile_read(self):
+        """{class: {launches, ms, flops, bytes}} since profiling was enabled."""
+        out = {}
+        for i, name in enumerate(self.PROFILE_CLASSES):
+            n, ms, fl, by = C.c_int64(), C.c_double(), C.c_double(), C.c_double()
+            self.check(self.lib.tn_profile_read(self.h, i, C.byref(n), C.byref(ms), C.byref(fl), C.byref(by)))
+            out[name] = {"launches": n.value, "ms": ms.value, "flops": fl.value, "bytes": by.value}
+        return out
+
+    def pipe_peak(self, which):
+        """Measured FMA rate of the CUDA cores in TFLOP/s: which = "fp32" or "fp64"."""
+        v = C.c_double()
+        self.check(self.lib.tn_pipe_peak(self.h, {"fp32": 0, "fp64": 1}[which], C.byref(v)))
         return v.value
 
 
@@ -264,35 +290,70 @@ def _as_matrix(t, row_inds, col_inds):
     return mt, m, n
 
 
+def _labelled_modes(A, left, new_label):
+    """Integer modes for A's labels (by position) plus one for the new label."""
+    ids = {lab: k for k, lab in enumerate(A.inds)}
+    if new_label in ids:
+        raise ValueError(f"label {new_label!r} is already an index of the tensor")
+    ids[new_label] = len(ids)
+    for lab in left:
+        if lab not in ids or lab == new_label:
+            raise ValueError(f"label {lab!r} is not an index of the tensor")
+    return ids
+
+
 def tensor_qr_thin(A: DeviceTensor, inds_q, inds_r=None, ind_virtual="_qr", precision="native"):
-    """Muscle.tensor_qr_thin: Q carries (inds_q…, ind_virtual), R (ind_virtual, inds_r…)."""
+    """Muscle.tensor_qr_thin (tn_tensor_qr_thin): Q carries (inds_q…, ind_virtual),
+    R (ind_virtual, inds_r…); inds_r defaults to A's other labels in A's order."""
     inds_q = list(inds_q)
-    inds_r = [i for i in A.inds if i not in inds_q] if inds_r is None else list(inds_r)
-    mt, m, n = _as_matrix(A, inds_q, inds_r)
+    rest = [i for i in A.inds if i not in inds_q]
+    if inds_r is not None and sorted(map(str, inds_r)) != sorted(map(str, rest)):
+        raise ValueError("inds_q and inds_r must partition the tensor's labels")
+    ids = _labelled_modes(A, inds_q, ind_virtual)
+    m = int(np.prod([A.dim(i) for i in inds_q], dtype=np.int64)) if inds_q else 1
+    n = int(np.prod([A.dim(i) for i in rest], dtype=np.int64)) if rest else 1
     k = min(m, n)
     Q = DeviceTensor(A.ctx, [A.dim(i) for i in inds_q] + [k], A.dtype, inds_q + [ind_virtual])
-    R = DeviceTensor(A.ctx, [k] + [A.dim(i) for i in inds_r], A.dtype, [ind_virtual] + inds_r)
-    A.ctx.check(
-        A.ctx.lib.tn_qr_thin(A.ctx.h, A.code, precision_code(precision), m, n, C.c_void_p(mt.ptr), max(m, 1), 0,
-                             C.c_void_p(Q.ptr), 0, C.c_void_p(R.ptr), 0, 1)
-    )
+    R = DeviceTensor(A.ctx, [k] + [A.dim(i) for i in rest], A.dtype, [ind_virtual] + rest)
+    qm = (C.c_int32 * max(1, len(inds_q)))(*[ids[i] for i in inds_q])
+    da, dq, dr = _desc(A, ids), _desc(Q, ids), _desc(R, ids)
+    A.ctx.check(A.ctx.lib.tn_tensor_qr_thin(A.ctx.h, A.code, precision_code(precision), C.byref(da), len(inds_q), qm,
+                                            ids[ind_virtual], C.byref(dq), C.byref(dr)))
+    if inds_r is not None and list(inds_r) != rest:
+        R = permute(R, [ind_virtual] + list(inds_r))
     return Q, R
 
 
-def tensor_svd_thin(A: DeviceTensor, inds_u, inds_v=None, ind_s="_svd", precision="native"):
-    """Muscle.tensor_svd_thin: U (inds_u…, ind_s), s (ind_s) real FP64 descending,
-    V (ind_s, inds_v…) with A = U·diag(s)·V."""
+def tensor_svd_thin(A: DeviceTensor, inds_u, inds_v=None, ind_s="_svd", precision="native", maxdim=None,
+                    threshold=None):
+    """Muscle.tensor_svd_thin (tn_tensor_svd_thin): U (inds_u…, ind_s), s (ind_s) real
+    FP64 descending, V (ind_s, inds_v…) with A = U·diag(s)·V.  ``maxdim`` / ``threshold``
+    truncate like compress! (keep ≤ maxdim, then |s| > threshold, at least one)."""
     inds_u = list(inds_u)
-    inds_v = [i for i in A.inds if i not in inds_u] if inds_v is None else list(inds_v)
-    mt, m, n = _as_matrix(A, inds_u, inds_v)
+    rest = [i for i in A.inds if i not in inds_u]
+    if inds_v is not None and sorted(map(str, inds_v)) != sorted(map(str, rest)):
+        raise ValueError("inds_u and inds_v must partition the tensor's labels")
+    ids = _labelled_modes(A, inds_u, ind_s)
+    m = int(np.prod([A.dim(i) for i in inds_u], dtype=np.int64)) if inds_u else 1
+    n = int(np.prod([A.dim(i) for i in rest], dtype=np.int64)) if rest else 1
     k = min(m, n)
     U = DeviceTensor(A.ctx, [A.dim(i) for i in inds_u] + [k], A.dtype, inds_u + [ind_s])
     s = DeviceTensor(A.ctx, [k], np.float64, [ind_s])
-    V = DeviceTensor(A.ctx, [k] + [A.dim(i) for i in inds_v], A.dtype, [ind_s] + inds_v)
-    A.ctx.check(
-        A.ctx.lib.tn_svd_thin(A.ctx.h, A.code, precision_code(precision), m, n, C.c_void_p(mt.ptr), max(m, 1), 0,
-                              C.c_void_p(U.ptr), 0, C.c_void_p(s.ptr), 0, C.c_void_p(V.ptr), 0, 1)
-    )
+    V = DeviceTensor(A.ctx, [k] + [A.dim(i) for i in rest], A.dtype, [ind_s] + rest)
+    um = (C.c_int32 * max(1, len(inds_u)))(*[ids[i] for i in inds_u])
+    du, dv = _desc(U, ids), _desc(V, ids)
+    da = _desc(A, ids)
+    r = C.c_int64()
+    A.ctx.check(A.ctx.lib.tn_tensor_svd_thin(A.ctx.h, A.code, precision_code(precision), C.byref(da), len(inds_u), um,
+                                             ids[ind_s], -1 if maxdim is None else int(maxdim),
+                                             -1.0 if threshold is None else float(threshold), C.byref(du),
+                                             C.c_void_p(s.ptr), C.byref(dv), C.byref(r)))
+    kr = r.value
+    U.shape = tuple(du.dims[i] for i in range(du.rank))
+    V.shape = tuple(dv.dims[i] for i in range(dv.rank))
+    s.shape = (kr,)
+    if inds_v is not None and list(inds_v) != rest:
+        V = permute(V, [ind_s] + list(inds_v))
     return U, s, V
 
 

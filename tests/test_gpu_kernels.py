@@ -308,3 +308,39 @@ def test_contract_c32_tensor_core(ctx):
     tc = tenetgb.binary_einsum(ta, tb, out_inds=list("ad"), precision="mixed")
     ref = np.einsum("abc,cbd->ad", A.astype(np.complex128), B.astype(np.complex128))
     assert np.abs(tc.numpy() - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("dtype,tol", [(np.complex128, 1e-12), (np.complex64, 2e-5)])
+def test_labelled_qr_and_svd_on_a_rank4_tensor(ctx, dtype, tol):
+    """tn_tensor_qr_thin / tn_tensor_svd_thin (Muscle.tensor_qr_thin / tensor_svd_thin):
+    the left labels are not leading in the tensor, so the library matricises by label;
+    Q·R and U·diag(s)·V rebuild the tensor, Q and U are isometries, s matches LAPACK, and
+    the truncated SVD keeps min(maxdim, k) values above the threshold with V compacted."""
+    import tenetgb
+
+    rng = np.random.default_rng(17)
+    x = cgauss(rng, (6, 5, 7, 4)).astype(dtype)
+    labels = ["a", "b", "c", "d"]
+    t = tenetgb.DeviceTensor.from_numpy(ctx, x, labels)
+    left = ["c", "a"]  # matrix rows: (c, a) → 42, columns: (b, d) → 20
+    xm = np.transpose(x, (2, 0, 1, 3)).reshape(42, 20, order="F")
+    Q, R = tenetgb.tensor_qr_thin(t, left, ind_virtual="v")
+    assert Q.inds == ["c", "a", "v"] and R.inds == ["v", "b", "d"] and Q.shape == (7, 6, 20)
+    q, r = Q.numpy().reshape(42, 20, order="F"), R.numpy().reshape(20, 20, order="F")
+    assert np.abs(q @ r - xm).max() <= tol * np.abs(xm).max() * 10
+    np.testing.assert_allclose(q.conj().T @ q, np.eye(20), atol=tol * 10)
+    U, s, V = tenetgb.tensor_svd_thin(t, left, ind_s="s")
+    s_ref = np.linalg.svd(xm.astype(np.complex128), compute_uv=False)
+    assert np.abs(s.numpy() - s_ref).max() <= tol * s_ref[0] * 10
+    u, v = U.numpy().reshape(42, 20, order="F"), V.numpy().reshape(20, 20, order="F")
+    assert np.abs((u * s.numpy()) @ v - xm).max() <= tol * s_ref[0] * 10
+    # truncation: maxdim 9, then |s| > s_ref[6] → keeps 6 values
+    Ut, st, Vt = tenetgb.tensor_svd_thin(t, left, ind_s="s", maxdim=9, threshold=float(s_ref[6]) * (1 + 1e-9))
+    assert st.shape == (6,) and Ut.shape == (7, 6, 6) and Vt.shape == (6, 5, 4)
+    ut, vt = Ut.numpy().reshape(42, 6, order="F"), Vt.numpy().reshape(6, 20, order="F")
+    ref6 = (u[:, :6] * s.numpy()[:6]) @ v[:6, :]
+    assert np.abs((ut * st.numpy()) @ vt - ref6).max() <= tol * s_ref[0] * 10
+    with pytest.raises(ValueError):
+        tenetgb.tensor_svd_thin(t, ["z"], ind_s="s")
+    with pytest.raises(ValueError):
+        tenetgb.tensor_qr_thin(t, ["a"], ind_virtual="b")
