@@ -5,9 +5,12 @@
 // Both operands are K-major (the contraction index contiguous), which is the layout the
 // contraction planner produces with the permutation kernel.  Precision modes:
 //   * TF32      — one pass (A, B), FP32 accumulation;
-//   * 3×TF32    — three passes (A_hi·B_hi + A_hi·B_lo + A_lo·B_hi) into the same TMEM
-//                 accumulator, where x = x_hi + x_lo and x_hi has TF32's 10-bit mantissa:
-//                 FP32-grade products from the TF32 tensor pipe.
+//   * 3×TF32    — three passes A_hi·B_hi + (A_hi·B_lo + A_lo·B_hi), where x_hi is x
+//                 rounded to nearest TF32 and x_lo = x − x_hi exactly; the hi·hi pass and
+//                 the two small correction passes accumulate in separate TMEM
+//                 accumulators (the corrections would otherwise be lost to the large
+//                 accumulator's alignment) and are summed in the epilogue: FP32-grade
+//                 products from the TF32 tensor pipe.
 // Complex operands use the real 4M form as one real GEMM of twice the size:
 //   [Re C; Im C] = [[Ar, −Ai], [Ai, Ar]] · [Br; Bi]
 // built by a prep kernel that also does the hi/lo split, with an epilogue that writes the
@@ -121,8 +124,9 @@ __global__ void __launch_bounds__(128, 1)
   const int gsize = min(kGroupM, tiles_m - first_m);
   const int in_grp = (int)blockIdx.x % per_group;
   const int m0 = (first_m + in_grp % gsize) * BM, n0 = (in_grp / gsize) * BN;
+  const uint32_t tcols = passes > 1 ? 2 * BN : BN;  // hi·hi accumulator [+ corrections]
   if (warp == 0) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(BN)
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)), "r"(tcols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -161,11 +165,14 @@ __global__ void __launch_bounds__(128, 1)
       ok = mbar_wait(&full[s], (t / STAGES) & 1, err);
       if (!ok) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int pass = t / nk;
+      const uint32_t acc = tmem + (pass > 0 ? (uint32_t)BN : 0u);  // corrections: their own accumulator
+      const bool first = (t % nk == 0) && pass <= 1;
 #pragma unroll
       for (int kk = 0; kk < 4; ++kk) {  // 4 × (K = 8 tf32 = 32 bytes)
         const uint64_t a = sdesc(sA + s * A_BYTES) + (uint64_t)((kk * 32) >> 4);
         const uint64_t b = sdesc(sB + s * B_BYTES) + (uint64_t)((kk * 32) >> 4);
-        mma_tf32(tmem, a, b, (t > 0 || kk > 0) ? 1u : 0u);
+        mma_tf32(acc, a, b, (first && kk == 0) ? 0u : 1u);
       }
       mma_commit(&empty[s]);
     }
@@ -187,6 +194,17 @@ __global__ void __launch_bounds__(128, 1)
             "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
           : "r"(taddr));
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (passes > 1) {  // add the correction accumulator
+        uint32_t q[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(q[0]), "=r"(q[1]), "=r"(q[2]), "=r"(q[3]), "=r"(q[4]), "=r"(q[5]), "=r"(q[6]), "=r"(q[7]),
+              "=r"(q[8]), "=r"(q[9]), "=r"(q[10]), "=r"(q[11]), "=r"(q[12]), "=r"(q[13]), "=r"(q[14]), "=r"(q[15])
+            : "r"(taddr + (uint32_t)BN));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j) r[j] = __float_as_uint(__uint_as_float(r[j]) + __uint_as_float(q[j]));
+      }
       if (row < M) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -206,13 +224,19 @@ __global__ void __launch_bounds__(128, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN) : "memory");
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tcols) : "memory");
 }
 
 // ---------------------------------------------------------------------------------
 // operand preparation: K-major real planes (hi, lo) with K padded to Kp (multiple of 32)
 // ---------------------------------------------------------------------------------
-__device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
+// x rounded to the nearest TF32 value (10-bit mantissa, ties away from zero): the
+// remainder x − hi is exact in FP32 and at most half a TF32 unit
+__device__ __forceinline__ float tf32_hi(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
 
 // element (r, c) of op(X) for a column-major complex X with leading dimension ld
 __device__ __forceinline__ cxf ld_op(const cxf* X, int64_t ld, char op, int64_t r, int64_t c) {

@@ -172,6 +172,7 @@ struct tn_ctx {
   // diagnostics of the last Jacobi SVD: sweeps per precision, rotations per sweep of
   // the worst active matrix of the large-matrix path (-1: shared-memory path)
   int last_sweeps_fp32 = 0, last_sweeps_fp64 = 0;
+  int last_refine_iters = 0;  // refinement iterations of the last truncated mixed SVD
   int sweep_rotations[64] = {0};
   float sweep_ratio[64] = {0};  // largest off-diagonal ratio of each sweep (worst active matrix)
   // time of the last DMRG run per phase (ms): gauge moves, environments, eigensolves,
@@ -402,6 +403,9 @@ tn_status_t scale_rows_sqrt(tn_ctx* ctx, cx<T>* X, int64_t rows, int64_t cols, i
 // X_b(r, c) *= 1/sqrt(S_b[r]) (0 where S_b[r] == 0)
 tn_status_t scale_rows_invsqrt(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int64_t ld,
                                const double* S, int64_t sX, int64_t sS, int64_t batch);
+// X_b(r, c) *= S_b[r] (mode 1), or zeroed where S_b[r] == 0 (mode 0)
+tn_status_t scale_rows_mode(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int64_t ld, const double* S, int64_t sX,
+                            int64_t sS, int64_t batch, int mode);
 tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out);
 tn_status_t copy_matrix_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src,
                             int64_t lds, cxd* dst, int64_t ldd, int64_t sSrc = 0,

@@ -281,11 +281,13 @@ tn_status_t mps_ensure_site(tn_mps* p, int i, size_t elems) { return ensure_site
 // simple update core (Muscle.simple_update with AbsorbEqually), batched
 // A (chl·d1 × chm), B (chm × d2·chr), G (d1 d2 × d1 d2) column-major, instance strides
 // sA, sB; G shared by all instances.  Reserves the workspace itself.
+// absorb_right: A' = U, B' = S·Vh (the same two-site state, all of S on the right), so
+// that A' is already left-isometric when the centre moves on to the right.
 // ---------------------------------------------------------------------------------
 tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, int64_t d1, int64_t chm, int64_t d2,
                                int64_t chr, const cxd* A, int64_t sA, const cxd* Bm, int64_t sB, const cxd* dG,
                                int64_t maxdim, double threshold, int64_t batch, su_out_fn out_fn, void* out_arg,
-                               double* Sout, int64_t* rank_out) {
+                               double* Sout, int64_t* rank_out, bool absorb_right = false) {
   const int64_t m = chl * d1, n = d2 * chr, k = std::min(m, n), dd = d1 * d2;
   // m ≥ n (the saturated TEBD case, θ square): U and S only, then
   //   B' = √S Vh = diag(1/√s) Uᴴ θ  (one GEMM; A'B' keeps its ε‖θ‖ accuracy)
@@ -315,14 +317,24 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
   cxd *Aout = nullptr, *Bout = nullptr;
   int64_t sAo = 0, sBo = 0;
   TN_RETURN_IF(out_fn(out_arg, r, &Aout, &sAo, &Bout, &sBo));
-  // A' = U[:, :r] √S
+  // A' = U[:, :r] √S  (or U[:, :r])
   TN_RETURN_IF(copy_matrix_cxd(ctx, m * r, 1, U, m * r, Aout, m * r, m * k, sAo, batch));
-  TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
-  if (left_only) {
+  if (absorb_right) {
+    if (left_only) {
+      // B' = S Vh = U[:, :r]ᴴ θ, rows beyond an instance's own rank (S = 0) zeroed
+      TN_RETURN_IF(gemm_c64(ctx, prec, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
+      TN_RETURN_IF(scale_rows_mode(ctx, Bout, r, n, r, S, sBo, k, batch, 0));
+    } else {
+      TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
+      TN_RETURN_IF(scale_rows_mode(ctx, Bout, r, n, r, S, sBo, k, batch, 1));
+    }
+  } else if (left_only) {
+    TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
     // B' = diag(1/√s) U[:, :r]ᴴ θ
     TN_RETURN_IF(gemm_c64(ctx, prec, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
     TN_RETURN_IF(scale_rows_invsqrt(ctx, Bout, r, n, r, S, sBo, k, batch));
   } else {
+    TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
     // B' = √S Vh[:r, :]
     TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
     TN_RETURN_IF(scale_rows_sqrt<double>(ctx, Bout, r, n, r, S, sBo, k, batch));
@@ -353,14 +365,21 @@ tn_status_t pair_out(void* arg, int64_t r, cxd** Aout, int64_t* sAo, cxd** Bout,
   return TN_OK;
 }
 
-tn_status_t apply_gate2(tn_mps* p, int a, const cxd* dG, int64_t maxdim, double threshold) {
+// absorb_right: site a keeps U (left-isometric) and site a+1 all of S, so the form
+// becomes MixedCanonical(a+1) — the same state as AbsorbEqually's MixedCanonical([a, a+1]),
+// with the first of the next centre move's two QR factorisations already done
+tn_status_t apply_gate2(tn_mps* p, int a, const cxd* dG, int64_t maxdim, double threshold, bool absorb_right = false) {
   const int64_t d = p->d;
   PairOut e{p, a};
   int64_t r = 0;
   TN_RETURN_IF(simple_update_core(p->ctx, p->prec, p->bond[a - 1], d, p->bond[a], d, p->bond[a + 1], p->site[a],
                                   p->cap[a], p->site[a + 1], p->cap[a + 1], dG, maxdim, threshold, p->B, pair_out, &e,
-                                  nullptr, &r));
+                                  nullptr, &r, absorb_right));
   p->bond[a] = r;
+  if (absorb_right) {
+    p->kind = TN_FORM_MIXED;
+    p->lo = p->hi = a + 1;
+  }
   return TN_OK;
 }
 
@@ -758,8 +777,13 @@ tn_status_t tn_mps_evolve_brickwork(tn_mps* p, int32_t n_layers, const int32_t* 
   for (int l = 0; l < n_layers; ++l) {
     for (int g = 0; g < n_gates[l]; ++g) {
       int a = starts[l] + 2 * g;
+      // within a layer the next gate is further right: S goes to the right-hand site, whose
+      // QR the centre move needs anyway, and the left-hand site is left as U.  The last
+      // gate of a layer keeps Tenet's AbsorbEqually, so every layer (and the call) ends in
+      // the reference's form (MixedCanonical([a, a+1])) and split.
+      const bool right = g + 1 < n_gates[l];
       TN_RETURN_IF(canonize_mixed(p, a, a + 1));
-      TN_RETURN_IF(apply_gate2(p, a, p->gates + off, maxdim, threshold));
+      TN_RETURN_IF(apply_gate2(p, a, p->gates + off, maxdim, threshold, right));
       off += g4;
     }
   }

@@ -57,6 +57,19 @@ __global__ void k_scale_rows_invsqrt(cxd* X, int64_t rows, int64_t cols, int64_t
     }
 }
 
+// X_b(r, c) *= S_b[r] (mode 1) or keeps its value where S_b[r] > 0 and becomes 0 elsewhere
+// (mode 0: the rows beyond an instance's kept rank of a zero-padded batch)
+__global__ void k_scale_rows_mode(cxd* X, int64_t rows, int64_t cols, int64_t ld, int64_t sX, const double* S,
+                                  int64_t sS, int64_t batch, int mode) {
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
+      int64_t r = t % rows, c = t / rows;
+      const double s = S[b * sS + r];
+      const double f = mode == 1 ? s : (s > 0.0 ? 1.0 : 0.0);
+      X[b * sX + r + c * ld] = f * X[b * sX + r + c * ld];
+    }
+}
+
 // rank_b = #{ j < min(maxdim, k) : |S_b[j]| > threshold }, at least 1 (S descending);
 // one block per instance
 __global__ void k_rank_select(const double* S, int64_t k, int64_t sS, int64_t maxdim, double threshold, int* out) {
@@ -245,6 +258,15 @@ tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out) {
   double ss = 0;
   TN_RETURN_IF(sumsq<double2>(ctx, n, reinterpret_cast<const double2*>(x), &ss));
   *h_out = sqrt(ss);
+  return TN_OK;
+}
+
+tn_status_t scale_rows_mode(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int64_t ld, const double* S, int64_t sX,
+                            int64_t sS, int64_t batch, int mode) {
+  if (rows * cols * batch == 0) return TN_OK;
+  dim3 g(blocks_for(ctx, rows * cols), (unsigned)(batch < 65535 ? batch : 65535));
+  k_scale_rows_mode<<<g, 256, 0, ctx->stream>>>(X, rows, cols, ld, sX, S, sS, batch, mode);
+  TN_LAUNCHED(ctx);
   return TN_OK;
 }
 

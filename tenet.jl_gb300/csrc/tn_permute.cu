@@ -7,6 +7,8 @@
 // coalesced gather; otherwise the two contiguous modes form a 32×32 tile staged in
 // shared memory so that both the loads and the stores are coalesced.  Elements are
 // moved whole: a ComplexF64 element is one 128-bit access.
+#include <algorithm>
+
 #include "tn_internal.cuh"
 
 namespace {
@@ -53,6 +55,41 @@ __global__ void k_permute_generic(PermPlan p, int64_t total, const E* __restrict
       oo += c * p.os[j];
     }
     out[oo] = maybe_conj(__ldg(in + io), conj);
+  }
+}
+
+// the contiguous mode is the same in both layouts (e.g. (0, 2, 1)): each row of it is a
+// contiguous run in the input and in the output, copied by one block with four
+// independent 128-bit loads in flight per thread; the row's offsets are decoded once
+template <typename E>
+__global__ void __launch_bounds__(256) k_permute_rows(PermPlan p, int64_t rows, const E* __restrict__ in,
+                                                      E* __restrict__ out, bool conj) {
+  const int64_t n0 = p.n[0];
+  for (int64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+    int64_t rem = row, io = 0, oo = 0;
+#pragma unroll 1
+    for (int j = 1; j < p.r; ++j) {
+      const int64_t q = rem / p.n[j];
+      const int64_t c = rem - q * p.n[j];
+      rem = q;
+      io += c * p.is[j];
+      oo += c * p.os[j];
+    }
+    const E* src = in + io;
+    E* dst = out + oo;
+    for (int64_t base = threadIdx.x; base < n0; base += 4 * (int64_t)blockDim.x) {
+      E v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t t = base + u * (int64_t)blockDim.x;
+        if (t < n0) v[u] = __ldg(src + t);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t t = base + u * (int64_t)blockDim.x;
+        if (t < n0) dst[t] = maybe_conj(v[u], conj);
+      }
+    }
   }
 }
 
@@ -135,6 +172,13 @@ tn_status_t run_plan(tn_ctx* ctx, PermPlan p, const E* in, E* out, bool conj) {
     if (p.os[j] == 1 && jo < 0) jo = j;
   }
   const bool tiled = ja >= 0 && jo >= 0 && ja != jo && p.n[ja] >= 8 && p.n[jo] >= 8;
+  if (ja == 0 && jo == 0 && p.r > 1 && p.n[0] >= 32) {
+    const int64_t rows = total / p.n[0];
+    const int64_t blocks = std::min<int64_t>(rows, (int64_t)ctx->num_sms * 16);
+    k_permute_rows<E><<<(unsigned)blocks, 256, 0, ctx->stream>>>(p, rows, in, out, conj);
+    TN_LAUNCHED(ctx);
+    return TN_OK;
+  }
   if (!tiled) {
     int threads = 256;
     int64_t blocks = (total + threads - 1) / threads;

@@ -202,7 +202,7 @@ __device__ __forceinline__ void rot_apply_c(T c, cx<T> se, cx<T>& wi, cx<T>& wj)
 // LAT (cached norms, no truncation flags): the latency-bound form for the dataflow
 // kernel — the cached norms and ‖A‖²_F are fetched with the columns, thread 0 forms only
 // the rotation (make_rot_lean), and thread 32 updates the norms and counters.
-template <typename T, int NT, int R, bool EXACT, bool LAT = false>
+template <typename T, int NT, int R, bool EXACT, bool LAT = false, bool PV = false>
 __device__ __forceinline__ void jacobi_pair(int64_t m, int64_t n, int64_t b, int i, int j, cx<T>* W, int64_t sW,
                                             cx<T>* V, int64_t sV, T* nrm, int64_t nmat, int* cnt, int* ratio, T tol,
                                             const unsigned char* __restrict__ tail) {
@@ -221,11 +221,23 @@ __device__ __forceinline__ void jacobi_pair(int64_t m, int64_t n, int64_t b, int
   constexpr int NW = NT / 32;
   __shared__ T red[NW][4];
   cx<T> x[R], y[R];
+  // PV (V accumulated, few rows per thread): the V columns (n ≤ m ≤ NT·R rows) are loaded
+  // together with W's, so their latency overlaps the reduction instead of following the
+  // rotation (without V the registers are left to occupancy)
+  constexpr bool kPrefetchV = PV && R <= 4;
+  constexpr int RV = kPrefetchV ? R : 1;
+  cx<T> vx[RV], vy[RV];
+  cx<T>* vi = V ? V + b * sV + (int64_t)i * n : nullptr;
+  cx<T>* vj = V ? V + b * sV + (int64_t)j * n : nullptr;
   cx<T> g = mkcx<T>(0, 0);
   T al = 0, be = 0;
 #pragma unroll
   for (int q = 0; q < R; ++q) {
     const int64_t t = threadIdx.x + (int64_t)q * NT;
+    if (kPrefetchV && V && t < n) {
+      vx[q < RV ? q : 0] = vi[t];
+      vy[q < RV ? q : 0] = vj[t];
+    }
     if (t < m) {
       x[q] = wi[t];
       y[q] = wj[t];
@@ -344,9 +356,17 @@ __device__ __forceinline__ void jacobi_pair(int64_t m, int64_t n, int64_t b, int
       wj[t] = y[q];
     }
   }
-  if (V) {
-    cx<T>* vi = V + b * sV + (int64_t)i * n;
-    cx<T>* vj = V + b * sV + (int64_t)j * n;
+  if (V && kPrefetchV) {
+#pragma unroll
+    for (int q = 0; q < RV; ++q) {
+      const int64_t t = threadIdx.x + (int64_t)q * NT;
+      if (t < n) {
+        rot_apply_c(c, se, vx[q], vy[q]);
+        vi[t] = vx[q];
+        vj[t] = vy[q];
+      }
+    }
+  } else if (V) {
     for (int64_t t = threadIdx.x; t < n; t += NT) {
       cx<T> a = vi[t], e = vj[t];
       rot_apply_c(c, se, a, e);
@@ -356,7 +376,7 @@ __device__ __forceinline__ void jacobi_pair(int64_t m, int64_t n, int64_t b, int
   }
 }
 
-template <typename T, int NT, int R, bool EXACT>
+template <typename T, int NT, int R, bool EXACT, bool PV = false>
 __global__ void __launch_bounds__(NT)
     k_jacobi_step_reg(int64_t m, int64_t n, int N, int r, cx<T>* W, int64_t sW, cx<T>* V, int64_t sV, T* nrm,
                       const int* active, int* rotated, T tol, const unsigned char* __restrict__ tail) {
@@ -365,7 +385,8 @@ __global__ void __launch_bounds__(NT)
   int i, j;
   rr_pair(N, r, blockIdx.x, i, j);
   if (j >= n) return;
-  jacobi_pair<T, NT, R, EXACT>(m, n, b, i, j, W, sW, V, sV, nrm, gridDim.y, rotated, rotated + gridDim.y, tol, tail);
+  jacobi_pair<T, NT, R, EXACT, false, PV>(m, n, b, i, j, W, sW, V, sV, nrm, gridDim.y, rotated, rotated + gridDim.y,
+                                          tol, tail);
 }
 
 // Persistent one-sided Jacobi for small matrices, where a round is far too little work to
@@ -883,8 +904,14 @@ static tn_status_t launch_step(tn_ctx* ctx, int64_t m, int64_t n, int N, int r, 
   constexpr bool EX = sizeof(T) == 4;
   const dim3 grid(N / 2, gy);
   const int64_t sW = m * n, sV = n * n;
-  if (m <= 512)
+  if (m <= 512 && V)
+    k_jacobi_step_reg<T, 128, 4, EX, true><<<grid, 128, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated,
+                                                                         tol, tail);
+  else if (m <= 512)
     k_jacobi_step_reg<T, 128, 4, EX><<<grid, 128, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol, tail);
+  else if (m <= 1024 && V)
+    k_jacobi_step_reg<T, 256, 4, EX, true><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated,
+                                                                         tol, tail);
   else if (m <= 1024)
     k_jacobi_step_reg<T, 256, 4, EX><<<grid, 256, 0, ctx->stream>>>(m, n, N, r, W, sW, V, sV, nrm, active, rotated, tol, tail);
   else if (m <= 2048)
@@ -1222,6 +1249,73 @@ __global__ void k_ortho_poly(int64_t n, int64_t batch, cxd* G, const cxf* E2, co
   }
 }
 
+// ---------------------------------------------------------------------------------
+// Refinement of the right singular vectors by matrix products (the truncated mixed path).
+//
+// The iteration is Ogita & Aishima's refinement of an approximate eigenvector basis
+// (T. Ogita, K. Aishima, "Iterative refinement for symmetric eigenvalue decomposition",
+// Japan J. Indust. Appl. Math. 35 (2018)) applied to AᴴA through W = A·V, so AᴴA is never
+// formed: with R = I − VᴴV and S = WᴴW = Vᴴ(AᴴA)V,
+//     λ_i = S_ii / (1 − R_ii),
+//     E_ii = R_ii / 2,   E_ij = (S_ij + λ_j R_ij) / (λ_j − λ_i)   (i ≠ j),
+//     V ← V + V·E,
+// which converges quadratically once the columns are separated.  Every product is a
+// split-BF16 tensor-core GEMM whose digit planes are scaled per row and per column, so
+// S_ij is accurate to ~ε·σ_i·σ_j (graded, like one-sided Jacobi) and the σ_i come out
+// with relative accuracy.  A pair whose first-order step exceeds kRefineStepMax (a
+// near-degenerate pair) gets the orthogonality part R_ij/2 only and is left to one FP64
+// Jacobi check afterwards; pairs of two tail columns (ranked below the kept set) are only
+// kept orthogonal.
+// ---------------------------------------------------------------------------------
+constexpr double kRefineStepMax = 0.1;
+constexpr int kRefineMaxIter = 6;
+
+__global__ void k_set_identity_cxd(int64_t n, int64_t batch, cxd* X) {
+  const int64_t total = n * n * batch;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t w = t % (n * n);
+    X[t] = mkcx((w % n) == (w / n) ? 1.0 : 0.0, 0.0);
+  }
+}
+
+// λ_i = Re S_ii / (1 − Re R_ii)
+__global__ void k_refine_lambda(int64_t n, int64_t batch, const cxd* __restrict__ S, const cxd* __restrict__ R,
+                                double* __restrict__ lam) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * batch; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / n, i = t % n, d = b * n * n + i + i * n;
+    lam[t] = S[d].x / (1.0 - R[d].x);
+  }
+}
+
+// E (in place over R); emax[b] = the largest applied |E_ij| (float bits), clusters[b] =
+// pairs with a kept column left to the FP64 check
+__global__ void k_refine_step(int64_t n, int64_t batch, const cxd* __restrict__ S, cxd* RE,
+                              const double* __restrict__ lam, const unsigned char* __restrict__ tail, int* emax,
+                              int* clusters) {
+  const int64_t total = n * n * batch;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = t / (n * n), w = t % (n * n), i = w % n, j = w / n;
+    const cxd r = RE[t];
+    cxd e = mkcx(0.5 * r.x, 0.5 * r.y);
+    if (i != j) {
+      const bool both_tail = tail && tail[b * n + i] && tail[b * n + j];
+      if (!both_tail) {
+        const double li = lam[b * n + i], lj = lam[b * n + j], den = lj - li;
+        const cxd sij = S[t];
+        const cxd num = mkcx(sij.x + lj * r.x, sij.y + lj * r.y);
+        const double mag = sqrt(num.x * num.x + num.y * num.y);
+        if (fabs(den) > 0.0 && mag <= kRefineStepMax * fabs(den)) {
+          e = mkcx(num.x / den, num.y / den);
+          atomicMax(&emax[b], __float_as_int((float)(mag / fabs(den))));
+        } else if (mag > 0.0) {
+          atomicAdd(&clusters[b], 1);
+        }
+      }
+    }
+    RE[t] = e;
+  }
+}
+
 size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
   size_t s = 0;
   s += ws_round(sizeof(cxf) * (size_t)(m * n * batch));      // W32
@@ -1234,6 +1328,7 @@ size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
   s += ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // V scratch when V is not wanted
   s += ws_round(sizeof(cxf) * (size_t)(n * n * batch));  // E³ when W32 has no room for it
   s += ws_round((size_t)(n * batch));                     // tail flags
+  s += ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // R / E of the refinement
   return s;
 }
 
@@ -1267,6 +1362,7 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   double* nrm64 = ws_take<double>(ctx, (size_t)((n + 1) * batch));
   float* nrm32 = ws_take<float>(ctx, (size_t)((n + 1) * batch));
   unsigned char* tail = ws_take<unsigned char>(ctx, (size_t)(n * batch));
+  cxd* RE = ws_take<cxd>(ctx, (size_t)(n * n * batch));
   const int64_t keep_m = (!want_v && keep > 0) ? keep + std::max<int64_t>(16, keep / 8) : 0;
   for (int64_t b = 0; b < batch; ++b) {
     int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
@@ -1290,6 +1386,66 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
     int64_t blocks = std::min<int64_t>((cnt + 255) / 256, 4096);
     k_f2d<<<(unsigned)blocks, 256, 0, ctx->stream>>>(cnt, V32, V64);
     TN_LAUNCHED(ctx);
+  }
+  if (keep_m > 0 && keep_m < n) {
+    // truncated: refine V by matrix products (tensor pipe) instead of FP64 Jacobi sweeps
+    const unsigned blocks = (unsigned)std::min<int64_t>((n * n * batch + 255) / 256, 4096);
+    const unsigned lblocks = (unsigned)std::min<int64_t>((n * batch + 255) / 256, 1024);
+    const cxd one = mkcx(1.0, 0.0), zero = mkcx(0.0, 0.0), mone = mkcx(-1.0, 0.0);
+    std::vector<int> h_stat(2 * batch);
+    bool w_current = false;
+    int clusters = 0;
+    ctx->last_refine_iters = 0;
+    for (int it = 0; it < kRefineMaxIter; ++it) {
+      TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, one, A, lda, sA, V64, n, n * n, zero, W64, m, m * n,
+                            batch));
+      TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'C', 'N', n, n, m, one, W64, m, m * n, W64, m, m * n, zero, G, n, n * n,
+                            batch));
+      k_set_identity_cxd<<<blocks, 256, 0, ctx->stream>>>(n, batch, RE);
+      TN_LAUNCHED(ctx);
+      TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'C', 'N', n, n, n, mone, V64, n, n * n, V64, n, n * n, one, RE, n, n * n,
+                            batch));
+      k_refine_lambda<<<lblocks, 256, 0, ctx->stream>>>(n, batch, G, RE, nrm64);
+      TN_LAUNCHED(ctx);
+      TN_CHECK_CUDA(ctx, cudaMemsetAsync(rotated, 0, sizeof(int) * 2 * batch, ctx->stream));
+      k_refine_step<<<blocks, 256, 0, ctx->stream>>>(n, batch, G, RE, nrm64, tail, rotated, rotated + batch);
+      TN_LAUNCHED(ctx);
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_stat.data(), rotated, sizeof(int) * 2 * batch, cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+      TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+      float emax = 0.f;
+      clusters = 0;
+      for (int64_t b = 0; b < batch; ++b) {
+        float e;
+        memcpy(&e, &h_stat[b], sizeof(float));
+        emax = std::max(emax, e);
+        clusters += h_stat[batch + b];
+      }
+      ctx->last_refine_iters = it + 1;
+      if (emax < 1e-15f) {  // the correction is below FP64 resolution: W = A·V is final
+        w_current = true;
+        break;
+      }
+      // V ← V + V·E
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(V, V64, sizeof(cxd) * (size_t)(n * n * batch), cudaMemcpyDeviceToDevice,
+                                         ctx->stream));
+      TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', n, n, n, one, V64, n, n * n, RE, n, n * n, one, V, n, n * n,
+                            batch));
+      std::swap(V, V64);
+      // quadratic convergence: a step below 1e-10 leaves ~1e-20 (the floor is ε over the
+      // smallest relative gap, which further steps do not lower)
+      if (emax < 1e-10f) break;
+    }
+    if (!w_current)
+      TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, one, A, lda, sA, V64, n, n * n, zero, W64, m, m * n,
+                            batch));
+    ctx->last_sweeps_fp64 = 0;
+    if (clusters > 0)  // near-degenerate pairs with a kept column: one-sided Jacobi finishes them
+      TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W64, nullptr, batch, true, active, rotated, nrm64, kMaxSweeps, nullptr,
+                                        &noconv, tail, keep_m, true));
+    TN_RETURN_IF(jacobi_finalize<double>(ctx, m, n, W64, nullptr, order, U, sU, S, sS, nullptr, 0, false, batch));
+    if (noconv) return tn_set_error(ctx, TN_ENOCONV, "Jacobi SVD did not converge within %d sweeps", kMaxSweeps);
+    return TN_OK;
   }
   // One orthonormalisation step: with E = VᴴV − I (FP64 GEMM),
   //   V ← V (I − E/2 + 3E²/8 − 5E³/16)   (the (I + E)^{-1/2} series; residual ~ (35/128)E⁴)

@@ -12,6 +12,8 @@
   mixed and split-BF16 forms.
 * The closed 8×8 lattice (bond 8, seed 4) contracted to a scalar along the greedy path:
   FP64 GPU against the complex128 oracle along the same path to ≤ 1e-12.
+* The 512-MPS ragged population (canonize → compress(χ/2) → norm, one grouped call):
+  norms against the oracle and the per-instance device path.
 
 These take minutes of oracle time on the host cores (marked slow as well as gpu).
 """
@@ -124,3 +126,41 @@ def test_lattice_8x8_bond8_fp64_matches_oracle(ctx):
     err = abs(val - ref) / abs(ref)
     print(f"\n8x8 lattice: |ref| = {abs(ref):.6e} (product of norms {scale:.3e}); relative error {err:.2e}")
     assert err <= 1e-12
+
+
+def test_batched_512_population_norms(ctx):
+    """Config 4 at its full size: the 512-MPS ragged population (L in [16, 128], χ
+    log-uniform in [16, 512], seed 5), canonize → compress(χ/2) → norm in one grouped
+    call.  The norms of the 150 cheapest instances (by L·χ³) are checked against the
+    oracle on their initial sites, and 12 instances spread over the χ range (the largest
+    included) against the per-instance device path, to 1e-12 relative."""
+    import tenetgb
+    from tenetgb import workloads as W
+    from tenetgb.group import MPSGroup
+
+    Ls, chis = W.batched_population()
+    maxdim = [max(1, c // 2) for c in chis]
+    g = MPSGroup.random(Ls, chis, seed=5, ctx=ctx)
+    ctx.sync()
+    cost = np.array([L * c**3 for L, c in zip(Ls, chis)])
+    cheap = list(np.argsort(cost)[:150])
+    spread = list(np.argsort(chis)[np.linspace(0, len(chis) - 1, 12).astype(int)])
+    init = {b: g.sites(b) for b in set(cheap) | set(spread)}
+    norms = g.canonize_compress_norm(maxdim)
+    assert norms.shape == (512,) and np.all(np.isfinite(norms)) and np.all(norms > 0)
+    worst = 0.0
+    for b in cheap:
+        p = O.OMPS([a.copy() for a in init[b]])
+        O.canonize(p, O.MixedCanonical(Ls[b]))
+        O.compress(p, maxdim=maxdim[b])
+        worst = max(worst, abs(norms[b] - O.norm(p)) / O.norm(p))
+    worst_dev = 0.0
+    for b in spread:
+        psi = tenetgb.MPS([a.copy() for a in init[b]], ctx=ctx)
+        psi.canonize_(tenetgb.MixedCanonical(Ls[b]))
+        psi.compress_(maxdim=maxdim[b])
+        worst_dev = max(worst_dev, abs(norms[b] - psi.norm()) / psi.norm())
+        del psi
+    print(f"\n512-MPS population: norms vs oracle (150 cheapest) {worst:.2e}; vs per-instance device path "
+          f"(12, χ {min(chis[b] for b in spread)}..{max(chis[b] for b in spread)}) {worst_dev:.2e}")
+    assert worst <= 1e-12 and worst_dev <= 1e-12

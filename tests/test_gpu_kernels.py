@@ -29,6 +29,8 @@ def cgauss(rng, shape, dtype=np.complex128):
     ((33, 65), (1, 0)),
     ((1, 17, 1, 9), (3, 2, 1, 0)),
     ((8, 8, 8, 8, 8), (4, 0, 3, 1, 2)),
+    ((96, 3, 5, 2), (0, 3, 1, 2)),
+    ((1000, 7, 3), (0, 2, 1)),
 ])
 @pytest.mark.parametrize("dtype", [np.complex128, np.complex64, np.float64, np.float32])
 def test_permute_bit_exact(ctx, shape, perm, dtype):
@@ -52,6 +54,8 @@ def test_permute_conj(ctx):
     t = tenetgb.DeviceTensor.from_numpy(ctx, x, ["a", "b", "c"])
     out = tenetgb.permute(t, ["c", "a", "b"], conj=True).numpy()
     np.testing.assert_array_equal(out, np.transpose(x, (2, 0, 1)).conj())
+    out = tenetgb.permute(t, ["a", "c", "b"], conj=True).numpy()  # contiguous mode kept: row copies
+    np.testing.assert_array_equal(out, np.transpose(x, (0, 2, 1)).conj())
 
 
 @pytest.mark.parametrize("opa,opb", [("N", "N"), ("N", "C"), ("C", "N"), ("T", "T"), ("T", "N")])
@@ -334,8 +338,8 @@ def test_labelled_qr_and_svd_on_a_rank4_tensor(ctx, dtype, tol):
     assert np.abs(s.numpy() - s_ref).max() <= tol * s_ref[0] * 10
     u, v = U.numpy().reshape(42, 20, order="F"), V.numpy().reshape(20, 20, order="F")
     assert np.abs((u * s.numpy()) @ v - xm).max() <= tol * s_ref[0] * 10
-    # truncation: maxdim 9, then |s| > s_ref[6] → keeps 6 values
-    Ut, st, Vt = tenetgb.tensor_svd_thin(t, left, ind_s="s", maxdim=9, threshold=float(s_ref[6]) * (1 + 1e-9))
+    # truncation: maxdim 9, then |s| above the midpoint of s_5 and s_6 → keeps 6 values
+    Ut, st, Vt = tenetgb.tensor_svd_thin(t, left, ind_s="s", maxdim=9, threshold=float(s_ref[5] + s_ref[6]) / 2)
     assert st.shape == (6,) and Ut.shape == (7, 6, 6) and Vt.shape == (6, 5, 4)
     ut, vt = Ut.numpy().reshape(42, 6, order="F"), Vt.numpy().reshape(6, 20, order="F")
     ref6 = (u[:, :6] * s.numpy()[:6]) @ v[:6, :]
@@ -344,3 +348,29 @@ def test_labelled_qr_and_svd_on_a_rank4_tensor(ctx, dtype, tol):
         tenetgb.tensor_svd_thin(t, ["z"], ind_s="s")
     with pytest.raises(ValueError):
         tenetgb.tensor_qr_thin(t, ["a"], ind_virtual="b")
+
+
+@pytest.mark.parametrize("k", [512, 4096])
+def test_three_pass_tf32_is_fp32_grade(ctx, k):
+    """3×TF32 (round-to-nearest split, corrections in their own accumulator) is as accurate
+    as the FP32 CUDA-core GEMM on the same ComplexF32 data, also at long contractions."""
+    import ctypes as C
+
+    import tenetgb
+
+    rng = np.random.default_rng(14)
+    m = n = 256
+    A, B = cgauss(rng, (m, k), np.complex64), cgauss(rng, (k, n), np.complex64)
+    ref = A.astype(np.complex128) @ B.astype(np.complex128)
+    dA = tenetgb.DeviceTensor.from_numpy(ctx, A)
+    dB = tenetgb.DeviceTensor.from_numpy(ctx, B)
+    one, zero = (C.c_double * 2)(1, 0), (C.c_double * 2)(0, 0)
+    errs = {}
+    for prec in ("native", "mixed", "tf32"):
+        dC = tenetgb.DeviceTensor(ctx, (m, n), np.complex64)
+        ctx.check(ctx.lib.tn_gemm(ctx.h, 2, tenetgb.core.precision_code(prec), b"N", b"N", m, n, k, one,
+                                  C.c_void_p(dA.ptr), m, 0, C.c_void_p(dB.ptr), k, 0, zero, C.c_void_p(dC.ptr), m, 0, 1))
+        errs[prec] = np.linalg.norm(dC.numpy() - ref) / np.linalg.norm(ref)
+    print(errs)
+    assert errs["mixed"] <= 2.0 * errs["native"] + 1e-7, errs
+    assert errs["tf32"] > 10 * errs["mixed"], errs
