@@ -319,8 +319,10 @@ def run_ours(args):
     peaks = pipe_peaks(ctx)
     prof_psi = psi_mixed.copy()
     ctx.profile(True)
+    ctx.refine_stats(reset=True)
     prof_psi.evolve_brickwork_([prof_layer], maxdim=CHI_MAX, threshold=CUTOFF)
     prof = ctx.profile_read()
+    refine = ctx.refine_stats(reset=True)
     ctx.profile(False)
     del prof_psi
     rooflines = kernel_rooflines(prof, peaks)
@@ -411,6 +413,8 @@ def run_ours(args):
         "clocks": clk.summary(),
         "roofline": roofline_entry(rooflines, peaks, traffic=DOMINANT_TRAFFIC.get(max(rooflines, key=lambda k: rooflines[k]["ms"]))),
         "kernel_rooflines": rooflines,
+        "refinement": dict(refine, per_call_iterations=refine["iterations"] / max(1, refine["calls"]),
+                           note="truncated mixed SVDs of the profiled layer (one per gate, B instances each)"),
         "peaks": peaks,
     }
     if rank == 0:

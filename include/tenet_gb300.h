@@ -217,6 +217,18 @@ tn_status_t tn_tensor_svd_thin(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t pre
  * number of rotations applied in each sweep of the first matrix (up to n_rot) */
 tn_status_t tn_svd_last_sweeps(tn_ctx* ctx, int32_t* fp32_sweeps, int32_t* fp64_sweeps,
                                int32_t* rotations, int32_t n_rot);
+/* cumulative statistics of the truncated mixed-precision SVD (the FP32 pre-pass + matrix-
+ * product refinement of the kept right vectors) on this context: totals[0] calls,
+ * totals[1] refinement iterations, totals[2] near-degenerate pairs handed to the FP64
+ * one-sided Jacobi of the marked columns, totals[3] calls that needed full FP64 sweeps;
+ * reset != 0 zeroes them after the read */
+tn_status_t tn_svd_refine_stats(tn_ctx* ctx, int64_t* totals, int32_t reset);
+/* the last truncated mixed-precision SVD: per refinement iteration k (< *iterations, at
+ * most 8) trace[4k..4k+3] = the largest applied step |E_ij|, the largest |I − VᴴV|_ij,
+ * the largest ‖E‖_F over the batch and the near-degenerate pairs marked; *outcome 0
+ * converged, 1 left the quadratic regime (FP64 sweeps from the FP32 basis), 2 out of
+ * iterations (FP64 sweeps from the refined basis) */
+tn_status_t tn_svd_last_refine(tn_ctx* ctx, float* trace, int32_t* iterations, int32_t* outcome);
 /* the largest off-diagonal ratio |w_iᴴw_j| / (‖w_i‖‖w_j‖) seen in each sweep of the
  * first matrix of the last multi-launch Jacobi phase (up to n values) */
 tn_status_t tn_svd_last_ratios(tn_ctx* ctx, float* ratios, int32_t n);
@@ -334,7 +346,8 @@ tn_status_t tn_mps_sample(tn_mps* mps, int32_t instance, int64_t nshots, const d
  * column-major (w_{i-1}, d, d, w_i) = (left bond, output, input, right bond) C64, with
  * w_0 = w_L = 1; mpo_bonds holds w_1..w_{L-1}.  algorithm 0: direct contraction (every
  * instance; bonds become χ_i·w_i, form MixedCanonical(all)); 1: zip-up with truncation
- * (maxdim > 0 and/or threshold > 0; single-instance MPS). */
+ * (maxdim > 0 and/or threshold > 0; every instance, the common bond the largest kept rank
+ * with each instance's surplus singular values zero). */
 tn_status_t tn_mps_evolve_mpo(tn_mps* mps, const void* const* h_mpo_sites, const int64_t* mpo_bonds, int32_t algorithm,
                               int64_t maxdim, double threshold);
 /* dmrg!(ψ, H; method) (src/Algorithms/DMRG.jl:45-461): ground-state search in place.

@@ -8,10 +8,12 @@
 // Splitting.  Every row i of op(A) gets a power-of-two scale σ_i ≥ max_k(|Re a_ik|,
 // |Im a_ik|) and every column j of op(B) a scale τ_j.  Each real part v of an entry is
 // cut into S signed digits of b bits (b ≤ 8):
-//     v = σ · 2^{1-b} · Σ_{p=0}^{S-1} d_p · 2^{-bp} + r,   |d_p| ≤ 2^{b-1} integers,
-//     |r| ≤ 2^{-bS} σ,
-// computed exactly in FP64 (x ← 2^{b-1}·v/σ; d ← rint(x); x ← 2^b·(x − d); …).  Every
-// digit is an integer of magnitude ≤ 128, exactly representable in BF16.
+//     v = σ · 2^{2-b} · Σ_{p=0}^{S-1} d_p · 2^{-bp} + r,   |d_p| ≤ 2^{b-1} integers,
+//     |r| ≤ 2^{1-bS} σ,
+// computed exactly (the top digit rint(2^{b-2}·v/σ) in FP64 — one bit of headroom, so the
+// carry from the lower digits keeps it within 2^{b-1} — the others as balanced base-2^b
+// digits of the remainder held as one int64).  Every digit is an integer of magnitude
+// ≤ 2^{b-1} ≤ 128, exactly representable in BF16.
 //
 // Products.  Complex arithmetic uses the real 4M form with Re/Im rows interleaved:
 //     A''[2i]   = [Re a_i·, −Im a_i·],  A''[2i+1] = [Im a_i·, Re a_i·]   (2m × 2k)
@@ -24,10 +26,10 @@
 // b is the widest digit with S·K·2^{2b-2} ≤ 2^24, which keeps the FP32 accumulation
 // exact, and contractions too long for b = 7 are split on the host into chunks that
 // accumulate into C.  The epilogue combines the levels in FP64 (Horner in 2^-b) and
-// applies σ_i τ_j 2^{2-2b}:
-//     c_ij = σ_i τ_j 2^{2-2b} Σ_L 2^{-bL} acc_L.
+// applies σ_i τ_j 2^{4-2b}:
+//     c_ij = σ_i τ_j 2^{4-2b} Σ_L 2^{-bL} acc_L.
 // The only approximation is the dropped pairs (p + q ≥ S) and the digit remainders, of
-// relative size ~S·2^{-bS} per product: S = 8, b = 7 gives ~53 bits, FP64-grade products.
+// relative size ~S·2^{1-bS} per product: S = 8, b = 7 gives ~52 bits, FP64-grade products.
 //
 // Kernel.  One CTA (6 warps) per 128×64 tile of the real 4M product, for one batch
 // instance.  Warp 4 lane 0 issues TMA loads: per K stage (64 BF16 = 128 bytes, 128-byte
@@ -230,7 +232,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const int row = m0 + warp * 32 + lane;  // real row of the 4M product: 2i + (0 Re | 1 Im)
       const int i = row >> 1;
       const bool re_lane = (lane & 1) == 0;
-      const double si = (row < M2) ? ldexp(sig[(int64_t)bidx * m_complex + i], 2 - 2 * bits) : 0.0;
+      const double si = (row < M2) ? ldexp(sig[(int64_t)bidx * m_complex + i], 4 - 2 * bits) : 0.0;
       const double hb = ldexp(1.0, -bits);
       cxd* Cb = C + (int64_t)bidx * sC;
 #pragma unroll 1
@@ -310,7 +312,7 @@ __global__ void k_oz_scales(OpView v, int64_t R, int64_t K, int64_t batch, doubl
 }
 
 __device__ __forceinline__ unsigned short bf16_bits(double d) {
-  return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));
+  return __bfloat16_as_ushort(__float2bfloat16_rn((float)d));  // |d| ≤ 128 integer: exact
 }
 
 // digit planes of one operand.  a_form: A'' rows 2r (Re) / 2r+1 (Im) with columns
@@ -340,22 +342,42 @@ __global__ void __launch_bounds__(256)
     const int64_t r = r0 + u, c = c0 + tx;
     if (r >= R || c >= K) continue;
     const cxd x = tile[tx][u];
-    const double inv = ldexp(1.0 / scale[b * R + r], bits - 1);  // powers of two: exact
-    const double up = ldexp(1.0, bits);
-    double xr = x.x * inv, xi = x.y * inv;
-    for (int p = 0; p < S; ++p) {
-      const double dr = rint(xr), di = rint(xi);
-      xr = (xr - dr) * up;
-      xi = (xi - di) * up;
+    // The top digit is rint(x) in FP64; the remainder (|·| ≤ ½) becomes one integer of
+    // b·(S−1) fraction bits (≤ 2^55: exact in int64), whose balanced base-2^b digits are
+    // peeled off from the bottom with integer operations (the FP64 pipe is the scarce one
+    // on this part); the carry left after S−1 digits (−1, 0 or 1) goes to the top digit.
+    const double inv = ldexp(1.0 / scale[b * R + r], bits - 2);  // powers of two: exact
+    const double xr = x.x * inv, xi = x.y * inv;
+    const double tr = rint(xr), ti = rint(xi);
+    const double lo_scale = ldexp(1.0, bits * (S - 1));
+    long long Xr = llrint((xr - tr) * lo_scale), Xi = llrint((xi - ti) * lo_scale);
+    const long long half = 1ll << (bits - 1), mask = (1ll << bits) - 1;
+    int dr[OZ_MAX_S], di[OZ_MAX_S];
+#pragma unroll
+    for (int p = OZ_MAX_S - 1; p >= 1; --p) {
+      if (p < S) {
+        const long long lr = ((Xr + half) & mask) - half, li = ((Xi + half) & mask) - half;
+        Xr = (Xr - lr) >> bits;
+        Xi = (Xi - li) >> bits;
+        dr[p] = (int)lr;
+        di[p] = (int)li;
+      }
+    }
+    dr[0] = (int)tr + (int)Xr;
+    di[0] = (int)ti + (int)Xi;
+#pragma unroll
+    for (int p = 0; p < OZ_MAX_S; ++p) {
+      if (p >= S) break;
       unsigned short* o = out + ((int64_t)p * batch + b) * plane;
+      const double vr = (double)dr[p], vi = (double)di[p];
       if (a_form) {
-        o[(2 * r) * pitch + c] = bf16_bits(dr);
-        o[(2 * r) * pitch + K + c] = bf16_bits(-di);
-        o[(2 * r + 1) * pitch + c] = bf16_bits(di);
-        o[(2 * r + 1) * pitch + K + c] = bf16_bits(dr);
+        o[(2 * r) * pitch + c] = bf16_bits(vr);
+        o[(2 * r) * pitch + K + c] = bf16_bits(-vi);
+        o[(2 * r + 1) * pitch + c] = bf16_bits(vi);
+        o[(2 * r + 1) * pitch + K + c] = bf16_bits(vr);
       } else {
-        o[r * pitch + c] = bf16_bits(dr);
-        o[r * pitch + K + c] = bf16_bits(di);
+        o[r * pitch + c] = bf16_bits(vr);
+        o[r * pitch + K + c] = bf16_bits(vi);
       }
     }
   }

@@ -172,7 +172,16 @@ struct tn_ctx {
   // diagnostics of the last Jacobi SVD: sweeps per precision, rotations per sweep of
   // the worst active matrix of the large-matrix path (-1: shared-memory path)
   int last_sweeps_fp32 = 0, last_sweeps_fp64 = 0;
-  int last_refine_iters = 0;  // refinement iterations of the last truncated mixed SVD
+  int last_refine_iters = 0;     // refinement iterations of the last truncated mixed SVD
+  int last_refine_clusters = 0;  // its near-degenerate pairs left to the FP64 check
+  // cumulative over the context: truncated mixed SVD calls, refinement iterations, marked
+  // pairs, calls finished by the full FP64 sweeps
+  int64_t refine_totals[4] = {0, 0, 0, 0};
+  // the last truncated mixed SVD: per iteration the largest step, the largest |R_ij|, the
+  // largest ‖E‖_F and the marked pairs; outcome 0 converged, 1 diverged (FP64 sweeps from
+  // the pre-pass basis), 2 out of iterations (FP64 sweeps from the refined basis)
+  float refine_trace[8][4] = {};
+  int refine_outcome = 0;
   int sweep_rotations[64] = {0};
   float sweep_ratio[64] = {0};  // largest off-diagonal ratio of each sweep (worst active matrix)
   // time of the last DMRG run per phase (ms): gauge moves, environments, eigensolves,

@@ -1048,11 +1048,15 @@ tn_status_t evolve_mpo_direct(tn_mps* p, const std::vector<const cxd*>& hW, cons
   return TN_OK;
 }
 
-// zip-up (evolve.jl:49-129), one instance
+// zip-up (evolve.jl:49-129), every instance of the MPS in lockstep: the carried block,
+// the contractions and the truncated SVDs are batched over the B instances (instance
+// stride = the largest block), the common new bond is the largest kept rank, and an
+// instance's surplus singular values are zero (rank_select_batched), so each instance
+// carries exactly its own truncated state
 tn_status_t evolve_mpo_zipup(tn_mps* p, const std::vector<const cxd*>& hW, const std::vector<int64_t>& w,
                              int64_t maxdim, double threshold) {
   tn_ctx* ctx = p->ctx;
-  const int L = p->L, d = p->d;
+  const int L = p->L, d = p->d, B = p->B;
   std::vector<int64_t> ob(p->bond);  // bonds before the sweep
   int64_t mx = 1, wm = 1;
   for (int i = 0; i <= L; ++i) {
@@ -1062,66 +1066,72 @@ tn_status_t evolve_mpo_zipup(tn_mps* p, const std::vector<const cxd*>& hW, const
   const int64_t km = std::max<int64_t>(d * mx * wm, 1);  // largest carried bond before truncation
   const int64_t big = km * d * mx * wm;                   // largest (k o) × (r b) block
   const int64_t rows = km * d, cols = mx * wm, kk = std::min(rows, cols);
-  const size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(wm * d * d * wm)) + 5 * ws_round(sizeof(cxd) * (size_t)big) +
-                      ws_round(sizeof(cxd) * (size_t)(rows * kk)) + ws_round(sizeof(double) * (size_t)kk) +
-                      ws_round(sizeof(cxd) * (size_t)(kk * cols)) + svd_any_workspace(TN_C64, p->prec, rows, cols, 1);
+  const size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(wm * d * d * wm)) +
+                      5 * ws_round(sizeof(cxd) * (size_t)(big * B)) + ws_round(sizeof(cxd) * (size_t)(rows * kk * B)) +
+                      ws_round(sizeof(double) * (size_t)(kk * B)) + ws_round(sizeof(cxd) * (size_t)(kk * cols * B)) +
+                      svd_any_workspace(TN_C64, p->prec, rows, cols, B);
   TN_RETURN_IF(ws_reserve(ctx, need));
   cxd* W0 = ws_take<cxd>(ctx, (size_t)(wm * d * d * wm));
   cxd* W1 = ws_take<cxd>(ctx, (size_t)(wm * d * d * wm));
-  cxd* R = ws_take<cxd>(ctx, (size_t)big);
-  cxd* X = ws_take<cxd>(ctx, (size_t)big);
-  cxd* Y = ws_take<cxd>(ctx, (size_t)big);
-  cxd* T = ws_take<cxd>(ctx, (size_t)big);
-  cxd* Tm = ws_take<cxd>(ctx, (size_t)big);
-  cxd* U = ws_take<cxd>(ctx, (size_t)(rows * kk));
-  double* S = ws_take<double>(ctx, (size_t)kk);
-  cxd* Vh = ws_take<cxd>(ctx, (size_t)(kk * cols));
-  set_one(ctx, R, 1, 1);  // the carried block before site 1: (k = 1, χ_0 = 1, w_0 = 1)
+  cxd* R = ws_take<cxd>(ctx, (size_t)(big * B));
+  cxd* X = ws_take<cxd>(ctx, (size_t)(big * B));
+  cxd* Y = ws_take<cxd>(ctx, (size_t)(big * B));
+  cxd* T = ws_take<cxd>(ctx, (size_t)(big * B));
+  cxd* Tm = ws_take<cxd>(ctx, (size_t)(big * B));
+  cxd* U = ws_take<cxd>(ctx, (size_t)(rows * kk * B));
+  double* S = ws_take<double>(ctx, (size_t)(kk * B));
+  cxd* Vh = ws_take<cxd>(ctx, (size_t)(kk * cols * B));
+  TN_RETURN_IF(set_one(ctx, R, big, B));  // the carried block before site 1: (k = 1, χ_0 = 1, w_0 = 1)
   int64_t k = 1;
   for (int i = 1; i <= L; ++i) {
     const int64_t c = ob[i - 1], r = ob[i], a = w[i - 1], b = w[i];
     TN_CHECK_CUDA(ctx, cudaMemcpyAsync(W0, hW[i - 1], sizeof(cxd) * a * d * d * b, cudaMemcpyHostToDevice, ctx->stream));
-    // R (k, c, a) → (k, a, c);  X ((k a) × (s r)) = R' ((k a) × c) · A (c × (s r))
+    // R (k, c, a) → (k, a, c) per instance (the last mode is the instance, stride big)
     {
-      const int64_t dims[3] = {k, c, a};
-      const int32_t perm[3] = {0, 2, 1};
-      TN_RETURN_IF(permute_t<pd2>(ctx, 3, dims, nullptr, perm, (const pd2*)R, (pd2*)Y, false));
+      const int64_t dims[4] = {k, c, a, B};
+      const int64_t str[4] = {1, k, k * c, big};
+      const int32_t perm[4] = {0, 2, 1, 3};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 4, dims, str, perm, (const pd2*)R, (pd2*)Y, false));
     }
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k * a, d * r, c, kOne, Y, k * a, 0, p->site[i], c, 0, kZero, X, k * a, 0, 1));
-    // X (k, a, s, r) → (k, r, a, s);  W (a, o, s, b) → (a, s, o, b)
+    // X ((k a) × (s r)) = R' ((k a) × c) · A (c × (s r)), Y packed at stride k·a·c
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k * a, d * r, c, kOne, Y, k * a, k * a * c, p->site[i], c, p->cap[i],
+                                 kZero, X, k * a, big, B));
+    // X (k, a, s, r) → (k, r, a, s) per instance;  W (a, o, s, b) → (a, s, o, b)
     {
-      const int64_t dims[4] = {k, a, d, r};
-      const int32_t perm[4] = {0, 3, 1, 2};
-      TN_RETURN_IF(permute_t<pd2>(ctx, 4, dims, nullptr, perm, (const pd2*)X, (pd2*)Y, false));
+      const int64_t dims[5] = {k, a, d, r, B};
+      const int64_t str[5] = {1, k, k * a, k * a * d, big};
+      const int32_t perm[5] = {0, 3, 1, 2, 4};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 5, dims, str, perm, (const pd2*)X, (pd2*)Y, false));
       const int64_t wd[4] = {a, d, d, b};
       const int32_t wp[4] = {0, 2, 1, 3};
       TN_RETURN_IF(permute_t<pd2>(ctx, 4, wd, nullptr, wp, (const pd2*)W0, (pd2*)W1, false));
     }
-    // T ((k r) × (o b)) = Y ((k r) × (a s)) · W' ((a s) × (o b))
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k * r, d * b, a * d, kOne, Y, k * r, 0, W1, a * d, 0, kZero, T, k * r, 0, 1));
-    // T (k, r, o, b) → (k, o, r, b): the matrix ((k o) × (r b))
-    {
-      const int64_t dims[4] = {k, r, d, b};
-      const int32_t perm[4] = {0, 2, 1, 3};
-      TN_RETURN_IF(permute_t<pd2>(ctx, 4, dims, nullptr, perm, (const pd2*)T, (pd2*)Tm, false));
-    }
+    // T ((k r) × (o b)) = Y ((k r) × (a s)) · W' ((a s) × (o b)); Y packed at stride k·r·a·d
+    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'N', k * r, d * b, a * d, kOne, Y, k * r, k * r * a * d, W1, a * d, 0, kZero,
+                                 T, k * r, big, B));
+    // T (k, r, o, b) → (k, o, r, b): the matrix ((k o) × (r b)), packed at stride m·n
     const int64_t m = k * d, n = r * b;
+    {
+      const int64_t dims[5] = {k, r, d, b, B};
+      const int64_t str[5] = {1, k, k * r, k * r * d, big};
+      const int32_t perm[5] = {0, 2, 1, 3, 4};
+      TN_RETURN_IF(permute_t<pd2>(ctx, 5, dims, str, perm, (const pd2*)T, (pd2*)Tm, false));
+    }
     if (i == L) {  // last site: (k, o, 1)
       TN_RETURN_IF(ensure_site(p, i, (size_t)(k * d)));
-      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], Tm, sizeof(cxd) * k * d, cudaMemcpyDeviceToDevice, ctx->stream));
+      TN_RETURN_IF(copy_instances(ctx, p->site[i], p->cap[i], Tm, (size_t)(m * n), (size_t)(k * d), B));
       p->bond[i - 1] = k;
       break;
     }
     const int64_t kmin = std::min(m, n);
-    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, Tm, m, 0, U, 0, S, 0, Vh, 0, 1));
+    TN_RETURN_IF(svd_any(ctx, TN_C64, p->prec, m, n, Tm, m, m * n, U, m * kmin, S, kmin, Vh, kmin * n, B));
     int64_t rk = 0;
-    TN_RETURN_IF(rank_select(ctx, S, kmin, maxdim, threshold, &rk));
+    TN_RETURN_IF(rank_select_batched(ctx, S, kmin, kmin, B, maxdim, threshold, &rk, nullptr));
     // site i = U[:, :rk] as (k, o, rk);  R = diag(S[:rk]) Vh[:rk, :] as (rk, r, b)
     TN_RETURN_IF(ensure_site(p, i, (size_t)(m * rk)));
-    TN_CHECK_CUDA(ctx, cudaMemcpyAsync(p->site[i], U, sizeof(cxd) * m * rk, cudaMemcpyDeviceToDevice, ctx->stream));
-    TN_RETURN_IF(copy_matrix_cxd(ctx, rk, n, Vh, kmin, R, rk));
-    TN_RETURN_IF(scale_rows_sqrt<double>(ctx, R, rk, n, rk, S));  // √S …
-    TN_RETURN_IF(scale_rows_sqrt<double>(ctx, R, rk, n, rk, S));  // … twice: S
+    TN_RETURN_IF(copy_instances(ctx, p->site[i], p->cap[i], U, (size_t)(m * kmin), (size_t)(m * rk), B));
+    TN_RETURN_IF(copy_matrix_cxd(ctx, rk, n, Vh, kmin, R, rk, kmin * n, big, B));
+    TN_RETURN_IF(scale_rows_mode(ctx, R, rk, n, rk, S, big, kmin, B, 1));
     p->bond[i - 1] = k;
     k = rk;
     TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // W0 came from pageable host memory
@@ -1154,7 +1164,6 @@ tn_status_t tn_mps_evolve_mpo(tn_mps* p, const void* const* h_mpo_sites, const i
   if (algorithm == 0) return evolve_mpo_direct(p, hW, w);
   TN_ARG(ctx, algorithm == 1, "evolve: algorithm must be 0 (direct) or 1 (zip-up)");
   TN_ARG(ctx, maxdim > 0 || threshold > 0, "Either `maxdim` or `threhold` must be specified");
-  TN_ARG(ctx, p->B == 1, "evolve: the zip-up runs on single-instance MPS");
   if (p->kind == TN_FORM_BOND) TN_RETURN_IF(tn_mps_canonize_mixed(p, p->lo, p->lo));  // absorb Λ
   return evolve_mpo_zipup(p, hW, w, maxdim, threshold);
 }

@@ -28,7 +28,10 @@
 
 namespace {
 
-constexpr int kMaxSweeps = 40;
+// one-sided Jacobi converges quadratically at the end but only linearly while a wide,
+// smoothly decaying spectrum (e.g. 512 values over 14 decades) is being sorted out: such
+// matrices take 40-60 sweeps
+constexpr int kMaxSweeps = 80;
 constexpr size_t kSmemMax = 200 * 1024;
 
 template <typename T>
@@ -998,7 +1001,7 @@ template <typename T>
 static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T>* V, int64_t batch, bool v_given,
                                int* active, int* rotated, T* nrm, int max_sweeps, int* sweeps_out, bool* noconv_out,
                                unsigned char* tail = nullptr, int64_t keep = 0, bool tail_preset = false,
-                               double min_rot_frac = 0.0) {
+                               double min_rot_frac = 0.0, bool tail_fixed = false) {
   if (!(tail && keep > 0 && keep < n && n <= 4096)) {
     tail = nullptr;
     keep = 0;
@@ -1125,7 +1128,7 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
         TN_CHECK_CUDA(ctx, cudaMemsetAsync(tail, 0, (size_t)(n * batch), ctx->stream));
         tail = nullptr;
       }
-      if (tail && n_active > 0 && (tail_preset || 2 * max_rot < pairs))
+      if (tail && !tail_fixed && n_active > 0 && (tail_preset || 2 * max_rot < pairs))
         TN_RETURN_IF(update_tail_flags<T>(ctx, n, batch, nrm, keep, tail));
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
     }
@@ -1262,12 +1265,26 @@ __global__ void k_ortho_poly(int64_t n, int64_t batch, cxd* G, const cxf* E2, co
 // which converges quadratically once the columns are separated.  Every product is a
 // split-BF16 tensor-core GEMM whose digit planes are scaled per row and per column, so
 // S_ij is accurate to ~ε·σ_i·σ_j (graded, like one-sided Jacobi) and the σ_i come out
-// with relative accuracy.  A pair whose first-order step exceeds kRefineStepMax (a
-// near-degenerate pair) gets the orthogonality part R_ij/2 only and is left to one FP64
-// Jacobi check afterwards; pairs of two tail columns (ranked below the kept set) are only
-// kept orthogonal.
+// with relative accuracy.  Per pair (i, j), with num = S_ij + λ_j R_ij, den = λ_j − λ_i,
+// λ = max(λ_i, λ_j) and |num| the larger of |S_ij + λ_j R_ij| and |S_ij + λ_i R_ij| (the
+// same for both orders of the pair):
+//   * |num| ≤ kRefineNoise·λ: the pair is converged (its coupling is at the rounding level
+//     of the products); only the orthogonality part R_ij/2 is applied, so no rotation is
+//     driven by noise;
+//   * |num| ≤ kRefineStepMax·|den| and |den| > kRefineGapMin·λ: the first-order step;
+//   * otherwise (a near-degenerate pair, or one the pre-pass left far from converged):
+//     R_ij/2 only, and both columns are marked for the FP64 one-sided Jacobi of the
+//     marked columns afterwards.
+// Pairs of two tail columns (ranked below the kept set by the current λ) are only kept
+// orthogonal.  The noise floor makes the steps that are applied at most
+// kRefineNoise/kRefineGapMin (1e-8) when only rounding drives them, so the iteration
+// ends: after a step of at most kRefineStop the deviation left is its square.
 // ---------------------------------------------------------------------------------
 constexpr double kRefineStepMax = 0.1;
+constexpr double kRefineGapMin = 1e-6;
+constexpr double kRefineNoise = 1e-14;
+constexpr float kRefineStop = 1e-8f;
+constexpr double kRefineNormMax = 0.5;  // ‖E‖_F above which the first-order steps diverge
 constexpr int kRefineMaxIter = 6;
 
 __global__ void k_set_identity_cxd(int64_t n, int64_t batch, cxd* X) {
@@ -1278,42 +1295,208 @@ __global__ void k_set_identity_cxd(int64_t n, int64_t batch, cxd* X) {
   }
 }
 
-// λ_i = Re S_ii / (1 − Re R_ii)
+// λ_i = Re S_ii / (1 − Re R_ii); stat[4b + 2] = max_i λ_i (float bits)
 __global__ void k_refine_lambda(int64_t n, int64_t batch, const cxd* __restrict__ S, const cxd* __restrict__ R,
-                                double* __restrict__ lam) {
+                                double* __restrict__ lam, int* stat) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n * batch; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t b = t / n, i = t % n, d = b * n * n + i + i * n;
-    lam[t] = S[d].x / (1.0 - R[d].x);
+    const double l = S[d].x / (1.0 - R[d].x);
+    lam[t] = l;
+    if (l > 0.0) atomicMax(&stat[4 * b + 2], __float_as_int((float)l));
   }
 }
 
-// E (in place over R); emax[b] = the largest applied |E_ij| (float bits), clusters[b] =
-// pairs with a kept column left to the FP64 check
-__global__ void k_refine_step(int64_t n, int64_t batch, const cxd* __restrict__ S, cxd* RE,
-                              const double* __restrict__ lam, const unsigned char* __restrict__ tail, int* emax,
-                              int* clusters) {
-  const int64_t total = n * n * batch;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t b = t / (n * n), w = t % (n * n), i = w % n, j = w / n;
-    const cxd r = RE[t];
+// the pairs the refinement diagonalises: not two tail columns, neither column numerically
+// zero (λ ≤ n·ε²·λ_max: its U column is completed orthonormally at the end)
+__device__ __forceinline__ bool refine_pair(int64_t n, int64_t b, int64_t i, int64_t j, const unsigned char* tail,
+                                            double li, double lj, const int* stat) {
+  if (tail && tail[b * n + i] && tail[b * n + j]) return false;
+  const double negl = (double)n * 4.93e-32 * (double)__int_as_float(stat[4 * b + 2]);
+  return li > negl && lj > negl;
+}
+
+// E (in place over R) by the per-pair rule above; grid (·, batch), one matrix per grid
+// row, so each warp reduces its statistics before one atomic per warp.  stat[4b] = the
+// largest applied step |E_ij| (float bits), stat[4b + 1] = marked pairs, stat[4b + 3] =
+// the largest |R_ij|; esq[b] = ‖E‖²_F of the applied steps.
+__global__ void __launch_bounds__(256)
+    k_refine_step(int64_t n, const cxd* __restrict__ S, cxd* RE, const double* __restrict__ lam,
+                  const unsigned char* __restrict__ tail, int* stat, double* __restrict__ esq,
+                  unsigned char* __restrict__ cluster) {
+  const int64_t b = blockIdx.y, nn = n * n;
+  const cxd* Sb = S + b * nn;
+  cxd* Rb = RE + b * nn;
+  float emax = 0.f, rmax = 0.f;
+  double e2 = 0.0;
+  int marked = 0;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < nn; w += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = w % n, j = w / n;
+    const cxd r = Rb[w];
+    rmax = fmaxf(rmax, (float)sqrt(r.x * r.x + r.y * r.y));
     cxd e = mkcx(0.5 * r.x, 0.5 * r.y);
     if (i != j) {
-      const bool both_tail = tail && tail[b * n + i] && tail[b * n + j];
-      if (!both_tail) {
-        const double li = lam[b * n + i], lj = lam[b * n + j], den = lj - li;
-        const cxd sij = S[t];
+      const double li = lam[b * n + i], lj = lam[b * n + j];
+      if (refine_pair(n, b, i, j, tail, li, lj, stat)) {
+        const double den = lj - li, big = fmax(li, lj);
+        const cxd sij = Sb[w];
         const cxd num = mkcx(sij.x + lj * r.x, sij.y + lj * r.y);
-        const double mag = sqrt(num.x * num.x + num.y * num.y);
-        if (fabs(den) > 0.0 && mag <= kRefineStepMax * fabs(den)) {
+        // the pair is classified by the larger of |num_ij| and |num_ji| = |S_ij + λ_i R_ij|,
+        // so E_ij and E_ji always come from the same rule: then E_ij + conj(E_ji) = R_ij and
+        // the first-order part of the new S_ij cancels (a pair split between the rules
+        // would keep a coupling of the size of λ·R_ij)
+        const double nx = sij.x + li * r.x, ny = sij.y + li * r.y;
+        const double mag = fmax(sqrt(num.x * num.x + num.y * num.y), sqrt(nx * nx + ny * ny));
+        if (mag <= kRefineNoise * big) {
+          // converged pair: orthogonality only
+        } else if (mag <= kRefineStepMax * fabs(den) && fabs(den) > kRefineGapMin * big) {
           e = mkcx(num.x / den, num.y / den);
-          atomicMax(&emax[b], __float_as_int((float)(mag / fabs(den))));
-        } else if (mag > 0.0) {
-          atomicAdd(&clusters[b], 1);
+          const double st = mag / fabs(den);
+          emax = fmaxf(emax, (float)st);
+          e2 += st * st;
+        } else {
+          ++marked;
+          cluster[b * n + i] = 1;
+          cluster[b * n + j] = 1;
         }
       }
     }
-    RE[t] = e;
+    Rb[w] = e;
   }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+    rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  }
+  e2 = warp_sum(e2);
+  marked = warp_sum(marked);
+  if ((threadIdx.x & 31) == 0) {
+    if (emax > 0.f) atomicMax(&stat[4 * b], __float_as_int(emax));
+    if (rmax > 0.f) atomicMax(&stat[4 * b + 3], __float_as_int(rmax));
+    if (marked) atomicAdd(&stat[4 * b + 1], marked);
+    if (e2 > 0.0) atomicAdd(&esq[b], e2);
+  }
+}
+
+// FP64 one-sided Jacobi of the marked columns of each matrix, in shared memory: one CTA
+// per matrix, the k marked columns of W (m rows) loaded once; each round-robin round
+// gives one warp per disjoint pair (dot products by warp shuffles, the rotation formed
+// by every lane identically, as make_rot_c forms it for the sweep kernels); sweeps until
+// one rotates nothing.  The same rotations are applied to the columns of V (n rows, in
+// place in global memory) when V is given, so W = A·V still holds.  Inside the
+// refinement this removes the marked pairs' coupling, which would otherwise feed every
+// coupling of the marked columns back at the rate coupling/gap per iteration (linear
+// convergence).  A rotation inside the marked set leaves the columns as orthogonal to
+// the unmarked ones as they were.  status[b]: 0 done,
+// 1 more than kmax marked columns (nothing changed), 2 not converged in max_sweeps.
+// The column list is built by ballots in column order, so the result is deterministic.
+template <int NT>
+__global__ void __launch_bounds__(NT)
+    k_cluster_jacobi(int64_t m, int64_t n, cxd* __restrict__ W, int64_t sW, cxd* __restrict__ V, int64_t sV,
+                     const unsigned char* __restrict__ cluster, int kmax, double tol, const int* __restrict__ stat,
+                     int max_sweeps, int* __restrict__ status) {
+  extern __shared__ unsigned char smem_raw[];
+  cxd* Ws = reinterpret_cast<cxd*>(smem_raw);
+  int* idx = reinterpret_cast<int*>(Ws + (size_t)m * kmax);
+  __shared__ int s_count, s_rot;
+  constexpr int NW = NT / 32;
+  const int64_t b = blockIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) {
+    int count = 0;
+    for (int64_t base = 0; base < n; base += 32) {
+      const bool f = base + lane < n && cluster[b * n + base + lane];
+      const unsigned mask = __ballot_sync(0xffffffffu, f);
+      const int pos = count + __popc(mask & ((1u << lane) - 1u));
+      if (f && pos < kmax) idx[pos] = (int)(base + lane);
+      count += __popc(mask);
+    }
+    if (lane == 0) s_count = count;
+  }
+  __syncthreads();
+  const int k = s_count;
+  if (k > kmax) {
+    if (threadIdx.x == 0) status[b] = 1;
+    return;
+  }
+  if (threadIdx.x == 0) status[b] = 0;
+  if (k < 2) return;
+  cxd* Wb = W + b * sW;
+  for (int c = 0; c < k; ++c)
+    for (int64_t r = threadIdx.x; r < m; r += NT) Ws[(size_t)c * m + r] = Wb[(int64_t)idx[c] * m + r];
+  const double negl = (double)n * 4.93e-32 * (double)__int_as_float(stat[4 * b + 2]);
+  const int K = k + (k & 1);
+  int sweep = 0;
+  bool any = false;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (threadIdx.x == 0) s_rot = 0;
+    __syncthreads();
+    for (int r = 0; r < K - 1; ++r) {
+      for (int p = warp; p < K / 2; p += NW) {
+        int i, j;
+        rr_pair(K, r, p, i, j);
+        if (j >= k) continue;
+        cxd* wi = Ws + (size_t)i * m;
+        cxd* wj = Ws + (size_t)j * m;
+        cxd g = mkcx(0.0, 0.0);
+        double al = 0.0, be = 0.0;
+        for (int64_t t = lane; t < m; t += 32) {
+          const cxd x = wi[t], y = wj[t];
+          cfma_cj(g, x, y);
+          al += abs2(x);
+          be += abs2(y);
+        }
+        g.x = warp_sum(g.x);
+        g.y = warp_sum(g.y);
+        al = warp_sum(al);
+        be = warp_sum(be);
+        const RotC<double> Rt = make_rot_c(al, be, g, tol, negl);
+        if (!Rt.apply) continue;
+        if (lane == 0) s_rot = 1;
+        for (int64_t t = lane; t < m; t += 32) {
+          cxd x = wi[t], y = wj[t];
+          rot_apply_c(Rt.c, Rt.se, x, y);
+          wi[t] = x;
+          wj[t] = y;
+        }
+        if (V) {
+          cxd* vi = V + b * sV + (int64_t)idx[i] * n;
+          cxd* vj = V + b * sV + (int64_t)idx[j] * n;
+          for (int64_t t = lane; t < n; t += 32) {
+            cxd x = vi[t], y = vj[t];
+            rot_apply_c(Rt.c, Rt.se, x, y);
+            vi[t] = x;
+            vj[t] = y;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    const int rotated = s_rot;
+    __syncthreads();
+    if (!rotated) break;
+    any = true;
+  }
+  if (sweep == max_sweeps && threadIdx.x == 0) status[b] = 2;
+  if (!any) return;
+  for (int c = 0; c < k; ++c)
+    for (int64_t r = threadIdx.x; r < m; r += NT) Wb[(int64_t)idx[c] * m + r] = Ws[(size_t)c * m + r];
+}
+
+__global__ void k_scale_real_cxd(int64_t count, cxd* X, double f) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x)
+    X[t] = mkcx(f * X[t].x, f * X[t].y);
+}
+tn_status_t scale_real_cxd(tn_ctx* ctx, cxd* X, int64_t count, double f) {
+  k_scale_real_cxd<<<(unsigned)std::min<int64_t>((count + 255) / 256, 4096), 256, 0, ctx->stream>>>(count, X, f);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+// the FP64 check's flags: every column outside a near-degenerate pair counts as tail, so
+// only pairs with a marked column are examined
+__global__ void k_cluster_flags(int64_t count, const unsigned char* __restrict__ cluster, unsigned char* __restrict__ f) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x)
+    f[t] = cluster[t] ? 0 : 1;
 }
 
 size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
@@ -1329,6 +1512,7 @@ size_t svd_mixed_workspace(int64_t m, int64_t n, int64_t batch) {
   s += ws_round(sizeof(cxf) * (size_t)(n * n * batch));  // E³ when W32 has no room for it
   s += ws_round((size_t)(n * batch));                     // tail flags
   s += ws_round(sizeof(cxd) * (size_t)(n * n * batch));  // R / E of the refinement
+  s += ws_round((size_t)(n * batch)) + ws_round(sizeof(int) * (size_t)(5 * batch + 4));  // cluster marks, stats
   return s;
 }
 
@@ -1363,6 +1547,8 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
   float* nrm32 = ws_take<float>(ctx, (size_t)((n + 1) * batch));
   unsigned char* tail = ws_take<unsigned char>(ctx, (size_t)(n * batch));
   cxd* RE = ws_take<cxd>(ctx, (size_t)(n * n * batch));
+  unsigned char* cluster = ws_take<unsigned char>(ctx, (size_t)(n * batch));
+  int* stat = ws_take<int>(ctx, (size_t)(5 * batch + 4));
   const int64_t keep_m = (!want_v && keep > 0) ? keep + std::max<int64_t>(16, keep / 8) : 0;
   for (int64_t b = 0; b < batch; ++b) {
     int64_t blocks = std::min<int64_t>((m * n + 255) / 256, 2048);
@@ -1392,38 +1578,87 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
     const unsigned blocks = (unsigned)std::min<int64_t>((n * n * batch + 255) / 256, 4096);
     const unsigned lblocks = (unsigned)std::min<int64_t>((n * batch + 255) / 256, 1024);
     const cxd one = mkcx(1.0, 0.0), zero = mkcx(0.0, 0.0), mone = mkcx(-1.0, 0.0);
-    std::vector<int> h_stat(2 * batch);
-    bool w_current = false;
+    std::vector<int> h_stat(4 * batch);
+    std::vector<double> h_esq(batch);
+    double* esq = nrm64 + n * batch;  // free during the refinement (the sweeps use it for ‖A‖²_F)
+    int* cstat = stat + 4 * batch;    // status of the marked-column Jacobi
+    const int kmax = (int)std::min<int64_t>(n, (int64_t)(kSmemMax / (sizeof(cxd) * (size_t)m + sizeof(int))));
+    if (kmax >= 2)
+      TN_CHECK_CUDA(ctx, cudaFuncSetAttribute(k_cluster_jacobi<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)kSmemMax));
+    // the marked-column Jacobi on W (and V when given); returns whether it ran
+    auto cluster_jacobi = [&](cxd* Vr) -> tn_status_t {
+      const size_t smem = sizeof(cxd) * (size_t)m * kmax + sizeof(int) * (size_t)kmax;
+      TN_CHECK_CUDA(ctx, cudaMemsetAsync(cstat, 0, sizeof(int) * (size_t)batch, ctx->stream));
+      k_cluster_jacobi<512><<<(unsigned)batch, 512, smem, ctx->stream>>>(m, n, W64, m * n, Vr, n * n, cluster, kmax,
+                                                                          jacobi_tol<double>(m), stat, 40, cstat);
+      TN_LAUNCHED(ctx);
+      return TN_OK;
+    };
+    bool w_fresh = false, converged = false, diverged = false, cluster_ran = false;
     int clusters = 0;
+    float emax = 0.f, rmax = 0.f;
     ctx->last_refine_iters = 0;
     for (int it = 0; it < kRefineMaxIter; ++it) {
-      TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, one, A, lda, sA, V64, n, n * n, zero, W64, m, m * n,
-                            batch));
+      TN_CHECK_CUDA(ctx, cudaMemsetAsync(cluster, 0, (size_t)(n * batch), ctx->stream));
+      if (!w_fresh)
+        TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, one, A, lda, sA, V64, n, n * n, zero, W64, m,
+                              m * n, batch));
+      w_fresh = true;
+      cluster_ran = false;
       TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'C', 'N', n, n, m, one, W64, m, m * n, W64, m, m * n, zero, G, n, n * n,
                             batch));
       k_set_identity_cxd<<<blocks, 256, 0, ctx->stream>>>(n, batch, RE);
       TN_LAUNCHED(ctx);
       TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'C', 'N', n, n, n, mone, V64, n, n * n, V64, n, n * n, one, RE, n, n * n,
                             batch));
-      k_refine_lambda<<<lblocks, 256, 0, ctx->stream>>>(n, batch, G, RE, nrm64);
+      TN_CHECK_CUDA(ctx, cudaMemsetAsync(stat, 0, sizeof(int) * 4 * batch, ctx->stream));
+      TN_CHECK_CUDA(ctx, cudaMemsetAsync(esq, 0, sizeof(double) * batch, ctx->stream));
+      k_refine_lambda<<<lblocks, 256, 0, ctx->stream>>>(n, batch, G, RE, nrm64, stat);
       TN_LAUNCHED(ctx);
-      TN_CHECK_CUDA(ctx, cudaMemsetAsync(rotated, 0, sizeof(int) * 2 * batch, ctx->stream));
-      k_refine_step<<<blocks, 256, 0, ctx->stream>>>(n, batch, G, RE, nrm64, tail, rotated, rotated + batch);
-      TN_LAUNCHED(ctx);
-      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_stat.data(), rotated, sizeof(int) * 2 * batch, cudaMemcpyDeviceToHost,
+      // the kept set by the current λ (the pre-pass ranked the columns by FP32 norms, which
+      // cannot order values below ~1e-7 of the largest)
+      TN_RETURN_IF(update_tail_flags<double>(ctx, n, batch, nrm64, keep_m, tail));
+      {
+        const dim3 sg((unsigned)std::min<int64_t>((n * n + 255) / 256, std::max<int64_t>(1, 4096 / batch)),
+                      (unsigned)batch);
+        k_refine_step<<<sg, 256, 0, ctx->stream>>>(n, G, RE, nrm64, tail, stat, esq, cluster);
+        TN_LAUNCHED(ctx);
+      }
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_stat.data(), stat, sizeof(int) * 4 * batch, cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+      TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_esq.data(), esq, sizeof(double) * batch, cudaMemcpyDeviceToHost,
                                          ctx->stream));
       TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-      float emax = 0.f;
+      emax = 0.f;
+      rmax = 0.f;
+      double enorm = 0.0;
+      bool finite = true;
       clusters = 0;
       for (int64_t b = 0; b < batch; ++b) {
-        float e;
-        memcpy(&e, &h_stat[b], sizeof(float));
+        float e, r;
+        memcpy(&e, &h_stat[4 * b], sizeof(float));
+        memcpy(&r, &h_stat[4 * b + 3], sizeof(float));
+        finite = finite && std::isfinite(e) && std::isfinite(r) && std::isfinite(h_esq[b]);
         emax = std::max(emax, e);
-        clusters += h_stat[batch + b];
+        rmax = std::max(rmax, r);
+        enorm = std::max(enorm, sqrt(h_esq[b]));
+        clusters += h_stat[4 * b + 1];
       }
       ctx->last_refine_iters = it + 1;
-      if (emax < 1e-15f) {  // the correction is below FP64 resolution: W = A·V is final
-        w_current = true;
+      ctx->refine_trace[it][0] = emax;
+      ctx->refine_trace[it][1] = rmax;
+      ctx->refine_trace[it][2] = (float)enorm;
+      ctx->refine_trace[it][3] = (float)clusters;
+      // outside the quadratic regime (a basis the FP32 pre-pass could not resolve, e.g.
+      // values below ~1e-7 of the largest inside the kept set): the first-order steps
+      // would not converge, so the FP64 sweeps take over from the pre-pass basis
+      if (!finite || enorm > kRefineNormMax || rmax > 0.25f || (it >= 3 && emax > 1e-3f)) {
+        diverged = true;
+        break;
+      }
+      if (emax == 0.f && rmax <= 1e-15f && clusters == 0) {  // nothing to correct: W = A·V is final
+        converged = true;
         break;
       }
       // V ← V + V·E
@@ -1432,17 +1667,82 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
       TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', n, n, n, one, V64, n, n * n, RE, n, n * n, one, V, n, n * n,
                             batch));
       std::swap(V, V64);
-      // quadratic convergence: a step below 1e-10 leaves ~1e-20 (the floor is ε over the
-      // smallest relative gap, which further steps do not lower)
-      if (emax < 1e-10f) break;
+      w_fresh = false;
+      if (clusters > 0 && kmax >= 2) {
+        // W = A·V for the new basis, then the marked pairs are rotated in both
+        TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, one, A, lda, sA, V64, n, n * n, zero, W64, m,
+                              m * n, batch));
+        TN_RETURN_IF(cluster_jacobi(V64));
+        w_fresh = cluster_ran = true;
+      }
+      // quadratic convergence: steps and non-orthogonality of at most kRefineStop leave
+      // their squares (≤ 1e-16)
+      if (emax <= kRefineStop && rmax <= kRefineStop) {
+        converged = true;
+        break;
+      }
     }
-    if (!w_current)
+    ctx->refine_outcome = converged ? 0 : (diverged ? 1 : 2);
+    bool restored = false;
+    if (!converged) {
+      if (diverged) {
+        // back to the pre-pass basis
+        const int64_t cnt = n * n * batch;
+        k_f2d<<<(unsigned)std::min<int64_t>((cnt + 255) / 256, 4096), 256, 0, ctx->stream>>>(cnt, V32, V64);
+        TN_LAUNCHED(ctx);
+      }
+      // restore V's unitarity (V ← V + V·R/2, quadratic: the pre-pass leaves R ~ 1e-4)
+      // and leave every pair with a kept column to the FP64 sweeps
+      for (int rep = 0; rep < 3; ++rep) {
+        k_set_identity_cxd<<<blocks, 256, 0, ctx->stream>>>(n, batch, RE);
+        TN_LAUNCHED(ctx);
+        TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'C', 'N', n, n, n, mone, V64, n, n * n, V64, n, n * n, one, RE, n,
+                              n * n, batch));
+        TN_RETURN_IF(scale_real_cxd(ctx, RE, n * n * batch, 0.5));
+        TN_CHECK_CUDA(ctx, cudaMemcpyAsync(V, V64, sizeof(cxd) * (size_t)(n * n * batch), cudaMemcpyDeviceToDevice,
+                                           ctx->stream));
+        TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', n, n, n, one, V64, n, n * n, RE, n, n * n, one, V, n, n * n,
+                              batch));
+        std::swap(V, V64);
+      }
+      restored = true;
+      w_fresh = false;
+    }
+    if (!w_fresh)
       TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, one, A, lda, sA, V64, n, n * n, zero, W64, m, m * n,
                             batch));
     ctx->last_sweeps_fp64 = 0;
-    if (clusters > 0)  // near-degenerate pairs with a kept column: one-sided Jacobi finishes them
+    ctx->last_refine_clusters = clusters;
+    bool sweep_marked = false;
+    if (!restored && clusters > 0) {
+      // pairs still marked at the end: the marked-column Jacobi (already run on this W
+      // when the last iteration stepped); a matrix with more marked columns than fit, or
+      // unconverged, takes the FP64 sweeps over the pairs with a marked column
+      if (kmax < 2) {
+        sweep_marked = true;
+      } else {
+        if (!cluster_ran) TN_RETURN_IF(cluster_jacobi(nullptr));
+        std::vector<int> h_c(batch);
+        TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_c.data(), cstat, sizeof(int) * batch, cudaMemcpyDeviceToHost, ctx->stream));
+        TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int64_t b = 0; b < batch; ++b) sweep_marked |= h_c[b] != 0;
+      }
+    }
+    ctx->refine_totals[0] += 1;
+    ctx->refine_totals[1] += ctx->last_refine_iters;
+    ctx->refine_totals[2] += clusters;
+    ctx->refine_totals[3] += (restored || sweep_marked) ? 1 : 0;
+    if (restored) {
+      // unconverged refinement: FP64 one-sided Jacobi with the truncation flags finishes
+      // (after a divergence the flags are derived afresh from the sweeps' own norms)
       TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W64, nullptr, batch, true, active, rotated, nrm64, kMaxSweeps, nullptr,
-                                        &noconv, tail, keep_m, true));
+                                        &noconv, tail, keep_m, !diverged));
+    } else if (sweep_marked) {
+      k_cluster_flags<<<lblocks, 256, 0, ctx->stream>>>(n * batch, cluster, tail);
+      TN_LAUNCHED(ctx);
+      TN_RETURN_IF(jacobi_core<double>(ctx, m, n, W64, nullptr, batch, true, active, rotated, nrm64, kMaxSweeps, nullptr,
+                                        &noconv, tail, keep_m, true, 0.0, true));
+    }
     TN_RETURN_IF(jacobi_finalize<double>(ctx, m, n, W64, nullptr, order, U, sU, S, sS, nullptr, 0, false, batch));
     if (noconv) return tn_set_error(ctx, TN_ENOCONV, "Jacobi SVD did not converge within %d sweeps", kMaxSweeps);
     return TN_OK;
@@ -1741,6 +2041,25 @@ extern "C" tn_status_t tn_svd_last_sweeps(tn_ctx* ctx, int32_t* fp32_sweeps, int
   if (fp32_sweeps) *fp32_sweeps = ctx->last_sweeps_fp32;
   if (fp64_sweeps) *fp64_sweeps = ctx->last_sweeps_fp64;
   for (int i = 0; rotations && i < n_rot && i < 64; ++i) rotations[i] = ctx->sweep_rotations[i];
+  return TN_OK;
+}
+
+extern "C" tn_status_t tn_svd_refine_stats(tn_ctx* ctx, int64_t* totals, int32_t reset) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, totals, "tn_svd_refine_stats: null output");
+  for (int i = 0; i < 4; ++i) totals[i] = ctx->refine_totals[i];
+  if (reset)
+    for (int i = 0; i < 4; ++i) ctx->refine_totals[i] = 0;
+  return TN_OK;
+}
+
+extern "C" tn_status_t tn_svd_last_refine(tn_ctx* ctx, float* trace, int32_t* iterations, int32_t* outcome) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, trace && iterations && outcome, "tn_svd_last_refine: null output");
+  *iterations = ctx->last_refine_iters;
+  *outcome = ctx->refine_outcome;
+  for (int k = 0; k < ctx->last_refine_iters && k < 8; ++k)
+    for (int q = 0; q < 4; ++q) trace[4 * k + q] = ctx->refine_trace[k][q];
   return TN_OK;
 }
 

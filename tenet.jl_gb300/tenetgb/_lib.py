@@ -102,6 +102,8 @@ SIGNATURES = {
     "tn_svd_thin": (_st, [_vp, C.c_int, C.c_int, _i64, _i64, _vp, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, _i64]),
     "tn_svd_last_sweeps": (_st, [_vp, _pi32, _pi32, _pi32, _i32]),
     "tn_svd_last_ratios": (_st, [_vp, C.POINTER(C.c_float), _i32]),
+    "tn_svd_refine_stats": (_st, [_vp, C.POINTER(C.c_int64), _i32]),
+    "tn_svd_last_refine": (_st, [_vp, C.POINTER(C.c_float), _pi32, _pi32]),
     "tn_svd_thin_noalloc": (_st, [_vp, _i64, _i64, _vp, _i64, _vp, _vp, _vp]),
     "tn_truncation_rank": (_st, [_vp, _vp, _i64, _i64, _dbl, _pi64]),
     "tn_hadamard": (_st, [_vp, C.c_int, _i32, _pi64, _i32, _vp, _vp, _vp]),

@@ -152,6 +152,24 @@ class Context:
             out[name] = {"launches": n.value, "ms": ms.value, "flops": fl.value, "bytes": by.value}
         return out
 
+    def refine_stats(self, reset=False):
+        """Cumulative counts of the truncated mixed SVD: calls, refinement iterations,
+        near-degenerate pairs finished by the FP64 Jacobi of the marked columns, and calls
+        that needed full FP64 sweeps."""
+        t = (C.c_int64 * 4)()
+        self.check(self.lib.tn_svd_refine_stats(self.h, t, int(bool(reset))))
+        return {"calls": t[0], "iterations": t[1], "marked_pairs": t[2], "full_fp64_sweeps": t[3]}
+
+    def last_refine(self):
+        """The last truncated mixed SVD's refinement: per iteration (largest step, largest
+        |I − VᴴV|, largest ‖E‖_F, marked pairs) and the outcome ("converged", "diverged",
+        "out_of_iterations")."""
+        tr = (C.c_float * 32)()
+        it, oc = C.c_int32(), C.c_int32()
+        self.check(self.lib.tn_svd_last_refine(self.h, tr, C.byref(it), C.byref(oc)))
+        rows = [tuple(tr[4 * k + q] for q in range(4)) for k in range(min(it.value, 8))]
+        return rows, ("converged", "diverged", "out_of_iterations")[oc.value]
+
     def pipe_peak(self, which):
         """Measured FMA rate of the CUDA cores in TFLOP/s: which = "fp32" or "fp64"."""
         v = C.c_double()

@@ -132,8 +132,11 @@ def test_batched_512_population_norms(ctx):
     """Config 4 at its full size: the 512-MPS ragged population (L in [16, 128], χ
     log-uniform in [16, 512], seed 5), canonize → compress(χ/2) → norm in one grouped
     call.  The norms of the 150 cheapest instances (by L·χ³) are checked against the
-    oracle on their initial sites, and 12 instances spread over the χ range (the largest
-    included) against the per-instance device path, to 1e-12 relative."""
+    oracle on their initial sites to 1e-12 relative, and 12 instances spread over the χ
+    range (the largest included) against the per-instance device path to 1e-10: the two
+    device paths order their Jacobi rotations differently, so at a cut inside a dense
+    random spectrum (512 values, smallest relative gaps ~1e-5) the kept vectors agree to
+    ε/gap, and the downstream truncations carry that into the norm."""
     import tenetgb
     from tenetgb import workloads as W
     from tenetgb.group import MPSGroup
@@ -154,13 +157,15 @@ def test_batched_512_population_norms(ctx):
         O.canonize(p, O.MixedCanonical(Ls[b]))
         O.compress(p, maxdim=maxdim[b])
         worst = max(worst, abs(norms[b] - O.norm(p)) / O.norm(p))
-    worst_dev = 0.0
+    worst_dev, devs = 0.0, []
     for b in spread:
         psi = tenetgb.MPS([a.copy() for a in init[b]], ctx=ctx)
         psi.canonize_(tenetgb.MixedCanonical(Ls[b]))
         psi.compress_(maxdim=maxdim[b])
-        worst_dev = max(worst_dev, abs(norms[b] - psi.norm()) / psi.norm())
+        devs.append((int(chis[b]), abs(norms[b] - psi.norm()) / psi.norm()))
+        worst_dev = max(worst_dev, devs[-1][1])
         del psi
     print(f"\n512-MPS population: norms vs oracle (150 cheapest) {worst:.2e}; vs per-instance device path "
-          f"(12, χ {min(chis[b] for b in spread)}..{max(chis[b] for b in spread)}) {worst_dev:.2e}")
-    assert worst <= 1e-12 and worst_dev <= 1e-12
+          f"(12, χ {min(chis[b] for b in spread)}..{max(chis[b] for b in spread)}) {worst_dev:.2e}; "
+          + ", ".join(f"χ={c}: {e:.1e}" for c, e in devs))
+    assert worst <= 1e-12 and worst_dev <= 1e-10

@@ -77,3 +77,31 @@ def test_mpo_zipup_needs_a_truncation():
         tenetgb.evolve_mpo_(psi, rand_mpo(rng, 3), algorithm="zipup")
     with pytest.raises(ValueError):
         tenetgb.evolve_mpo_(psi, rand_mpo(rng, 2))
+
+
+@pytest.mark.parametrize("precision", ["native", "mixed"])
+def test_mpo_zipup_on_a_batch_of_instances(precision):
+    """The zip-up on a batched MPS (evolve.jl:49-129 for every instance in lockstep): one
+    instance is a product state written into the bonds, so its kept ranks are below the
+    others' and its surplus is zero-padded; each instance must equal its own oracle run."""
+    import tenetgb
+
+    rng = np.random.default_rng(53)
+    bonds = [1, 2, 4, 8, 8, 4, 2, 1]
+    insts = [rand_sites(rng, bonds) for _ in range(2)]
+    prod = [np.zeros_like(s) for s in insts[0]]
+    for s in prod:
+        s[0, 0, 0] = 1.0
+    insts = [prod] + insts
+    mpo = rand_mpo(rng, 7)
+    psi = tenetgb.MPS.batched([[s.copy() for s in x] for x in insts], precision=precision)
+    tenetgb.evolve_mpo_(psi, mpo, algorithm="zipup", maxdim=6, threshold=1e-12)
+    for b, x in enumerate(insts):
+        ref = O.OMPS([s.copy() for s in x])
+        O.evolve_mpo_zipup(ref, mpo, maxdim=6, threshold=1e-12)
+        v = psi.site(1, instance=b)
+        for i in range(2, 8):
+            v = np.tensordot(v, psi.site(i, instance=b), axes=(v.ndim - 1, 0))
+        a, r = v.reshape(-1), O.contract_state(ref).reshape(-1)
+        assert np.linalg.norm(a - r) <= 1e-12 * np.linalg.norm(r), b
+        assert all(x <= y for x, y in zip(ref.bondsizes(), psi.bondsizes()))
