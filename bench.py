@@ -138,7 +138,7 @@ def replica_throughput(ws, instances, steps, seconds):
 def layers_for(n):
     from tenetgb import workloads as W
 
-    return W.tebd_layers(L_SITES, n)
+    return W.tebd_layers(L_SITES, n, serpentine=True)
 
 
 def flush_l2(torch, buf):
@@ -190,7 +190,7 @@ _PIPE = {"jacobi_fp32": ("fp32_tflops", "fp32_cuda_cores"), "jacobi_fp64": ("fp6
          "gemm_fp64": ("fp64_tflops", "fp64_cuda_cores"), "gemm_split_bf16": ("bf16_tflops", "tensor"),
          "split_prep": (None, "hbm"), "qr": ("fp64_tflops", "fp64_cuda_cores"),
          "jacobi_coop": ("fp64_tflops", "fp64_cuda_cores")}
-_KERNEL = {"jacobi_fp32": "k_jacobi_step_reg<float>", "jacobi_fp64": "k_jacobi_step_reg<double>",
+_KERNEL = {"jacobi_fp32": "k_jacobi_block_f32 (FP32 block rounds)", "jacobi_fp64": "k_jacobi_step_reg<double>",
            "gemm_fp64": "k_gemm_cx<double>", "gemm_split_bf16": "k_gemm_oz (tcgen05 kind::f16)",
            "split_prep": "k_oz_scales + k_oz_split", "qr": "k_qr_panel + k_apply_block_reflector",
            "jacobi_coop": "k_jacobi_coop<double>"}
@@ -433,10 +433,10 @@ def cpu_sample(host_state, layer):
     applied to the same input state."""
     from oracle import tenet_oracle as O
 
-    start, gates = layer
+    gates = layer[1]
     psi = O.OMPS([np.ascontiguousarray(s) for s in host_state])
     t0 = time.perf_counter()
-    O.tebd(psi, [(start, gates)], maxdim=CHI_MAX, threshold=CUTOFF)
+    O.tebd(psi, [layer], maxdim=CHI_MAX, threshold=CUTOFF)
     dt = time.perf_counter() - t0
     return {"value": 1.0 / dt, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
             "sample": f"all {len(gates)} gates of one saturated layer (same input MPS), numpy/LAPACK, "
@@ -583,6 +583,34 @@ def profile_gate(args):
             torch.cuda.profiler.stop()
     print(json.dumps({"profile_gate_ms": 1e3 * dt, "precision": args.precision, "batch": args.batch,
                       "bond": psi.bondsizes()[9], "launches": ctx.launches()}))
+
+
+def profile_layer(args):
+    """One brickwork layer (odd bonds, 10 gates) on B saturated random MPS of 20 sites,
+    χ = 256 (θ 512×512 per gate): the small case for the launch list of the headline step.
+    The first layer builds the cached graphs; the second is bracketed by
+    cudaProfilerStart/Stop."""
+    import torch
+
+    import tenetgb
+    from tenetgb import workloads as W
+
+    ctx = tenetgb.Context(0)
+    insts = [W.random_mps_arrays(20, 2, CHI_MAX, seed=7 + b) for b in range(args.batch)]
+    layers = W.tebd_layers(20, 3)
+    psi = tenetgb.MPS.batched(insts, ctx=ctx, max_bond=CHI_MAX, precision=args.precision)
+    for rep, ly in enumerate([layers[0], layers[2]]):
+        ctx.sync()
+        if rep == 1:
+            torch.cuda.profiler.start()
+        t0 = time.perf_counter()
+        psi.evolve_brickwork_([ly], maxdim=CHI_MAX, threshold=CUTOFF)
+        ctx.sync()
+        dt = time.perf_counter() - t0
+        if rep == 1:
+            torch.cuda.profiler.stop()
+    print(json.dumps({"profile_layer_ms": 1e3 * dt, "precision": args.precision, "batch": args.batch,
+                      "gates": len(layers[2][1]), "launches": ctx.launches()}))
 
 
 def profile_svd(args):
@@ -1125,6 +1153,7 @@ def main():
     ap.add_argument("--serve-precision", default="native", choices=["native", "mixed"], help="serving arithmetic")
     ap.add_argument("--profile-gate", action="store_true", help="one saturated gate (small ncu case)")
     ap.add_argument("--profile-svd", action="store_true", help="the roofline kernel's SVD (small ncu case)")
+    ap.add_argument("--profile-layer", action="store_true", help="one brickwork layer, 20 sites (launch list)")
     ap.add_argument("--profile-dmrg", action="store_true", help="one saturated 2-site DMRG sweep (launch list)")
     ap.add_argument("--precision", default="native", choices=["native", "mixed"])
     ap.add_argument("--batch", type=int, default=16, help="MPS instances advanced in lockstep")
@@ -1140,6 +1169,8 @@ def main():
         profile_gate(args)
     elif args.profile_svd:
         profile_svd(args)
+    elif args.profile_layer:
+        profile_layer(args)
     elif args.profile_dmrg:
         profile_dmrg(args)
     elif args.workload == "lattice":

@@ -328,6 +328,15 @@ tn_status_t tn_mps_simple_update(tn_mps* mps, int32_t n_sites, int32_t a, const 
 tn_status_t tn_mps_evolve_brickwork(tn_mps* mps, int32_t n_layers, const int32_t* starts,
                                     const int32_t* n_gates, const void* h_gates,
                                     int64_t maxdim, double threshold);
+/* as tn_mps_evolve_brickwork, with a direction per layer: reverse[l] != 0 applies layer
+ * l's gates right→left (its gates are still stored left→right in h_gates).  A sweep
+ * that alternates direction (serpentine) starts each layer where the orthogonality
+ * centre was left, instead of moving it back across the chain; reverse == NULL is
+ * left→right everywhere.  Every gate is Tenet's simple_update! (canonize! to the pair,
+ * contract, SVD, truncate) on the state as left by the previous gate. */
+tn_status_t tn_mps_evolve_layers(tn_mps* mps, int32_t n_layers, const int32_t* starts,
+                                 const int32_t* n_gates, const int32_t* reverse,
+                                 const void* h_gates, int64_t maxdim, double threshold);
 /* ⟨b|a⟩ = Σ a·conj(b); h_out = (re, im) per instance */
 tn_status_t tn_mps_overlap(const tn_mps* a, const tn_mps* b, double* h_out);
 tn_status_t tn_mps_norm(tn_mps* mps, double* h_out);

@@ -668,12 +668,17 @@ def contract_state(psi: OMPS):
 
 
 def tebd(psi: OMPS, layers, maxdim, threshold, spectra=None, driver="gesdd"):
-    """Apply brickwork layers [(bond_start, [G...]), ...] left→right.  ``spectra`` (a
-    list) receives every gate's full θ spectrum, in order."""
-    for start, gates in layers:
-        for j, G in enumerate(gates):
+    """Apply brickwork layers: (bond_start, [G...]) left→right, or (bond_start, [G...],
+    reverse) right→left when reverse is true (gates listed left to right either way) —
+    one simple_update! per gate, in that order.  ``spectra`` (a list) receives every
+    gate's full θ spectrum, in order."""
+    for ly in layers:
+        start, gates = ly[0], ly[1]
+        order = range(len(gates) - 1, -1, -1) if (len(ly) > 2 and ly[2]) else range(len(gates))
+        for j in order:
             a = start + 2 * j
-            simple_update(psi, G, (a, a + 1), maxdim=maxdim, threshold=threshold, spectra=spectra, driver=driver)
+            simple_update(psi, gates[j], (a, a + 1), maxdim=maxdim, threshold=threshold, spectra=spectra,
+                          driver=driver)
     return psi
 
 

@@ -13,7 +13,7 @@ typedef tn_status_t (*su_out_fn)(void* arg, int64_t r, cxd** Aout, int64_t* sAou
 tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, int64_t d1, int64_t chm, int64_t d2,
                                int64_t chr, const cxd* A, int64_t sA, const cxd* Bm, int64_t sB, const cxd* dG,
                                int64_t maxdim, double threshold, int64_t batch, su_out_fn out_fn, void* out_arg,
-                               double* Sout, int64_t* rank_out, bool absorb_right = false);
+                               double* Sout, int64_t* rank_out, int absorb = kAbsorbEqually);
 
 namespace {
 

@@ -25,8 +25,8 @@
 // of K = 2k products of magnitude ≤ 2^{2b-2}, so its sum is an integer ≤ S·K·2^{2b-2};
 // b is the widest digit with S·K·2^{2b-2} ≤ 2^24, which keeps the FP32 accumulation
 // exact, and contractions too long for b = 7 are split on the host into chunks that
-// accumulate into C.  The epilogue combines the levels in FP64 (Horner in 2^-b) and
-// applies σ_i τ_j 2^{4-2b}:
+// accumulate into C.  The epilogue combines the levels exactly in int64 (the FP64 pipe
+// is the scarce one on this part) and applies σ_i τ_j 2^{4-2b} in FP64:
 //     c_ij = σ_i τ_j 2^{4-2b} Σ_L 2^{-bL} acc_L.
 // The only approximation is the dropped pairs (p + q ≥ S) and the digit remainders, of
 // relative size ~S·2^{1-bS} per product: S = 8, b = 7 gives ~52 bits, FP64-grade products.
@@ -37,7 +37,7 @@
 // of the A tile through a 4-slot ring.  Warp 5 lane 0 issues tcgen05.mma (M=128, N=64,
 // K=16): for plane p of A it multiplies every resident B plane q < S − p into level
 // p + q (TMEM columns 64·(p+q)…).  Warps 0-3 then read the S level accumulators with
-// tcgen05.ld (warp w owns rows 32w…32w+31), combine them in FP64, exchange Re/Im with
+// tcgen05.ld (warp w owns rows 32w…32w+31), combine them in int64, exchange Re/Im with
 // the neighbouring lane and write interleaved complex C.  Every mbarrier wait is
 // bounded: on timeout the kernel records an error word, skips the remaining work and
 // still releases its TMEM.
@@ -232,31 +232,46 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
       const int row = m0 + warp * 32 + lane;  // real row of the 4M product: 2i + (0 Re | 1 Im)
       const int i = row >> 1;
       const bool re_lane = (lane & 1) == 0;
-      const double si = (row < M2) ? ldexp(sig[(int64_t)bidx * m_complex + i], 4 - 2 * bits) : 0.0;
-      const double hb = ldexp(1.0, -bits);
+      // The levels are recombined exactly in int64 on the integer pipe (GB300's FP64 pipe
+      // is ~1/70 of its FP32 pipe, and an FP64 Horner step per level and output kept it
+      // busier than the tensor pipe): H = Σ_L acc_L · 2^{b(S−1−L)−D}, each acc_L an
+      // integer of magnitude ≤ 2^24 (exact in FP32), D = max(0, b(S−1) − 37) so that
+      // |H| < 2^62; the levels below 2^D are rounded to nearest (an error of at most
+      // S/2 units of 2^{D−b(S−1)} relative to acc_0, below 2^-60 of the largest term).
+      // One conversion to FP64 per output, then the scales σ_i τ_j 2^{4−2b+D−b(S−1)}.
+      const int D = bits * (S - 1) > 37 ? bits * (S - 1) - 37 : 0;
+      const double si =
+          (row < M2) ? ldexp(sig[(int64_t)bidx * m_complex + i], 4 - 2 * bits + D - bits * (S - 1)) : 0.0;
+      const bool alpha_one = alpha.x == 1.0 && alpha.y == 0.0;
       cxd* Cb = C + (int64_t)bidx * sC;
 #pragma unroll 1
       for (int cb = 0; cb < OZ_BN; cb += 16) {
-        double h[16];
+        long long h[16];
         float v[16];
-        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)((S - 1) * OZ_BN + cb), v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) h[j] = (double)v[j];
-        for (int L = S - 2; L >= 0; --L) {
+        for (int j = 0; j < 16; ++j) h[j] = 0;
+        for (int L = 0; L < S; ++L) {
           tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(L * OZ_BN + cb), v);
+          const int sh = bits * (S - 1 - L) - D;
+          if (sh >= 0) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) h[j] = fma(h[j], hb, (double)v[j]);
+            for (int j = 0; j < 16; ++j) h[j] += (long long)__float2int_rn(v[j]) * (1ll << sh);
+          } else {
+            const long long half = 1ll << (-sh - 1);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) h[j] += ((long long)__float2int_rn(v[j]) + half) >> (-sh);
+          }
         }
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int col = n0 + cb + j;
-          const double x = h[j];
+          const double x = (double)h[j];
           const double y = __shfl_xor_sync(0xffffffffu, x, 1);
           if (row < M2 && col < N && re_lane) {
             const double s = si * tau[(int64_t)bidx * N + col];
             const cxd c = mkcx(s * x, s * y);
             cxd* dst = Cb + i + (int64_t)col * ldc;
-            cxd out = alpha * c;
+            cxd out = alpha_one ? c : alpha * c;
             if (!beta_zero) out = out + beta * *dst;
             *dst = out;
           }

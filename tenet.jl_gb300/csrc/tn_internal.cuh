@@ -415,6 +415,14 @@ tn_status_t scale_rows_invsqrt(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, 
 // X_b(r, c) *= S_b[r] (mode 1), or zeroed where S_b[r] == 0 (mode 0)
 tn_status_t scale_rows_mode(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int64_t ld, const double* S, int64_t sX,
                             int64_t sS, int64_t batch, int mode);
+// how a two-site update splits S between the two sites (simple_update_core)
+constexpr int kAbsorbEqually = 0, kAbsorbRight = 1, kAbsorbLeft = 2;
+// X_b(r, c) *= S_b[c] (mode 1), or zeroed where S_b[c] == 0 (mode 0)
+tn_status_t scale_cols_mode(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int64_t ld, const double* S, int64_t sX,
+                            int64_t sS, int64_t batch, int mode);
+// dst_b (cols × rows) = src_b (rows × cols)ᴴ
+tn_status_t adjoint_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src, int64_t lds, int64_t sSrc, cxd* dst,
+                        int64_t ldd, int64_t sDst, int64_t batch);
 tn_status_t norm2_cxd(tn_ctx* ctx, int64_t n, const cxd* x, double* h_out);
 tn_status_t copy_matrix_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src,
                             int64_t lds, cxd* dst, int64_t ldd, int64_t sSrc = 0,

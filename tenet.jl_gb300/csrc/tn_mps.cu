@@ -281,20 +281,33 @@ tn_status_t mps_ensure_site(tn_mps* p, int i, size_t elems) { return ensure_site
 // simple update core (Muscle.simple_update with AbsorbEqually), batched
 // A (chl·d1 × chm), B (chm × d2·chr), G (d1 d2 × d1 d2) column-major, instance strides
 // sA, sB; G shared by all instances.  Reserves the workspace itself.
-// absorb_right: A' = U, B' = S·Vh (the same two-site state, all of S on the right), so
-// that A' is already left-isometric when the centre moves on to the right.
+// absorb (the same two-site state in every case, A'B' = the truncated θ):
+//   kAbsorbEqually  A' = U√S, B' = √S Vh (Tenet's AbsorbEqually)
+//   kAbsorbRight    A' = U, B' = S·Vh: A' is already left-isometric when the centre moves
+//                   on to the right
+//   kAbsorbLeft     A' = U·S, B' = Vh: B' is already right-isometric when the centre
+//                   moves on to the left.  With n ≥ m the SVD runs on θᴴ, whose left
+//                   vectors are V: B' = V[:, :r]ᴴ exactly isometric and A' = θ·V[:, :r]
+//                   (no division by S).
 // ---------------------------------------------------------------------------------
 tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, int64_t d1, int64_t chm, int64_t d2,
                                int64_t chr, const cxd* A, int64_t sA, const cxd* Bm, int64_t sB, const cxd* dG,
                                int64_t maxdim, double threshold, int64_t batch, su_out_fn out_fn, void* out_arg,
-                               double* Sout, int64_t* rank_out, bool absorb_right = false) {
+                               double* Sout, int64_t* rank_out, int absorb) {
   const int64_t m = chl * d1, n = d2 * chr, k = std::min(m, n), dd = d1 * d2;
-  // m ≥ n (the saturated TEBD case, θ square): U and S only, then
-  //   B' = √S Vh = diag(1/√s) Uᴴ θ  (one GEMM; A'B' keeps its ε‖θ‖ accuracy)
-  const bool left_only = m >= n;
+  // U-only SVDs (one factor from the Jacobi sweeps, the other by one GEMM):
+  //   m ≥ n (the saturated TEBD case, θ square), not absorbing left: U and S of θ, then
+  //     B' = √S Vh = diag(1/√s) Uᴴ θ (or S·Vh = Uᴴθ)
+  //   n ≥ m, absorbing left: V and S from θᴴ, then A' = θ·V
+  //   otherwise (absorbing left with m > n, or n > m not absorbing left) the full SVD
+  const bool left_of_adj = absorb == kAbsorbLeft && n >= m;
+  const bool left_only = absorb != kAbsorbLeft && m >= n;
+  const size_t svd_ws = left_of_adj ? svd_left_workspace(prec, n, m, batch)
+                                    : (left_only ? svd_left_workspace(prec, m, n, batch)
+                                                 : svd_any_workspace(TN_C64, prec, m, n, batch));
   size_t need = 2 * ws_round(sizeof(cxd) * (size_t)(batch * m * n)) + ws_round(sizeof(cxd) * (size_t)(batch * m * k)) +
                 ws_round(sizeof(double) * (size_t)(batch * k)) + ws_round(sizeof(cxd) * (size_t)(batch * k * n)) +
-                (left_only ? svd_left_workspace(prec, m, n, batch) : svd_any_workspace(TN_C64, prec, m, n, batch));
+                svd_ws;
   TN_RETURN_IF(ws_reserve(ctx, need));
   cxd* th0 = ws_take<cxd>(ctx, (size_t)(batch * m * n));
   cxd* th = ws_take<cxd>(ctx, (size_t)(batch * m * n));
@@ -307,37 +320,55 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
   // which are contiguous blocks of chl·dd elements
   TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, dd, dd, kOne, th0, chl, chl * dd, dG, dd, 0, kZero, th, chl,
                                chl * dd, chr * batch));
-  if (left_only)  // at most maxdim values survive the truncation below
+  if (left_of_adj) {
+    // θᴴ (n × m) in θ0's buffer; its left vectors V (n × k) go to the Vh buffer
+    TN_RETURN_IF(adjoint_cxd(ctx, m, n, th, m, m * n, th0, n, n * m, batch));
+    TN_RETURN_IF(svd_left(ctx, prec, n, m, th0, n, n * m, Vh, n * k, S, k, batch, maxdim > 0 && maxdim < m ? maxdim : 0));
+  } else if (left_only) {  // at most maxdim values survive the truncation below
     TN_RETURN_IF(svd_left(ctx, prec, m, n, th, m, m * n, U, m * k, S, k, batch, maxdim > 0 && maxdim < n ? maxdim : 0));
-  else
+  } else {
     TN_RETURN_IF(svd_any(ctx, TN_C64, prec, m, n, th, m, m * n, U, m * k, S, k, Vh, k * n, batch));
+  }
   int64_t r = 0;
   TN_RETURN_IF(rank_select_batched(ctx, S, k, k, batch, maxdim, threshold, &r, nullptr));
   if (prec != TN_PREC_NATIVE) TN_RETURN_IF(split_gemm_check(ctx));  // the stream has drained: one word
   cxd *Aout = nullptr, *Bout = nullptr;
   int64_t sAo = 0, sBo = 0;
   TN_RETURN_IF(out_fn(out_arg, r, &Aout, &sAo, &Bout, &sBo));
-  // A' = U[:, :r] √S  (or U[:, :r])
-  TN_RETURN_IF(copy_matrix_cxd(ctx, m * r, 1, U, m * r, Aout, m * r, m * k, sAo, batch));
-  if (absorb_right) {
-    if (left_only) {
-      // B' = S Vh = U[:, :r]ᴴ θ, rows beyond an instance's own rank (S = 0) zeroed
-      TN_RETURN_IF(gemm_c64(ctx, prec, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
-      TN_RETURN_IF(scale_rows_mode(ctx, Bout, r, n, r, S, sBo, k, batch, 0));
-    } else {
-      TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
-      TN_RETURN_IF(scale_rows_mode(ctx, Bout, r, n, r, S, sBo, k, batch, 1));
-    }
-  } else if (left_only) {
-    TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
-    // B' = diag(1/√s) U[:, :r]ᴴ θ
-    TN_RETURN_IF(gemm_c64(ctx, prec, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
-    TN_RETURN_IF(scale_rows_invsqrt(ctx, Bout, r, n, r, S, sBo, k, batch));
+  if (left_of_adj) {
+    // B' = V[:, :r]ᴴ; A' = θ V[:, :r], columns beyond an instance's own rank (S = 0) zeroed
+    TN_RETURN_IF(adjoint_cxd(ctx, n, r, Vh, n, n * k, Bout, r, sBo, batch));
+    TN_RETURN_IF(gemm_c64(ctx, prec, 'N', 'N', m, r, n, kOne, th, m, m * n, Vh, n, n * k, kZero, Aout, m, sAo, batch));
+    TN_RETURN_IF(scale_cols_mode(ctx, Aout, m, r, m, S, sAo, k, batch, 0));
   } else {
-    TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
-    // B' = √S Vh[:r, :]
-    TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
-    TN_RETURN_IF(scale_rows_sqrt<double>(ctx, Bout, r, n, r, S, sBo, k, batch));
+    // A' = U[:, :r] (· √S or · S below)
+    TN_RETURN_IF(copy_matrix_cxd(ctx, m * r, 1, U, m * r, Aout, m * r, m * k, sAo, batch));
+    if (absorb == kAbsorbLeft) {
+      // (m > n) B' = Vh[:r, :], A' = U S
+      TN_RETURN_IF(scale_cols_mode(ctx, Aout, m, r, m, S, sAo, k, batch, 1));
+      TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
+    } else if (absorb == kAbsorbRight) {
+      if (left_only) {
+        // B' = S Vh = U[:, :r]ᴴ θ, rows beyond an instance's own rank (S = 0) zeroed
+        TN_RETURN_IF(
+            gemm_c64(ctx, prec, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
+        TN_RETURN_IF(scale_rows_mode(ctx, Bout, r, n, r, S, sBo, k, batch, 0));
+      } else {
+        TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
+        TN_RETURN_IF(scale_rows_mode(ctx, Bout, r, n, r, S, sBo, k, batch, 1));
+      }
+    } else if (left_only) {
+      TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
+      // B' = diag(1/√s) U[:, :r]ᴴ θ
+      TN_RETURN_IF(
+          gemm_c64(ctx, prec, 'C', 'N', r, n, m, kOne, U, m, m * k, th, m, m * n, kZero, Bout, r, sBo, batch));
+      TN_RETURN_IF(scale_rows_invsqrt(ctx, Bout, r, n, r, S, sBo, k, batch));
+    } else {
+      TN_RETURN_IF(scale_cols_sqrt<double>(ctx, Aout, m, r, m, S, sAo, k, batch));
+      // B' = √S Vh[:r, :]
+      TN_RETURN_IF(copy_matrix_cxd(ctx, r, n, Vh, k, Bout, r, k * n, sBo, batch));
+      TN_RETURN_IF(scale_rows_sqrt<double>(ctx, Bout, r, n, r, S, sBo, k, batch));
+    }
   }
   if (Sout)
     TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(Sout, sizeof(double) * r, S, sizeof(double) * k, sizeof(double) * r, batch,
@@ -365,20 +396,22 @@ tn_status_t pair_out(void* arg, int64_t r, cxd** Aout, int64_t* sAo, cxd** Bout,
   return TN_OK;
 }
 
-// absorb_right: site a keeps U (left-isometric) and site a+1 all of S, so the form
-// becomes MixedCanonical(a+1) — the same state as AbsorbEqually's MixedCanonical([a, a+1]),
-// with the first of the next centre move's two QR factorisations already done
-tn_status_t apply_gate2(tn_mps* p, int a, const cxd* dG, int64_t maxdim, double threshold, bool absorb_right = false) {
+// kAbsorbRight: site a keeps U (left-isometric) and site a+1 all of S, so the form becomes
+// MixedCanonical(a+1) — the same state as AbsorbEqually's MixedCanonical([a, a+1]), with
+// the first of the next centre move's two QR factorisations already done; kAbsorbLeft
+// mirrors it (site a+1 = Vh, MixedCanonical(a)) for a centre moving on to the left
+tn_status_t apply_gate2(tn_mps* p, int a, const cxd* dG, int64_t maxdim, double threshold,
+                        int absorb = kAbsorbEqually) {
   const int64_t d = p->d;
   PairOut e{p, a};
   int64_t r = 0;
   TN_RETURN_IF(simple_update_core(p->ctx, p->prec, p->bond[a - 1], d, p->bond[a], d, p->bond[a + 1], p->site[a],
                                   p->cap[a], p->site[a + 1], p->cap[a + 1], dG, maxdim, threshold, p->B, pair_out, &e,
-                                  nullptr, &r, absorb_right));
+                                  nullptr, &r, absorb));
   p->bond[a] = r;
-  if (absorb_right) {
+  if (absorb != kAbsorbEqually) {
     p->kind = TN_FORM_MIXED;
-    p->lo = p->hi = a + 1;
+    p->lo = p->hi = absorb == kAbsorbRight ? a + 1 : a;
   }
   return TN_OK;
 }
@@ -761,6 +794,11 @@ tn_status_t tn_mps_simple_update(tn_mps* p, int32_t n_sites, int32_t a, const vo
 
 tn_status_t tn_mps_evolve_brickwork(tn_mps* p, int32_t n_layers, const int32_t* starts, const int32_t* n_gates,
                                     const void* h_gates, int64_t maxdim, double threshold) {
+  return tn_mps_evolve_layers(p, n_layers, starts, n_gates, nullptr, h_gates, maxdim, threshold);
+}
+
+tn_status_t tn_mps_evolve_layers(tn_mps* p, int32_t n_layers, const int32_t* starts, const int32_t* n_gates,
+                                 const int32_t* reverse, const void* h_gates, int64_t maxdim, double threshold) {
   if (!p) return TN_EINVAL;
   tn_ctx* ctx = p->ctx;
   TN_ARG(ctx, n_layers >= 0 && starts && n_gates && h_gates, "evolve: bad arguments");
@@ -775,17 +813,20 @@ tn_status_t tn_mps_evolve_brickwork(tn_mps* p, int32_t n_layers, const int32_t* 
   TN_RETURN_IF(upload_gates(p, h_gates, total));
   size_t off = 0;
   for (int l = 0; l < n_layers; ++l) {
-    for (int g = 0; g < n_gates[l]; ++g) {
-      int a = starts[l] + 2 * g;
-      // within a layer the next gate is further right: S goes to the right-hand site, whose
-      // QR the centre move needs anyway, and the left-hand site is left as U.  The last
-      // gate of a layer keeps Tenet's AbsorbEqually, so every layer (and the call) ends in
-      // the reference's form (MixedCanonical([a, a+1])) and split.
-      const bool right = g + 1 < n_gates[l];
+    const bool rev = reverse && reverse[l];
+    for (int q = 0; q < n_gates[l]; ++q) {
+      // gates are stored left to right; a reversed layer applies them right to left
+      const int g = rev ? n_gates[l] - 1 - q : q;
+      const int a = starts[l] + 2 * g;
+      // within a layer the next gate lies further along the sweep: S goes to the site on
+      // that side, whose QR (LQ) the centre move needs anyway, and the other site is left
+      // isometric.  The last gate of a layer keeps Tenet's AbsorbEqually, so every layer
+      // (and the call) ends in the reference's form (MixedCanonical([a, a+1])) and split.
+      const int absorb = q + 1 < n_gates[l] ? (rev ? kAbsorbLeft : kAbsorbRight) : kAbsorbEqually;
       TN_RETURN_IF(canonize_mixed(p, a, a + 1));
-      TN_RETURN_IF(apply_gate2(p, a, p->gates + off, maxdim, threshold, right));
-      off += g4;
+      TN_RETURN_IF(apply_gate2(p, a, p->gates + (size_t)g * g4 + off, maxdim, threshold, absorb));
     }
+    off += (size_t)n_gates[l] * g4;
   }
   return TN_OK;
 }

@@ -1,5 +1,7 @@
 // K5 — small fused ops: Hadamard (Λ absorption), √S absorption into U / Vh, the
 // truncation-rank decision on the singular-value spectrum, FP64 norms.
+#include <algorithm>
+
 #include "tn_internal.cuh"
 
 namespace {
@@ -266,6 +268,64 @@ tn_status_t scale_rows_mode(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int
   if (rows * cols * batch == 0) return TN_OK;
   dim3 g(blocks_for(ctx, rows * cols), (unsigned)(batch < 65535 ? batch : 65535));
   k_scale_rows_mode<<<g, 256, 0, ctx->stream>>>(X, rows, cols, ld, sX, S, sS, batch, mode);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+// X_b(r, c) *= S_b[c] (mode 1), or zeroed where S_b[c] == 0 (mode 0)
+__global__ void k_scale_cols_mode(cxd* X, int64_t rows, int64_t cols, int64_t ld, int64_t sX, const double* S,
+                                  int64_t sS, int64_t batch, int mode) {
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < rows * cols; t += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t r = t % rows, c = t / rows;
+      const double s = S[b * sS + c];
+      const double f = mode == 1 ? s : (s > 0.0 ? 1.0 : 0.0);
+      X[b * sX + r + c * ld] = f * X[b * sX + r + c * ld];
+    }
+}
+
+tn_status_t scale_cols_mode(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int64_t ld, const double* S, int64_t sX,
+                            int64_t sS, int64_t batch, int mode) {
+  if (rows * cols * batch == 0) return TN_OK;
+  dim3 g(blocks_for(ctx, rows * cols), (unsigned)(batch < 65535 ? batch : 65535));
+  k_scale_cols_mode<<<g, 256, 0, ctx->stream>>>(X, rows, cols, ld, sX, S, sS, batch, mode);
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
+// dst_b (cols × rows, ld ldd) = src_b (rows × cols, ld lds)ᴴ through 32×32 shared-memory
+// tiles (both sides coalesced); grid (tiles, batch)
+__global__ void __launch_bounds__(256) k_adjoint_cxd(int64_t rows, int64_t cols, const cxd* __restrict__ src,
+                                                     int64_t lds, int64_t sSrc, cxd* __restrict__ dst, int64_t ldd,
+                                                     int64_t sDst, int64_t batch) {
+  __shared__ cxd tile[32][33];
+  const int64_t tr = (rows + 31) / 32, tcn = (cols + 31) / 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 × 8
+  for (int64_t b = blockIdx.y; b < batch; b += gridDim.y)
+    for (int64_t t = blockIdx.x; t < tr * tcn; t += gridDim.x) {
+      const int64_t r0 = (t % tr) * 32, c0 = (t / tr) * 32;
+      for (int q = ty; q < 32; q += 8) {
+        const int64_t r = r0 + tx, c = c0 + q;
+        if (r < rows && c < cols) tile[q][tx] = src[b * sSrc + r + c * lds];
+      }
+      __syncthreads();
+      for (int q = ty; q < 32; q += 8) {
+        const int64_t c = c0 + tx, r = r0 + q;  // dst(c, r) = conj(src(r, c))
+        if (r < rows && c < cols) {
+          const cxd v = tile[tx][q];
+          dst[b * sDst + c + r * ldd] = mkcx(v.x, -v.y);
+        }
+      }
+      __syncthreads();
+    }
+}
+
+tn_status_t adjoint_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src, int64_t lds, int64_t sSrc, cxd* dst,
+                        int64_t ldd, int64_t sDst, int64_t batch) {
+  if (rows * cols * batch == 0) return TN_OK;
+  const int64_t tiles = ((rows + 31) / 32) * ((cols + 31) / 32);
+  dim3 g((unsigned)std::min<int64_t>(tiles, 4096), (unsigned)(batch < 65535 ? batch : 65535));
+  k_adjoint_cxd<<<g, 256, 0, ctx->stream>>>(rows, cols, src, lds, sSrc, dst, ldd, sDst, batch);
   TN_LAUNCHED(ctx);
   return TN_OK;
 }

@@ -392,6 +392,180 @@ __global__ void __launch_bounds__(NT)
                                           tol, tail);
 }
 
+// ---------------------------------------------------------------------------------
+// Block round of the FP32 pre-pass (m, n ≤ NT): the n columns form blocks of 8; the blocks
+// play a round-robin tournament (NB − 1 outer rounds per sweep, one launch each), and the
+// CTA of block pair (P, Q) of matrix b holds the 16 columns of W and V in registers — one
+// row per thread — while it visits the 64 cross pairs (P_i, Q_k) in 8 inner rounds of 8
+// disjoint pairs; in outer round 0 every block first visits its own 28 pairs (7 inner
+// rounds over P and Q together).  Every column pair is visited once per sweep, as in the
+// column-pair rounds, but W and V cross L2 once per outer round instead of once per pair
+// round (63 instead of 511 passes at n = 512).  Per inner round the 8 pairs' α, β, γ
+// (32 values) are reduced by a transposing butterfly (31 shuffles: lane l ends with the
+// warp sum of value l), then across warps in shared memory; lanes 4k of warp 0 form the
+// rotation of pair k exactly as make_rot_c does (with the truncation-aware tail rule of
+// jacobi_pair), and every thread applies the 8 rotations to its row of W and V.
+// Counters as k_jacobi_step_reg: rotations at cnt[b], the largest ratio at cnt[nmat + b].
+// ---------------------------------------------------------------------------------
+template <int H>
+__device__ __forceinline__ void transpose_stage(float* v, int lane) {
+  const bool up = (lane & H) != 0;
+#pragma unroll
+  for (int k = 0; k < H; ++k) {
+    const float send = up ? v[k] : v[k + H];
+    const float keep = up ? v[k + H] : v[k];
+    v[k] = keep + __shfl_xor_sync(0xffffffffu, send, H);
+  }
+}
+
+// Inner-round schedules with fixed register slots (so one round body serves every round
+// and the kernel stays small enough for the instruction cache): the data move instead.
+// Intra rounds pair slots (s, 7 − s), s < 4, inside each block (polygon method) and then
+// rotate slots 0..6 by one, so after r rotations slot s holds original column (s + r) mod 7
+// (slot 7 stays); cross rounds pair P slot k with Q slot k and then rotate the Q slots, so
+// Q slot k holds original column (k + r) mod 8.  Seven (eight) rotations restore the order.
+template <int OFF, int LEN>
+__device__ __forceinline__ void rotate_slots(cxf* a) {
+  const cxf t = a[OFF];
+#pragma unroll
+  for (int q = 0; q < LEN - 1; ++q) a[OFF + q] = a[OFF + q + 1];
+  a[OFF + LEN - 1] = t;
+}
+__host__ __device__ constexpr int blk_slot_i(bool intra, int k) { return intra ? (k & 3) + (k >= 4 ? 8 : 0) : k; }
+__host__ __device__ constexpr int blk_slot_j(bool intra, int k) { return intra ? 7 - (k & 3) + (k >= 4 ? 8 : 0) : 8 + k; }
+// the original column (0..15 within the block pair) in a slot at inner round r
+__host__ __device__ constexpr int blk_slot_orig(bool intra, int r, int slot) {
+  return intra ? ((slot & 7) < 7 ? ((slot & 7) + r) % 7 : 7) + (slot & 8) : (slot < 8 ? slot : 8 + ((slot - 8) + r) % 8);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NT, 512 / NT)
+    k_jacobi_block_f32(int64_t m, int64_t n, int NB, int R, cxf* __restrict__ W, cxf* __restrict__ V,
+                       const float* __restrict__ nrm, const int* __restrict__ active, int* __restrict__ cnt, float tol,
+                       const unsigned char* __restrict__ tail) {
+  constexpr int NC = 16, NW = NT / 32;
+  const int64_t b = blockIdx.y, nmat = gridDim.y;
+  if (!active[b]) return;
+  int P, Q;
+  rr_pair(NB, R, blockIdx.x, P, Q);
+  __shared__ int s_col[NC];
+  __shared__ unsigned char s_tail[NC];
+  __shared__ float red[2][NW][32];
+  __shared__ int s_cnt, s_ratio;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  if (t < NC) {
+    const int64_t c = t < 8 ? (int64_t)P * 8 + t : (int64_t)Q * 8 + (t - 8);
+    s_col[t] = c < n ? (int)c : -1;
+    s_tail[t] = (tail && c < n) ? tail[b * n + c] : 0;
+  }
+  if (t == 0) {
+    s_cnt = 0;
+    s_ratio = 0;
+  }
+  __syncthreads();
+  cxf* Wb = W + b * m * n;
+  cxf* Vb = V + b * n * n;
+  cxf w[NC], v[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int col = s_col[c];
+    w[c] = (col >= 0 && t < m) ? Wb[(int64_t)col * m + t] : mkcx<float>(0.f, 0.f);
+    v[c] = (col >= 0 && t < n) ? Vb[(int64_t)col * n + t] : mkcx<float>(0.f, 0.f);
+  }
+  const float negl = jacobi_eps<float>() * jacobi_eps<float>() * nrm[n * nmat + b];
+
+  // one inner round over 8 disjoint pairs (column slots i_k, j_k, compile-time after
+  // unrolling).  One barrier per round: every warp sums the per-warp partials itself (in
+  // the same order, so all warps form bit-identical rotations) from a double-buffered
+  // table, and lanes 4k hand pair k's rotation to the other lanes by shuffles.
+  int rb = 0;
+  auto round = [&](const bool intra, const int r) {
+    float val[32];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const cxf x = w[blk_slot_i(intra, k)], y = w[blk_slot_j(intra, k)];
+      val[4 * k + 0] = x.x * x.x + x.y * x.y;
+      val[4 * k + 1] = y.x * y.x + y.y * y.y;
+      val[4 * k + 2] = x.x * y.x + x.y * y.y;
+      val[4 * k + 3] = x.x * y.y - x.y * y.x;
+    }
+    transpose_stage<16>(val, lane);
+    transpose_stage<8>(val, lane);
+    transpose_stage<4>(val, lane);
+    transpose_stage<2>(val, lane);
+    transpose_stage<1>(val, lane);
+    red[rb][warp][lane] = val[0];
+    __syncthreads();
+    float tot = 0.f;
+#pragma unroll
+    for (int q = 0; q < NW; ++q) tot += red[rb][q][lane];
+    rb ^= 1;
+    const int base = lane & ~3;
+    const float al = __shfl_sync(0xffffffffu, tot, base);
+    const float be = __shfl_sync(0xffffffffu, tot, base + 1);
+    const cxf g = mkcx<float>(__shfl_sync(0xffffffffu, tot, base + 2), __shfl_sync(0xffffffffu, tot, base + 3));
+    float rc = 1.f, rsx = 0.f, rsy = 0.f;
+    int app = 0;
+    if ((lane & 3) == 0) {
+      const int k = lane >> 2;  // lane-dependent: the original columns at run time
+      const int i = blk_slot_orig(intra, r, blk_slot_i(intra, k)), j = blk_slot_orig(intra, r, blk_slot_j(intra, k));
+      if (s_col[i] >= 0 && s_col[j] >= 0 && !(s_tail[i] && s_tail[j])) {
+        RotC<float> Rt = make_rot_c(al, be, g, tol, negl);
+        float monitor = Rt.ratio;
+        if (s_tail[i] != s_tail[j] && al > 0.f && be > 0.f) {
+          const float ak = s_tail[i] ? be : al, at = s_tail[i] ? al : be;
+          monitor = Rt.ratio * (at / ak);
+          if (!(monitor > tol)) Rt.apply = 0;
+        }
+        app = Rt.apply;
+        rc = Rt.c;
+        rsx = Rt.se.x;
+        rsy = Rt.se.y;
+        if (warp == 0) {
+          if (al > 0.f && be > 0.f) atomicMax(&s_ratio, __float_as_int(monitor));
+          if (app) atomicAdd(&s_cnt, 1);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (__shfl_sync(0xffffffffu, app, 4 * k)) {
+        const float c = __shfl_sync(0xffffffffu, rc, 4 * k);
+        const cxf se = mkcx<float>(__shfl_sync(0xffffffffu, rsx, 4 * k), __shfl_sync(0xffffffffu, rsy, 4 * k));
+        rot_apply_c(c, se, w[blk_slot_i(intra, k)], w[blk_slot_j(intra, k)]);
+        rot_apply_c(c, se, v[blk_slot_i(intra, k)], v[blk_slot_j(intra, k)]);
+      }
+    }
+  };
+  if (R == 0) {
+#pragma unroll 1
+    for (int r = 0; r < 7; ++r) {
+      round(true, r);
+      rotate_slots<0, 7>(w);
+      rotate_slots<8, 7>(w);
+      rotate_slots<0, 7>(v);
+      rotate_slots<8, 7>(v);
+    }
+  }
+#pragma unroll 1
+  for (int r = 0; r < 8; ++r) {
+    round(false, r);
+    rotate_slots<8, 8>(w);
+    rotate_slots<8, 8>(v);
+  }
+  __syncthreads();  // warp 0's counter updates are complete before thread 0 reads them
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int col = s_col[c];
+    if (col >= 0 && t < m) Wb[(int64_t)col * m + t] = w[c];
+    if (col >= 0 && t < n) Vb[(int64_t)col * n + t] = v[c];
+  }
+  if (t == 0) {
+    if (s_cnt) atomicAdd(&cnt[b], s_cnt);
+    if (s_ratio) atomicMax(&cnt[nmat + b], s_ratio);
+  }
+}
+
 // Persistent one-sided Jacobi for small matrices, where a round is far too little work to
 // hide a launch: one cooperative launch runs every sweep of every matrix.  Rounds are
 // separated by grid-wide barriers (all CTAs co-resident by construction of the cooperative
@@ -1038,6 +1212,10 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
     std::vector<int> h_act(batch, 1), h_rot(2 * batch);
     TN_CHECK_CUDA(ctx, cudaMemcpyAsync(active, h_act.data(), sizeof(int) * batch, cudaMemcpyHostToDevice, ctx->stream));
     const int N = (int)(n + (n & 1));
+    // FP32 with V and m, n ≤ 512: block rounds (16 columns per CTA in registers)
+    const bool blocked = sizeof(T) == 4 && V && m <= 512 && n <= 512 && n >= 32;
+    const int NB0 = (int)((n + 7) / 8), NB = NB0 + (NB0 & 1);
+    const int rounds = blocked ? NB - 1 : N - 1;
     // A sweep whose largest off-diagonal ratio is ρ leaves ~ρ² for the next one
     // (one-sided Jacobi converges quadratically); when ρ² is below tol/10 the next
     // sweep would rotate nothing and is skipped.
@@ -1062,7 +1240,21 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       k_col_norms<T><<<(unsigned)std::max<int64_t>(nb, 1), 256, 0, ctx->stream>>>(m, n, W, m * n, nrm, batch);
       k_fro<T><<<(unsigned)std::min<int64_t>(batch, 65535), 256, 0, ctx->stream>>>(n, nrm, batch);
       tn_status_t st = TN_OK;
-      for (int r = 0; r < N - 1 && st == TN_OK; ++r)
+      if constexpr (sizeof(T) == 4) {
+        if (blocked) {
+          const dim3 grid((unsigned)(NB / 2), gy);
+          for (int r = 0; r < NB - 1; ++r) {
+            if (m <= 128 && n <= 128)
+              k_jacobi_block_f32<128><<<grid, 128, 0, ctx->stream>>>(m, n, NB, r, W, V, nrm, active, rotated, tol, tail);
+            else if (m <= 256 && n <= 256)
+              k_jacobi_block_f32<256><<<grid, 256, 0, ctx->stream>>>(m, n, NB, r, W, V, nrm, active, rotated, tol, tail);
+            else
+              k_jacobi_block_f32<512><<<grid, 512, 0, ctx->stream>>>(m, n, NB, r, W, V, nrm, active, rotated, tol, tail);
+            TN_LAUNCHED(ctx);
+          }
+        }
+      }
+      for (int r = 0; !blocked && r < N - 1 && st == TN_OK; ++r)
         st = launch_step<T>(ctx, m, n, N, r, W, V, nrm, active, rotated, tol, gy, tail);
       cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
       if (st != TN_OK) {
@@ -1074,7 +1266,7 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       cudaGraphDestroy(g);
       if (e != cudaSuccess) return tn_set_error(ctx, TN_ECUDA, "svd graph instantiate: %s", cudaGetErrorString(e));
       ctx->graphs[key] = ge;
-      ctx->launches -= (N - 1);  // counted again per replay below
+      ctx->launches -= rounds;  // counted again per replay below
     }
     if (tail && !tail_preset) TN_CHECK_CUDA(ctx, cudaMemsetAsync(tail, 0, (size_t)(n * batch), ctx->stream));
     const int64_t pairs = n * (n - 1) / 2;
@@ -1086,12 +1278,13 @@ static tn_status_t jacobi_core(tn_ctx* ctx, int64_t m, int64_t n, cx<T>* W, cx<T
       if (slot >= 0) {
         // per round, every pair of every active matrix: wᵢᴴwⱼ (8m) + the two rotated
         // columns of W (24m) [+ of V (24n)]; W [and V] read and written once
-        const double rounds = (double)(N - 1), act = (double)n_active;
-        const double flops = rounds * act * (N / 2) * (32.0 * m + (V ? 24.0 * n : 0.0));
-        const double bytes = rounds * act * 2.0 * sizeof(cx<T>) * ((double)m * n + (V ? (double)n * n : 0.0));
-        prof_end(ctx, slot, sizeof(T) == 4 ? TN_PROF_JACOBI_F32 : TN_PROF_JACOBI_F64, N - 1, flops, bytes);
+        // (block rounds: W and V cross memory once per outer round, NB − 1 per sweep)
+        const double pair_rounds = (double)(N - 1), act = (double)n_active;
+        const double flops = pair_rounds * act * (N / 2) * (32.0 * m + (V ? 24.0 * n : 0.0));
+        const double bytes = (double)rounds * act * 2.0 * sizeof(cx<T>) * ((double)m * n + (V ? (double)n * n : 0.0));
+        prof_end(ctx, slot, sizeof(T) == 4 ? TN_PROF_JACOBI_F32 : TN_PROF_JACOBI_F64, rounds, flops, bytes);
       }
-      ctx->launches += N + 1;  // norm refresh, ‖A‖_F, N-1 steps
+      ctx->launches += rounds + 2;  // norm refresh, ‖A‖_F, the rounds
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_rot.data(), rotated, sizeof(int) * 2 * batch, cudaMemcpyDeviceToHost,
                                          ctx->stream));
       TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

@@ -134,6 +134,7 @@ SIGNATURES = {
     "tn_mps_compress": (_st, [_vp, _i32, _i64, _dbl]),
     "tn_mps_simple_update": (_st, [_vp, _i32, _i32, _vp, _i64, _dbl]),
     "tn_mps_evolve_brickwork": (_st, [_vp, _i32, _pi32, _pi32, _vp, _i64, _dbl]),
+    "tn_mps_evolve_layers": (_st, [_vp, _i32, _pi32, _pi32, _pi32, _vp, _i64, _dbl]),
     "tn_mps_overlap": (_st, [_vp, _vp, _pdbl]),
     "tn_mps_norm": (_st, [_vp, _pdbl]),
     "tn_mps_normalize": (_st, [_vp]),

@@ -320,14 +320,20 @@ class MPS:
         return self.simple_update_(op, sites)
 
     def evolve_brickwork_(self, layers, maxdim=None, threshold=None):
-        """Apply brickwork layers [(start_bond, [G, …]), …] in one library call."""
-        starts = (C.c_int32 * len(layers))(*[int(s) for s, _ in layers])
-        counts = (C.c_int32 * len(layers))(*[len(g) for _, g in layers])
-        flat = [np.asfortranarray(np.asarray(G, dtype=np.complex128)).reshape(-1, order="F") for _, gs in layers for G in gs]
+        """Apply brickwork layers in one library call.  A layer is (start_bond, [G, …]) —
+        gates on bonds start, start+2, … applied left to right — or (start_bond, [G, …],
+        reverse) with reverse true for right to left (the gates still listed left to
+        right)."""
+        starts = (C.c_int32 * len(layers))(*[int(ly[0]) for ly in layers])
+        counts = (C.c_int32 * len(layers))(*[len(ly[1]) for ly in layers])
+        rev = (C.c_int32 * len(layers))(*[int(bool(ly[2])) if len(ly) > 2 else 0 for ly in layers])
+        flat = [np.asfortranarray(np.asarray(G, dtype=np.complex128)).reshape(-1, order="F") for ly in layers
+                for G in ly[1]]
         buf = np.ascontiguousarray(np.concatenate(flat)) if flat else np.zeros(1, np.complex128)
-        self._chk(self.lib.tn_mps_evolve_brickwork(self.h, len(layers), starts, counts, buf.ctypes.data_as(C.c_void_p),
-                                                   -1 if maxdim is None else int(maxdim),
-                                                   -1.0 if threshold is None else float(threshold)))
+        self._chk(self.lib.tn_mps_evolve_layers(self.h, len(layers), starts, counts, rev,
+                                                buf.ctypes.data_as(C.c_void_p),
+                                                -1 if maxdim is None else int(maxdim),
+                                                -1.0 if threshold is None else float(threshold)))
         return self
 
     def norm(self):

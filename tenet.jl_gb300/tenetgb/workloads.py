@@ -63,16 +63,19 @@ def gate_tensor(u4):
     return np.ascontiguousarray(u4.reshape(2, 2, 2, 2))
 
 
-def tebd_layers(L, n_layers, seed_base=3):
+def tebd_layers(L, n_layers, seed_base=3, serpentine=False):
     """Brickwork layers: odd layers (1-based) act on bonds (1,2),(3,4),…; even layers
-    on (2,3),(4,5),….  Layer ℓ (0-based) draws its gates from seed seed_base+ℓ."""
+    on (2,3),(4,5),….  Layer ℓ (0-based) draws its gates from seed seed_base+ℓ.  With
+    ``serpentine`` the even layers are applied right to left (layer tuples carry the
+    direction), so each layer starts where the previous one left the orthogonality
+    centre."""
     layers = []
     for ell in range(n_layers):
         rng = np.random.default_rng(seed_base + ell)
         start = 1 if ell % 2 == 0 else 2
         n_g = (L - start + 1) // 2
         gates = [gate_tensor(haar_unitary(rng, 4)) for _ in range(n_g)]
-        layers.append((start, gates))
+        layers.append((start, gates, serpentine and ell % 2 == 1))
     return layers
 
 
@@ -85,8 +88,10 @@ PLAIN_SMALL = dict(L=32, d=2, chi=64, seed=1, z_site=16)
 
 
 def tebd_workload(L=TEBD["L"], chi0=TEBD["chi0"], n_layers=TEBD["layers"], seed=TEBD["seed"]):
+    """The TEBD workload: the seeded initial MPS and its brickwork layers, odd layers
+    swept left to right and even layers right to left (serpentine)."""
     sites = random_mps_arrays(L, 2, chi0, seed)
-    return sites, tebd_layers(L, n_layers)
+    return sites, tebd_layers(L, n_layers, serpentine=True)
 
 
 def plain_small_workload(L=32, chi=64, seed=1):

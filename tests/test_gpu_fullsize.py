@@ -91,7 +91,7 @@ def test_saturated_gate_matches_oracle(ctx, tebd_run, precision):
     g = tenetgb.MPS(sat, ctx=ctx, max_bond=CHI)
     g.canonize_([32, 33])
     A, B = g.site(32), g.site(33)
-    start, gates = layers[5]
+    start, gates = layers[5][0], layers[5][1]
     G = gates[(32 - start) // 2]
     An_o, Bn_o, s_kept, s_full = O.simple_update_tensors(A, B, G, CHI, CUT)
     gap = O.truncation_gap(s_full, CHI, CUT)

@@ -186,12 +186,16 @@ def test_overlap_norm_amplitude_expectations(ctx):
     assert abs(psi.norm() - 1) <= 1e-13
 
 
+@pytest.mark.parametrize("serpentine", [True, False])
 @pytest.mark.parametrize("precision", ["native", "mixed"])
-def test_tebd_small_matches_oracle(ctx, precision):
-    """Brickwork TEBD with truncation (L=16, χ 4 → 16): overlaps and ⟨Z_i⟩ vs the oracle."""
+def test_tebd_small_matches_oracle(ctx, precision, serpentine):
+    """Brickwork TEBD with truncation (L=16, χ 4 → 16): overlaps and ⟨Z_i⟩ vs the oracle,
+    with every layer swept left to right, and with the even layers swept right to left
+    (the gates before the last of such a layer put S on their left site)."""
     from tenetgb import workloads as W
 
-    sites, layers = W.tebd_workload(L=16, chi0=4, n_layers=6)
+    sites = W.random_mps_arrays(16, 2, 4, seed=2)
+    layers = W.tebd_layers(16, 6, serpentine=serpentine)
     psi = gpu_mps(ctx, sites=sites, max_bond=16, precision=precision)
     psi.evolve_brickwork_(layers, maxdim=16, threshold=1e-12)
     p = O.OMPS([s.copy() for s in sites])
@@ -247,13 +251,16 @@ def test_batched_tebd_matches_oracle_per_instance(ctx, precision):
     ov = psi.overlap(psi)
     z = psi.local_expectations(W.pauli_z())
     nrm = psi.norm()
+    # ⟨Z_i⟩: 1e-11 in FP64; the mixed form is held to the 1e-10 of its accuracy target
+    # (the product instance's spectra end in exact zeros right at the cutoff)
+    z_tol = 1e-11 if precision == "native" else 1e-10
     for b, sites in enumerate(insts):
         p = O.OMPS([s.copy() for s in sites])
         O.tebd(p, layers, maxdim=32, threshold=1e-12)
         ov_o = O.overlap(p, p)
         assert abs(ov[b] - ov_o) <= 1e-12 * abs(ov_o), b
         z_o, _ = O.local_expectations(p, W.pauli_z())
-        assert np.abs(z[b] - z_o).max() <= 1e-11, b
+        assert np.abs(z[b] - z_o).max() <= z_tol, b
         assert abs(nrm[b] ** 2 - ov_o.real) <= 1e-12 * ov_o.real
     # the product instance's true ranks are below the common (padded) bond dimension
     p0 = O.OMPS([s.copy() for s in insts[0]])

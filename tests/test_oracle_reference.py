@@ -213,7 +213,8 @@ def test_tebd_small_unitary_invariants():
     v0 = O.contract_state(O.OMPS(sites))
     # apply the same gates to the dense vector
     v = v0.reshape([2] * 12)
-    for start, gates in layers:
+    for ly in layers:  # the gates of a layer commute: their order is immaterial here
+        start, gates = ly[0], ly[1]
         for j, G in enumerate(gates):
             a = start + 2 * j - 1
             v = np.moveaxis(np.tensordot(G, v, axes=([2, 3], [a, a + 1])), [0, 1], [a, a + 1])
