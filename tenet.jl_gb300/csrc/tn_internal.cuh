@@ -420,6 +420,8 @@ constexpr int kAbsorbEqually = 0, kAbsorbRight = 1, kAbsorbLeft = 2;
 // X_b(r, c) *= S_b[c] (mode 1), or zeroed where S_b[c] == 0 (mode 0)
 tn_status_t scale_cols_mode(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int64_t ld, const double* S, int64_t sX,
                             int64_t sS, int64_t batch, int mode);
+// out[l, p, blk] = Σ_q G[p, q] in[l, q, blk] over nblk contiguous rows × D blocks (in ≠ out)
+tn_status_t apply_phys(tn_ctx* ctx, int64_t rows, int64_t D, int64_t nblk, const cxd* in, cxd* out, const cxd* G);
 // dst_b (cols × rows) = src_b (rows × cols)ᴴ
 tn_status_t adjoint_cxd(tn_ctx* ctx, int64_t rows, int64_t cols, const cxd* src, int64_t lds, int64_t sSrc, cxd* dst,
                         int64_t ldd, int64_t sDst, int64_t batch);

@@ -318,8 +318,7 @@ tn_status_t simple_update_core(tn_ctx* ctx, tn_precision_t prec, int64_t chl, in
   TN_RETURN_IF(gemm_c64(ctx, prec, 'N', 'N', m, n, chm, kOne, A, m, sA, Bm, chm, sB, kZero, th0, m, m * n, batch));
   // θ[l, (a b), r] = Σ G[(a b), (a' b')] θ0[l, (a' b'), r] — batched over (r, instance),
   // which are contiguous blocks of chl·dd elements
-  TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, dd, dd, kOne, th0, chl, chl * dd, dG, dd, 0, kZero, th, chl,
-                               chl * dd, chr * batch));
+  TN_RETURN_IF(apply_phys(ctx, chl, dd, chr * batch, th0, th, dG));
   if (left_of_adj) {
     // θᴴ (n × m) in θ0's buffer; its left vectors V (n × k) go to the Vh buffer
     TN_RETURN_IF(adjoint_cxd(ctx, m, n, th, m, m * n, th0, n, n * m, batch));
@@ -423,8 +422,7 @@ tn_status_t apply_gate1(tn_mps* p, int i, const cxd* dG) {
   cxd* tmp = ws_take<cxd>(ctx, (size_t)(p->B * e));
   // new[l, a, r] = Σ_b G[a, b] A[l, b, r]  (batched over r within each instance)
   for (int b = 0; b < p->B; ++b)
-    TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', chl, d, d, kOne, p->site[i] + b * p->cap[i], chl, chl * d, dG, d, 0,
-                                 kZero, tmp + b * e, chl, chl * d, chr));
+    TN_RETURN_IF(apply_phys(ctx, chl, d, chr, p->site[i] + b * p->cap[i], tmp + b * e, dG));
   return copy_instances(ctx, p->site[i], p->cap[i], tmp, e, e, p->B);
 }
 
@@ -939,9 +937,7 @@ tn_status_t tn_mps_local_expectations(const tn_mps* p, const void* h_op, double*
       int64_t sAin = p->cap[i];
       if (pass == 0) {
         // OA[l, a, r] = Σ_b O[a, b] A[l, b, r]
-        for (int b = 0; b < B; ++b)
-          TN_RETURN_IF(gemm_cx<double>(ctx, 'N', 'T', x, d, d, kOne, p->site[i] + b * p->cap[i], x, x * d, dO, d, 0,
-                                       kZero, OA + b * t, x, x * d, x2));
+        for (int b = 0; b < B; ++b) TN_RETURN_IF(apply_phys(ctx, x, d, x2, p->site[i] + b * p->cap[i], OA + b * t, dO));
         Ain = OA;
         sAin = t;
       }

@@ -293,6 +293,51 @@ tn_status_t scale_cols_mode(tn_ctx* ctx, cxd* X, int64_t rows, int64_t cols, int
   return TN_OK;
 }
 
+// out[l, p, blk] = Σ_q G[p, q] · in[l, q, blk] for blocks of rows × D (column-major,
+// contiguous, D ≤ 16): one thread per (l, blk) holds the D inputs and writes the D
+// outputs; G (D × D, column-major) sits in shared memory.  Reads and writes each element
+// once, coalesced along l (a physical-index operator on an MPS site or a two-site θ).
+template <int D>
+__global__ void __launch_bounds__(256) k_apply_phys(int64_t rows, int64_t nblk, const cxd* __restrict__ in,
+                                                     cxd* __restrict__ out, const cxd* __restrict__ G) {
+  __shared__ cxd g[D * D];
+  for (int t = threadIdx.x; t < D * D; t += blockDim.x) g[t] = G[t];
+  __syncthreads();
+  const int64_t total = rows * nblk;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t l = t % rows, blk = t / rows;
+    const cxd* src = in + blk * rows * D + l;
+    cxd x[D];
+#pragma unroll
+    for (int q = 0; q < D; ++q) x[q] = src[q * rows];
+    cxd* dst = out + blk * rows * D + l;
+#pragma unroll
+    for (int p2 = 0; p2 < D; ++p2) {
+      cxd acc = mkcx(0.0, 0.0);
+#pragma unroll
+      for (int q = 0; q < D; ++q) cfma(acc, g[p2 + q * D], x[q]);
+      dst[p2 * rows] = acc;
+    }
+  }
+}
+
+tn_status_t apply_phys(tn_ctx* ctx, int64_t rows, int64_t D, int64_t nblk, const cxd* in, cxd* out, const cxd* G) {
+  if (rows * nblk == 0) return TN_OK;
+  const unsigned g = (unsigned)std::min<int64_t>((rows * nblk + 255) / 256, (int64_t)ctx->num_sms * 16);
+  switch (D) {
+    case 2: k_apply_phys<2><<<g, 256, 0, ctx->stream>>>(rows, nblk, in, out, G); break;
+    case 3: k_apply_phys<3><<<g, 256, 0, ctx->stream>>>(rows, nblk, in, out, G); break;
+    case 4: k_apply_phys<4><<<g, 256, 0, ctx->stream>>>(rows, nblk, in, out, G); break;
+    case 9: k_apply_phys<9><<<g, 256, 0, ctx->stream>>>(rows, nblk, in, out, G); break;
+    case 16: k_apply_phys<16><<<g, 256, 0, ctx->stream>>>(rows, nblk, in, out, G); break;
+    default:
+      return gemm_cx<double>(ctx, 'N', 'T', rows, D, D, mkcx(1.0, 0.0), in, rows, rows * D, G, D, 0, mkcx(0.0, 0.0), out,
+                             rows, rows * D, nblk);
+  }
+  TN_LAUNCHED(ctx);
+  return TN_OK;
+}
+
 // dst_b (cols × rows, ld ldd) = src_b (rows × cols, ld lds)ᴴ through 32×32 shared-memory
 // tiles (both sides coalesced); grid (tiles, batch)
 __global__ void __launch_bounds__(256) k_adjoint_cxd(int64_t rows, int64_t cols, const cxd* __restrict__ src,
