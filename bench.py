@@ -21,6 +21,7 @@ the same workload.  N>1 runs independent replicas, one per GPU (no collective).
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import subprocess
@@ -49,6 +50,7 @@ CONFIG = {
     "chi_max": CHI_MAX,
     "cutoff": CUTOFF,
     "gates_per_layer": "32 (odd) / 31 (even)",
+    "gate_order": "serpentine: odd layers left to right, even layers right to left",
     "saturation_layers_untimed": SAT_LAYERS,
     "step": "one brickwork layer on the saturated MPS",
     "seeds": {"mps": 2, "gates": "3+layer"},
@@ -419,7 +421,9 @@ def run_ours(args):
     }
     if rank == 0:
         if not args.quick:
+            print("bench: parity", file=sys.stderr, flush=True)
             out["parity_fp64_vs_oracle"] = parity_vs_oracle(ctx)
+        print("bench: cpu sample", file=sys.stderr, flush=True)
         out["cpu_baseline"] = cpu_sample(host_state, run_layers[0])
         if not args.quick:
             out["configs"] = other_configs(args, ctx, torch, stream, peaks)
@@ -540,6 +544,7 @@ def other_configs(args, ctx, torch, stream, peaks):
                      ("kernels", lambda: run_kernels(args, ctx, stream)),
                      ("batched_512", lambda: run_batched(args, ctx)),
                      ("serving", lambda: run_serving(args, rates=(1000, 5000)))]:
+        print(f"bench: {name}", file=sys.stderr, flush=True)
         t0 = time.perf_counter()
         try:
             r = fn()
@@ -1142,6 +1147,8 @@ def run_dmrg(args):
 
 
 def main():
+    # a fatal signal in native code prints the Python stacks of every thread
+    faulthandler.enable(file=sys.stderr, all_threads=True)
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="tebd", choices=["tebd", "lattice", "serving", "kernels", "batched", "dmrg", "plain"])
     ap.add_argument("--batched-sample", type=int, default=512, help="instances of the 512-MPS population (batched)")

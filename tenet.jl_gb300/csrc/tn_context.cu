@@ -60,13 +60,9 @@ tn_status_t ws_reserve(tn_ctx* ctx, size_t bytes) {
   if (bytes <= ctx->ws_cap) return TN_OK;
   // growth: the stream must be idle before the old arena is released
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  // (the cached graphs point into the arena; the profiler's events do not and stay)
   for (auto& kv : ctx->graphs) cudaGraphExecDestroy(kv.second);
   ctx->graphs.clear();
-  for (auto& r : ctx->prof_recs) {
-    cudaEventDestroy(r.a);
-    cudaEventDestroy(r.b);
-  }
-  for (cudaEvent_t e : ctx->prof_pool) cudaEventDestroy(e);
   if (ctx->ws) TN_RETURN_IF(tn_dev_free(ctx, ctx->ws));
   ctx->ws = nullptr;
   ctx->ws_cap = 0;

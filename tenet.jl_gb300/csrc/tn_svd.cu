@@ -1476,6 +1476,15 @@ __global__ void k_ortho_poly(int64_t n, int64_t batch, cxd* G, const cxf* E2, co
 constexpr double kRefineStepMax = 0.1;
 constexpr double kRefineGapMin = 1e-6;
 constexpr double kRefineNoise = 1e-14;
+// Digit planes of the refinement's products per iteration: an early step only has to
+// be accurate to well below the square of its own size (the next, quadratically
+// convergent step removes the rest), so the first iterations use fewer planes — 5 (~32
+// bits) for the first, 7 for the second, then the context's full setting; the stop test
+// is taken only at full precision.  The noise floor and the gap floor of the pair rule
+// follow the products' accuracy (~32·S·2^{1−7S} of the larger λ).
+inline int refine_slices(int it, int full) { return std::min(full, it == 0 ? 5 : (it == 1 ? 7 : 8)); }
+inline double refine_noise(int slices) { return std::max(kRefineNoise, 32.0 * slices * std::ldexp(1.0, 1 - 7 * slices)); }
+inline double refine_gapmin(double noise) { return std::max(kRefineGapMin, 1e4 * noise); }
 constexpr float kRefineStop = 1e-8f;
 constexpr double kRefineNormMax = 0.5;  // ‖E‖_F above which the first-order steps diverge
 constexpr int kRefineMaxIter = 6;
@@ -1515,7 +1524,7 @@ __device__ __forceinline__ bool refine_pair(int64_t n, int64_t b, int64_t i, int
 __global__ void __launch_bounds__(256)
     k_refine_step(int64_t n, const cxd* __restrict__ S, cxd* RE, const double* __restrict__ lam,
                   const unsigned char* __restrict__ tail, int* stat, double* __restrict__ esq,
-                  unsigned char* __restrict__ cluster) {
+                  unsigned char* __restrict__ cluster, double noise, double gapmin) {
   const int64_t b = blockIdx.y, nn = n * n;
   const cxd* Sb = S + b * nn;
   cxd* Rb = RE + b * nn;
@@ -1539,9 +1548,9 @@ __global__ void __launch_bounds__(256)
         // would keep a coupling of the size of λ·R_ij)
         const double nx = sij.x + li * r.x, ny = sij.y + li * r.y;
         const double mag = fmax(sqrt(num.x * num.x + num.y * num.y), sqrt(nx * nx + ny * ny));
-        if (mag <= kRefineNoise * big) {
-          // converged pair: orthogonality only
-        } else if (mag <= kRefineStepMax * fabs(den) && fabs(den) > kRefineGapMin * big) {
+        if (mag <= noise * big) {
+          // converged pair (at this iteration's product accuracy): orthogonality only
+        } else if (mag <= kRefineStepMax * fabs(den) && fabs(den) > gapmin * big) {
           e = mkcx(num.x / den, num.y / den);
           const double st = mag / fabs(den);
           emax = fmaxf(emax, (float)st);
@@ -1792,7 +1801,17 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
     int clusters = 0;
     float emax = 0.f, rmax = 0.f;
     ctx->last_refine_iters = 0;
+    const int full_slices = ctx->split_slices;
+    struct SlicesGuard {  // the context's setting comes back on every exit
+      tn_ctx* c;
+      int v;
+      ~SlicesGuard() { c->split_slices = v; }
+    } slices_guard{ctx, full_slices};
     for (int it = 0; it < kRefineMaxIter; ++it) {
+      const int slices = refine_slices(it, full_slices);
+      const bool full = slices == full_slices;
+      ctx->split_slices = slices;
+      const double noise = refine_noise(slices);
       TN_CHECK_CUDA(ctx, cudaMemsetAsync(cluster, 0, (size_t)(n * batch), ctx->stream));
       if (!w_fresh)
         TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, one, A, lda, sA, V64, n, n * n, zero, W64, m,
@@ -1815,7 +1834,8 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
       {
         const dim3 sg((unsigned)std::min<int64_t>((n * n + 255) / 256, std::max<int64_t>(1, 4096 / batch)),
                       (unsigned)batch);
-        k_refine_step<<<sg, 256, 0, ctx->stream>>>(n, G, RE, nrm64, tail, stat, esq, cluster);
+        k_refine_step<<<sg, 256, 0, ctx->stream>>>(n, G, RE, nrm64, tail, stat, esq, cluster, noise,
+                                                    refine_gapmin(noise));
         TN_LAUNCHED(ctx);
       }
       TN_CHECK_CUDA(ctx, cudaMemcpyAsync(h_stat.data(), stat, sizeof(int) * 4 * batch, cudaMemcpyDeviceToHost,
@@ -1850,7 +1870,7 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
         diverged = true;
         break;
       }
-      if (emax == 0.f && rmax <= 1e-15f && clusters == 0) {  // nothing to correct: W = A·V is final
+      if (full && emax == 0.f && rmax <= 1e-15f && clusters == 0) {  // nothing to correct: W = A·V is final
         converged = true;
         break;
       }
@@ -1870,11 +1890,12 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
       }
       // quadratic convergence: steps and non-orthogonality of at most kRefineStop leave
       // their squares (≤ 1e-16)
-      if (emax <= kRefineStop && rmax <= kRefineStop) {
+      if (full && emax <= kRefineStop && rmax <= kRefineStop) {
         converged = true;
         break;
       }
     }
+    ctx->split_slices = full_slices;
     ctx->refine_outcome = converged ? 0 : (diverged ? 1 : 2);
     bool restored = false;
     if (!converged) {
