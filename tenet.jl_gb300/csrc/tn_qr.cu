@@ -246,7 +246,9 @@ size_t qr_workspace(int64_t m, int64_t n, int64_t batch) {
   size_t tau = ws_round(sizeof(cx<T>) * (size_t)(k * batch + 1));
   // T factors: npan·nb² per matrix at the widest panel bounds every narrower choice
   size_t tm = ws_round(sizeof(cx<T>) * (size_t)((npan + 1) * nb * nb * batch + 1));
-  return w + tau + tm;
+  // the autotuner's private copy of A (Q may alias A)
+  size_t a0 = ws_round(sizeof(cx<T>) * (size_t)(m * n * batch));
+  return w + tau + tm + a0;
 }
 template size_t qr_workspace<double>(int64_t, int64_t, int64_t);
 template size_t qr_workspace<float>(int64_t, int64_t, int64_t);
@@ -341,6 +343,19 @@ tn_status_t qr_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda
     nb = std::min(it->second.first, nb_max);
     slab = it->second.second;
   } else if (ctx->autotune) {
+    // Every candidate factorises the same input, and Q may alias A (the in-place gauge
+    // move): the candidates and the final run read a private copy of A.
+    cx<T>* A0 = ws_take<cx<T>>(ctx, (size_t)(m * n * batch));
+    {
+      int64_t blocks = ((m * n) + 255) / 256;
+      if (blocks > 4096) blocks = 4096;
+      k_copy_in<T><<<dim3((unsigned)blocks, (unsigned)(batch < 65535 ? batch : 65535)), 256, 0, ctx->stream>>>(
+          m, n, A, lda, sA, A0, m * n, batch);
+      TN_LAUNCHED(ctx);
+    }
+    A = A0;
+    lda = m;
+    sA = m * n;
     float best = 1e30f;
     cudaEvent_t e0, e1;
     TN_CHECK_CUDA(ctx, cudaEventCreate(&e0));
