@@ -38,7 +38,10 @@ import numpy as np  # noqa: E402
 SAT_LAYERS = 5
 # DRAM bytes per launch of the step's dominant kernels from one ncu capture (dram__bytes_read.sum
 # + dram__bytes_write.sum, profiles/), by profiler class; None where not captured
-DOMINANT_TRAFFIC = {}
+# DRAM bytes per launch of the dominant kernels, from one ncu capture of the same shapes
+# (16 instances, θ 512×512): k_jacobi_block_f32 (an outer round, dram__bytes_read.sum +
+# dram__bytes_write.sum); the small-case capture has the headline step's shapes
+DOMINANT_TRAFFIC = {"jacobi_fp32": 67.17e6 + 6.68e6}
 L_SITES, CHI0, CHI_MAX, CUTOFF = 64, 16, 256, 1e-12
 METRIC = "tebd_gate_layers_per_s_chi256"
 UNIT = "layers/s"
