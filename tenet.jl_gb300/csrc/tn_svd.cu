@@ -1461,9 +1461,9 @@ __global__ void k_ortho_poly(int64_t n, int64_t batch, cxd* G, const cxf* E2, co
 // with relative accuracy.  Per pair (i, j), with num = S_ij + λ_j R_ij, den = λ_j − λ_i,
 // λ = max(λ_i, λ_j) and |num| the larger of |S_ij + λ_j R_ij| and |S_ij + λ_i R_ij| (the
 // same for both orders of the pair):
-//   * |num| ≤ kRefineNoise·λ: the pair is converged (its coupling is at the rounding level
-//     of the products); only the orthogonality part R_ij/2 is applied, so no rotation is
-//     driven by noise;
+//   * |num| ≤ kRefineNoise·λ and a relative gap below kRefineWideGap: the pair is converged
+//     (its coupling is at the rounding level of the products); only the orthogonality
+//     part R_ij/2 is applied, so no rotation is driven by noise;
 //   * |num| ≤ kRefineStepMax·|den| and |den| > kRefineGapMin·λ: the first-order step;
 //   * otherwise (a near-degenerate pair, or one the pre-pass left far from converged):
 //     R_ij/2 only, and both columns are marked for the FP64 one-sided Jacobi of the
@@ -1476,13 +1476,14 @@ __global__ void k_ortho_poly(int64_t n, int64_t batch, cxd* G, const cxf* E2, co
 constexpr double kRefineStepMax = 0.1;
 constexpr double kRefineGapMin = 1e-6;
 constexpr double kRefineNoise = 1e-14;
-// Digit planes of the refinement's products per iteration: an early step only has to
-// be accurate to well below the square of its own size (the next, quadratically
-// convergent step removes the rest), so the first iterations use fewer planes — 5 (~32
-// bits) for the first, 7 for the second, then the context's full setting; the stop test
-// is taken only at full precision.  The noise floor and the gap floor of the pair rule
+constexpr double kRefineWideGap = 1e-2;  // relative gap above which the noise floor does not apply
+// Digit planes of the refinement's products: the context's setting in every iteration.
+// (Fewer planes in the first iterations — 5, then 7 — saved ~8 % of the GEMM time but
+// left couplings of up to 1e-11 between neighbouring kept columns of U: a coupling the
+// reduced-precision steps left behind at the scale of their noise floor was classified
+// converged at full precision.)  The noise floor and the gap floor of the pair rule
 // follow the products' accuracy (~32·S·2^{1−7S} of the larger λ).
-inline int refine_slices(int it, int full) { return std::min(full, it == 0 ? 5 : (it == 1 ? 7 : 8)); }
+inline int refine_slices(int it, int full) { (void)it; return full; }
 inline double refine_noise(int slices) { return std::max(kRefineNoise, 32.0 * slices * std::ldexp(1.0, 1 - 7 * slices)); }
 inline double refine_gapmin(double noise) { return std::max(kRefineGapMin, 1e4 * noise); }
 constexpr float kRefineStop = 1e-8f;
@@ -1548,8 +1549,12 @@ __global__ void __launch_bounds__(256)
         // would keep a coupling of the size of λ·R_ij)
         const double nx = sij.x + li * r.x, ny = sij.y + li * r.y;
         const double mag = fmax(sqrt(num.x * num.x + num.y * num.y), sqrt(nx * nx + ny * ny));
-        if (mag <= noise * big) {
-          // converged pair (at this iteration's product accuracy): orthogonality only
+        if (mag <= noise * big && fabs(den) < kRefineWideGap * big) {
+          // converged near-degenerate pair (at this iteration's product accuracy): a step
+          // would be rounding over rounding, so orthogonality only.  A pair with a wide gap
+          // is stepped however small its coupling: the step's error is the coupling's
+          // (~ noise·big) over the gap, harmless, and skipping it would leave a relative
+          // coupling of noise·√(λ_big/λ_small) in U between well-separated values
         } else if (mag <= kRefineStepMax * fabs(den) && fabs(den) > gapmin * big) {
           e = mkcx(num.x / den, num.y / den);
           const double st = mag / fabs(den);
