@@ -201,6 +201,14 @@ _KERNEL = {"jacobi_fp32": "k_jacobi_block_f32 (FP32 block rounds)", "jacobi_fp64
            "jacobi_coop": "k_jacobi_coop<double>"}
 
 
+# what ncu shows bounds each class beyond the two roofs (profiles/ summaries)
+_LIMIT = {"jacobi_fp32": "instruction issue (ncu: 56-61 % of issue slots busy, one 512-thread CTA per SM); DRAM "
+                         "traffic is half the algorithmic bytes (the rest hits L2)",
+          "gemm_split_bf16": "N = 64 tiles (TMEM holds 8 levels x 64 columns): tensor subpipe 64 % busy yields 0.21 "
+                             "of peak; one CTA per SM, epilogue not overlapped",
+          "qr": "the FP64 pipe (one panel CTA per matrix between block-reflector updates)"}
+
+
 def kernel_rooflines(prof, peaks):
     """Per profiled class (event-timed inside the step): launches, ms, the algorithmic
     flops and bytes per launch, achieved rates and their fractions of the class's pipe
@@ -223,6 +231,8 @@ def kernel_rooflines(prof, peaks):
             e["pipe_peak_tflops"] = peaks[peak_key]
             e["frac_pipe"] = tfl / peaks[peak_key]
         e["bound"] = pipe if peak_key and e["frac_pipe"] >= e["frac_hbm"] else "hbm"
+        if name in _LIMIT:
+            e["limited_by"] = _LIMIT[name]
         out[name] = e
     return out
 
@@ -235,7 +245,7 @@ def roofline_entry(rooflines, peaks, traffic=None):
     else:
         achieved, peak, unit, frac = e["achieved_tflops"], e["pipe_peak_tflops"], "TFLOP/s", e["frac_pipe"]
     return {"bound": e["bound"], "kernel": e["kernel"], "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": frac, "traffic": traffic, "launch_avg_ms": e["launch_avg_ms"],
+            "frac": frac, "traffic": traffic, "limited_by": e.get("limited_by"), "launch_avg_ms": e["launch_avg_ms"],
             "flops_per_launch": e["flops_per_launch"], "bytes_per_launch": e["bytes_per_launch"],
             "share_of_step": e["share_of_profiled"],
             "timing": "CUDA events on the library stream around each launch / sweep graph inside one mixed B=16 layer",

@@ -1477,13 +1477,10 @@ constexpr double kRefineStepMax = 0.1;
 constexpr double kRefineGapMin = 1e-6;
 constexpr double kRefineNoise = 1e-14;
 constexpr double kRefineWideGap = 1e-2;  // relative gap above which the noise floor does not apply
-// Digit planes of the refinement's products: the context's setting in every iteration.
-// (Fewer planes in the first iterations — 5, then 7 — saved ~8 % of the GEMM time but
-// left couplings of up to 1e-11 between neighbouring kept columns of U: a coupling the
-// reduced-precision steps left behind at the scale of their noise floor was classified
-// converged at full precision.)  The noise floor and the gap floor of the pair rule
-// follow the products' accuracy (~32·S·2^{1−7S} of the larger λ).
-inline int refine_slices(int it, int full) { (void)it; return full; }
+// The refinement's products use the context's digit planes in every iteration (fewer
+// planes in the first iterations saved ~8 % of the GEMM time but left couplings of up to
+// 1e-11 between neighbouring kept columns of U).  The noise floor and the gap floor of the
+// pair rule follow the products' accuracy (~32·S·2^{1−7S} of the larger λ).
 inline double refine_noise(int slices) { return std::max(kRefineNoise, 32.0 * slices * std::ldexp(1.0, 1 - 7 * slices)); }
 inline double refine_gapmin(double noise) { return std::max(kRefineGapMin, 1e4 * noise); }
 constexpr float kRefineStop = 1e-8f;
@@ -1806,17 +1803,8 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
     int clusters = 0;
     float emax = 0.f, rmax = 0.f;
     ctx->last_refine_iters = 0;
-    const int full_slices = ctx->split_slices;
-    struct SlicesGuard {  // the context's setting comes back on every exit
-      tn_ctx* c;
-      int v;
-      ~SlicesGuard() { c->split_slices = v; }
-    } slices_guard{ctx, full_slices};
     for (int it = 0; it < kRefineMaxIter; ++it) {
-      const int slices = refine_slices(it, full_slices);
-      const bool full = slices == full_slices;
-      ctx->split_slices = slices;
-      const double noise = refine_noise(slices);
+      const double noise = refine_noise(ctx->split_slices);
       TN_CHECK_CUDA(ctx, cudaMemsetAsync(cluster, 0, (size_t)(n * batch), ctx->stream));
       if (!w_fresh)
         TN_RETURN_IF(gemm_c64(ctx, TN_PREC_MIXED, 'N', 'N', m, n, n, one, A, lda, sA, V64, n, n * n, zero, W64, m,
@@ -1875,7 +1863,7 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
         diverged = true;
         break;
       }
-      if (full && emax == 0.f && rmax <= 1e-15f && clusters == 0) {  // nothing to correct: W = A·V is final
+      if (emax == 0.f && rmax <= 1e-15f && clusters == 0) {  // nothing to correct: W = A·V is final
         converged = true;
         break;
       }
@@ -1895,12 +1883,11 @@ tn_status_t svd_tall_mixed(tn_ctx* ctx, int64_t m, int64_t n, const cxd* A, int6
       }
       // quadratic convergence: steps and non-orthogonality of at most kRefineStop leave
       // their squares (≤ 1e-16)
-      if (full && emax <= kRefineStop && rmax <= kRefineStop) {
+      if (emax <= kRefineStop && rmax <= kRefineStop) {
         converged = true;
         break;
       }
     }
-    ctx->split_slices = full_slices;
     ctx->refine_outcome = converged ? 0 : (diverged ? 1 : 2);
     bool restored = false;
     if (!converged) {
