@@ -329,6 +329,12 @@ def run_ours(args):
         torch.cuda.synchronize(dev)
     launches_total = ctx.launches() - launches0
     launches_per_step = launches_total / max(1, len(run_layers))
+    # the same layers applied left to right (each layer first moves the centre back
+    # across the chain): the gate order the layers had before the serpentine sweep
+    psi_lr = base.copy()
+    psi_lr.set_precision("mixed")
+    t_lr = timed(psi_lr, [(ly[0], ly[1], False) for ly in run_layers], args.warmup)
+    del psi_lr
     # one more mixed layer with the phase profiler on: each Jacobi sweep graph, GEMM and QR
     # of the step bracketed by CUDA events on the library stream (outside the timed region)
     peaks = pipe_peaks(ctx)
@@ -411,6 +417,9 @@ def run_ours(args):
         "dtype": "c64 (FP32 Jacobi pre-pass; split-BF16 tensor-core GEMMs; FP64 rotations/truncation/overlaps)",
         "data": "synthetic (seeded Gaussian MPS, Haar gates)",
         "config": bench_config(ws, Bt),
+        "left_to_right": {"value": replica_throughput(ws, Bt, K, sum(t_lr) / len(t_lr) * K), "unit": UNIT,
+                          "ms_per_step": 1e3 * sum(t_lr) / len(t_lr),
+                          "note": "mixed B=16 with every layer applied left to right"},
         "fp64": {"value": fp64_value, "unit": UNIT, "ms_per_step": 1e3 * tf / K, "instances": 1,
                  "speedup_of_value": value / fp64_value},
         "fp64_batched": {"value": fp64b_value, "unit": UNIT, "ms_per_step": 1e3 * tfb / K, "instances": Bt,
