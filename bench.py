@@ -396,6 +396,13 @@ def run_ours(args):
             h2d = sum(s.nbytes for st in states for s in st) + sum(np.asarray(g).nbytes for g in ly[1])
             d2h = sum(s.nbytes for st in new_states for s in st)
         states = new_states
+    # algorithmic work of the timed layers (tenetgb.flops_bytes: two QR moves, θ, the gate
+    # and the Golub–Reinsch SVD count per gate) on the saturated bonds
+    from tenetgb import flops_bytes as F
+
+    sat_bonds = base.bondsizes()
+    timed_layers = run_layers[args.warmup:]
+    layer_flops = [F.tebd_layer(sat_bonds, ly[0], len(ly[1])) for ly in timed_layers]
     # max over ranks
     K = args.steps
     tm, tf, tfb, te = max_over_ranks([sum(t_mixed), sum(t_fp64) / len(t_fp64) * K,
@@ -417,6 +424,11 @@ def run_ours(args):
         "dtype": "c64 (FP32 Jacobi pre-pass; split-BF16 tensor-core GEMMs; FP64 rotations/truncation/overlaps)",
         "data": "synthetic (seeded Gaussian MPS, Haar gates)",
         "config": bench_config(ws, Bt),
+        "algorithmic_tflops": {"mixed_batched": ws * Bt * sum(layer_flops) / tm / 1e12,
+                               "fp64": ws * sum(layer_flops) / (sum(t_fp64) / len(t_fp64) * K) / 1e12,
+                               "gflop_per_layer_instance": sum(layer_flops) / len(layer_flops) / 1e9,
+                               "convention": "two QR gauge moves + theta + gate + Golub-Reinsch SVD per gate, complex "
+                                             "MAC = 8 flops (tenetgb.flops_bytes)"},
         "left_to_right": {"value": replica_throughput(ws, Bt, K, sum(t_lr) / len(t_lr) * K), "unit": UNIT,
                           "ms_per_step": 1e3 * sum(t_lr) / len(t_lr),
                           "note": "mixed B=16 with every layer applied left to right"},
@@ -482,12 +494,16 @@ def run_reference(args):
     all_layers = layers_for(SAT_LAYERS + args.warmup + args.steps)
     psi = O.OMPS(W.random_mps_arrays(L_SITES, 2, CHI0, seed=2))
     O.tebd(psi, all_layers[:SAT_LAYERS], maxdim=CHI_MAX, threshold=CUTOFF)
-    times = []
+    from tenetgb import flops_bytes as F
+
+    times, flops = [], 0.0
     for k, ly in enumerate(all_layers[SAT_LAYERS:]):
+        fl = F.tebd_layer(psi.bondsizes(), ly[0], len(ly[1]))
         t0 = time.perf_counter()
         O.tebd(psi, [ly], maxdim=CHI_MAX, threshold=CUTOFF)
         if k >= args.warmup:
             times.append(time.perf_counter() - t0)
+            flops += fl
     t = sum(times)
     value = args.steps / t
     out = {
@@ -499,6 +515,7 @@ def run_reference(args):
                          "sample": "whole saturated brickwork layers (31-32 gates) per step, one MPS, numpy/LAPACK "
                                    f"on {os.cpu_count()} threads"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "algorithmic_tflops": flops / t / 1e12,
     }
     print(json.dumps(out), flush=True)
 
@@ -816,30 +833,11 @@ def run_kernels(args, ctx=None, stream=None):
 
 def batched_flops(Ls, chis, maxdims, d=2):
     """Algorithmic flops of canonize!(ψ, L) → compress!(ψ; maxdim) for the given shapes
-    (complex: QR 4(2mn² − ⅔n³) ×2 with Q; SVD 4(4m²n + 8mn² + 9n³); GEMM 8mnk)."""
+    (tenetgb.flops_bytes conventions)."""
+    from tenetgb import flops_bytes as F
     from tenetgb import workloads as W
 
-    def qr(m, n):
-        return 2 * 4 * (2 * m * n * n - 2 * n**3 / 3)
-
-    def svd(m, n):
-        m, n = max(m, n), min(m, n)
-        return 4 * (4 * m * m * n + 8 * m * n * n + 9 * n**3)
-
-    tot = 0.0
-    for L, chi, md in zip(Ls, chis, maxdims):
-        b = [1] + W.clamped_bonds(L, d, chi) + [1]
-        for k in range(1, L):  # QR sweep: A_k (b[k-1] d × b[k]), R·A_{k+1}
-            tot += qr(b[k - 1] * d, b[k]) + 8 * b[k] * b[k] * d * b[k + 1]
-        for i in range(L, 1, -1):  # LQ sweep
-            tot += qr(d * b[i], b[i - 1]) + 8 * b[i - 2] * d * b[i - 1] * b[i - 1]
-        prev = 1
-        for k in range(1, L):  # SVD sweep with truncation
-            m, n = prev * d, b[k]
-            r = min(md, m, n)
-            tot += svd(m, n) + 8 * r * n * m + 8 * r * n * d * b[k + 1]
-            prev = r
-    return tot
+    return sum(F.canonize_compress(L, W.clamped_bonds(L, d, chi), md, d) for L, chi, md in zip(Ls, chis, maxdims))
 
 
 def run_batched(args, ctx=None):
