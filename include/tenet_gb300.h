@@ -266,6 +266,17 @@ tn_status_t tn_simple_update(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec,
                              const void* d_A, const void* d_B, const void* d_G,
                              int64_t maxdim, double threshold, void* d_Aout, void* d_Bout,
                              double* d_Sout, int64_t* rank);
+/* the same with Muscle's `absorb` keyword: TN_ABSORB_EQUALLY (A' = U√S, B' = √S Vh, as
+ * tn_simple_update), TN_ABSORB_U (A' = U·S, B' = Vh right-isometric) or TN_ABSORB_V
+ * (A' = U left-isometric, B' = S·Vh).  Every mode gives the same A'B'. */
+#define TN_ABSORB_EQUALLY 0
+#define TN_ABSORB_V 1
+#define TN_ABSORB_U 2
+tn_status_t tn_simple_update_absorb(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec,
+                                    int64_t chl, int64_t d1, int64_t chm, int64_t d2, int64_t chr,
+                                    const void* d_A, const void* d_B, const void* d_G,
+                                    int64_t maxdim, double threshold, int32_t absorb,
+                                    void* d_Aout, void* d_Bout, double* d_Sout, int64_t* rank);
 
 /* ------------------------------------------------------------------------------------
  * Device-resident MPS (src/Components/MPS.jl:13-94) with the canonical-form trait

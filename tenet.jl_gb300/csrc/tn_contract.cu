@@ -178,3 +178,22 @@ extern "C" tn_status_t tn_simple_update(tn_ctx* ctx, tn_dtype_t dtype, tn_precis
   return simple_update_core(ctx, prec, chl, d1, chm, d2, chr, (const cxd*)A, 0, (const cxd*)B, 0, (const cxd*)G, maxdim,
                             threshold, 1, fixed_out, &f, Sout, rank);
 }
+
+extern "C" tn_status_t tn_simple_update_absorb(tn_ctx* ctx, tn_dtype_t dtype, tn_precision_t prec, int64_t chl,
+                                               int64_t d1, int64_t chm, int64_t d2, int64_t chr, const void* A,
+                                               const void* B, const void* G, int64_t maxdim, double threshold,
+                                               int32_t absorb, void* Aout, void* Bout, double* Sout, int64_t* rank) {
+  if (!ctx) return TN_EINVAL;
+  TN_ARG(ctx, absorb == TN_ABSORB_EQUALLY || absorb == TN_ABSORB_U || absorb == TN_ABSORB_V,
+         "tn_simple_update_absorb: absorb must be TN_ABSORB_EQUALLY, TN_ABSORB_U or TN_ABSORB_V");
+  if (absorb == TN_ABSORB_EQUALLY)
+    return tn_simple_update(ctx, dtype, prec, chl, d1, chm, d2, chr, A, B, G, maxdim, threshold, Aout, Bout, Sout,
+                            rank);
+  TN_ARG(ctx, dtype == TN_C64, "tn_simple_update_absorb: only C64 is implemented");
+  TN_ARG(ctx, chl >= 1 && d1 >= 1 && chm >= 1 && d2 >= 1 && chr >= 1, "tn_simple_update_absorb: sizes must be >= 1");
+  TN_ARG(ctx, A && B && G && Aout && Bout && rank, "tn_simple_update_absorb: null pointer");
+  FixedOut f{(cxd*)Aout, (cxd*)Bout};
+  return simple_update_core(ctx, prec, chl, d1, chm, d2, chr, (const cxd*)A, 0, (const cxd*)B, 0, (const cxd*)G, maxdim,
+                            threshold, 1, fixed_out, &f, Sout, rank,
+                            absorb == TN_ABSORB_U ? kAbsorbLeft : kAbsorbRight);
+}

@@ -115,6 +115,10 @@ SIGNATURES = {
         _st,
         [_vp, C.c_int, C.c_int, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp, _i64, _dbl, _vp, _vp, _vp, _pi64],
     ),
+    "tn_simple_update_absorb": (
+        _st,
+        [_vp, C.c_int, C.c_int, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp, _i64, _dbl, _i32, _vp, _vp, _vp, _pi64],
+    ),
     "tn_mps_create": (_st, [_vp, _i32, _i32, _pi64, _i64, C.c_int, C.POINTER(_vp)]),
     "tn_mps_create_batched": (_st, [_vp, _i32, _i32, _i32, _pi64, _i64, C.c_int, C.POINTER(_vp)]),
     "tn_mps_batch_size": (_st, [_vp, _pi32]),

@@ -398,9 +398,14 @@ def scale(t: DeviceTensor, s):
     return t
 
 
+_ABSORB = {"equally": 0, "v": 1, "u": 2}
+
+
 def simple_update(A: DeviceTensor, ia, B: DeviceTensor, ib, bond, op: DeviceTensor, oa, ob, maxdim=None,
-                  threshold=None, precision="native"):
-    """Muscle.simple_update(A, ia, B, ib, bond, op, oa, ob; maxdim, absorb=AbsorbEqually()).
+                  threshold=None, precision="native", absorb="equally"):
+    """Muscle.simple_update(A, ia, B, ib, bond, op, oa, ob; maxdim, absorb): ``absorb`` is
+    "equally" (AbsorbEqually, A' = U√S, B' = √S Vh), "u" (AbsorbU: A' = U·S, B' = Vh) or
+    "v" (AbsorbV: A' = U, B' = S·Vh).
 
     ``ia``/``ib`` are A's and B's physical labels, ``oa``/``ob`` the gate's output labels
     matching them; the gate's input labels are ``ia``/``ib``.  Returns (A', B') with A'
@@ -420,11 +425,14 @@ def simple_update(A: DeviceTensor, ia, B: DeviceTensor, ib, bond, op: DeviceTens
     An = DeviceTensor(A.ctx, ([chl] if la else []) + [d1, kmax], A.dtype, la + [ia, bond])
     Bn = DeviceTensor(A.ctx, [kmax, d2] + ([chr_] if lb else []), A.dtype, [bond, ib] + lb)
     r = C.c_int64()
+    if absorb not in _ABSORB:
+        raise ValueError(f"absorb must be one of {sorted(_ABSORB)}")
     A.ctx.check(
-        A.ctx.lib.tn_simple_update(A.ctx.h, L.TN_C64, precision_code(precision), chl, d1, chm, d2, chr_,
-                                   C.c_void_p(Am.ptr), C.c_void_p(Bm.ptr), C.c_void_p(G.ptr),
-                                   -1 if maxdim is None else int(maxdim), -1.0 if threshold is None else float(threshold),
-                                   C.c_void_p(An.ptr), C.c_void_p(Bn.ptr), None, C.byref(r))
+        A.ctx.lib.tn_simple_update_absorb(A.ctx.h, L.TN_C64, precision_code(precision), chl, d1, chm, d2, chr_,
+                                          C.c_void_p(Am.ptr), C.c_void_p(Bm.ptr), C.c_void_p(G.ptr),
+                                          -1 if maxdim is None else int(maxdim),
+                                          -1.0 if threshold is None else float(threshold), _ABSORB[absorb],
+                                          C.c_void_p(An.ptr), C.c_void_p(Bn.ptr), None, C.byref(r))
     )
     k = r.value
     An.shape = tuple(([chl] if la else []) + [d1, k])

@@ -284,3 +284,43 @@ def test_batched_compress_and_amplitude(ctx):
         assert abs(amp[b] - a_o) <= 1e-12 * np.sqrt(abs(O.overlap(p, p)))
         O.compress(p, maxdim=6)
         assert abs(nrm[b] - O.norm(p)) <= 1e-12 * O.norm(p)
+
+
+@pytest.mark.parametrize("precision", ["native", "mixed"])
+@pytest.mark.parametrize("chl,chr_", [(64, 64), (32, 64), (64, 32)])
+def test_simple_update_absorb_modes(ctx, precision, chl, chr_):
+    """Muscle.simple_update's absorb keyword: AbsorbEqually, AbsorbU and AbsorbV give the
+    same truncated θ' = A'B'; AbsorbV leaves A' left-isometric, AbsorbU leaves B'
+    right-isometric, AbsorbEqually splits S evenly (A'ᴴA' = B'B'ᴴ = diag S)."""
+    import tenetgb
+    from tenetgb import workloads as W
+
+    rng = np.random.default_rng(chl + 2 * chr_)
+    chm, d = 48, 2
+
+    def cg(shape):
+        return (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)) / np.sqrt(2)
+
+    A = tenetgb.DeviceTensor.from_numpy(ctx, cg((chl, d, chm)), ["l", "a", "m"])
+    B = tenetgb.DeviceTensor.from_numpy(ctx, cg((chm, d, chr_)), ["m", "b", "r"])
+    G = tenetgb.DeviceTensor.from_numpy(ctx, W.gate_tensor(W.haar_unitary(rng, 4)), ["ao", "bo", "a", "b"])
+    out = {}
+    for absorb in ("equally", "u", "v"):
+        An, Bn = tenetgb.simple_update(A, "a", B, "b", "m", G, "ao", "bo", maxdim=40, threshold=1e-12,
+                                       precision=precision, absorb=absorb)
+        a = An.numpy().reshape(chl * d, -1, order="F")
+        b = Bn.numpy().reshape(-1, d * chr_, order="F")
+        out[absorb] = (a, b)
+    ref = out["equally"][0] @ out["equally"][1]
+    for absorb, (a, b) in out.items():
+        assert a.shape[1] == 40
+        assert np.linalg.norm(a @ b - ref) <= 1e-12 * np.linalg.norm(ref), absorb
+    a, _ = out["v"]
+    assert np.abs(a.conj().T @ a - np.eye(40)).max() <= 1e-12
+    _, b = out["u"]
+    assert np.abs(b @ b.conj().T - np.eye(40)).max() <= 1e-12
+    a, b = out["equally"]
+    ga, gb = a.conj().T @ a, b @ b.conj().T
+    assert np.abs(ga - gb).max() <= 1e-12 * np.abs(ga).max()
+    with pytest.raises(ValueError):
+        tenetgb.simple_update(A, "a", B, "b", "m", G, "ao", "bo", maxdim=40, absorb="both")
