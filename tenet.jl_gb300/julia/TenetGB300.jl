@@ -353,10 +353,11 @@ end
 
 """
     Muscle.simple_update(A, ia, B, ib, bond, op, oa, ob; maxdim, absorb=AbsorbEqually())
-    on GB300 tensors (tn_simple_update; src/Operations/simple_update.jl:53-64)
+    on GB300 tensors (tn_simple_update_absorb; src/Operations/simple_update.jl:53-64)
 
 θ = op·A·B over the bond and the physical indices ia/ib (op's input indices), thin SVD
-over (A's side)|(B's side), at most `maxdim` values kept, √S into both sides.  A'
+over (A's side)|(B's side), at most `maxdim` values kept, S split by `absorb`
+(AbsorbEqually: √S into both sides; AbsorbU: into A'; AbsorbV: into B').  A'
 carries (A's other indices…, ia, bond), B' (bond, ib, B's other indices…): the
 physical indices keep A's and B's labels, which Tenet renames back afterwards.
 """
@@ -364,7 +365,10 @@ function Muscle.simple_update(A::Tensor{ComplexF64,Na,<:GB300Array}, ia::Index, 
                               ib::Index, bond::Index, op::Tensor{ComplexF64,4,<:GB300Array}, oa::Index, ob::Index;
                               maxdim=nothing, threshold=nothing, absorb=Muscle.AbsorbEqually(),
                               precision=TN_PREC_NATIVE) where {Na,Nb}
-    absorb isa Muscle.AbsorbEqually || throw(ArgumentError("GB300 simple_update: only AbsorbEqually is implemented"))
+    # Muscle's absorb behaviours (AbsorbEqually, AbsorbU, AbsorbV) → TN_ABSORB_*
+    mode = absorb isa Muscle.AbsorbEqually ? Int32(0) : absorb isa Muscle.AbsorbV ? Int32(1) :
+           absorb isa Muscle.AbsorbU ? Int32(2) :
+           throw(ArgumentError("GB300 simple_update: absorb must be AbsorbEqually, AbsorbU or AbsorbV"))
     la = filter(i -> i != ia && i != bond, collect(inds(A)))
     lb = filter(i -> i != ib && i != bond, collect(inds(B)))
     Am = arranged(A, [la..., ia, bond])
@@ -379,12 +383,12 @@ function Muscle.simple_update(A::Tensor{ComplexF64,Na,<:GB300Array}, ia::Index, 
     An = GB300Array{ComplexF64}(undef, (size(Am)[1:length(la)]..., d1, kmax); ctx)
     Bn = GB300Array{ComplexF64}(undef, (kmax, d2, size(Bm)[3:end]...); ctx)
     r = Ref{Int64}(0)
-    check(ccall((:tn_simple_update, libtenetgb), Int32,
+    check(ccall((:tn_simple_update_absorb, libtenetgb), Int32,
                 (Ptr{Cvoid}, Int32, Int32, Int64, Int64, Int64, Int64, Int64, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Int64,
-                 Float64, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Int64}),
+                 Float64, Int32, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cvoid}, Ref{Int64}),
                 ctx.h, TN_C64, precision, chl, d1, chm, d2, chr, Am.ptr, Bm.ptr, G.ptr,
-                maxdim === nothing ? -1 : maxdim, threshold === nothing ? -1.0 : Float64(threshold), An.ptr, Bn.ptr,
-                C_NULL, r), ctx.h)
+                maxdim === nothing ? -1 : maxdim, threshold === nothing ? -1.0 : Float64(threshold), mode, An.ptr,
+                Bn.ptr, C_NULL, r), ctx.h)
     An.dims = (size(Am)[1:length(la)]..., d1, Int(r[]))
     Bn.dims = (Int(r[]), d2, size(Bm)[3:end]...)
     return Tensor(An, [la..., ia, bond]), Tensor(Bn, [bond, ib, lb...])
