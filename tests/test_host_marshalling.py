@@ -1,0 +1,51 @@
+"""CPU checks of the host layer's argument marshalling for the layer evolution entry
+(no GPU: the library call is replaced by a recorder): layer starts, gate counts, the
+per-layer direction (two-element layers are left to right), the gates flattened in
+column-major order layer after layer, and the truncation arguments."""
+
+import ctypes as C
+
+import numpy as np
+
+
+class Recorder:
+    def __init__(self):
+        self.calls = []
+
+    def tn_mps_evolve_layers(self, h, n, starts, counts, rev, buf, maxdim, thr):
+        total = sum(counts[i] for i in range(n))
+        p = C.cast(buf, C.POINTER(C.c_double))
+        flat = np.array([p[i] for i in range(2 * 16 * total)])
+        self.calls.append(dict(n=n, starts=[starts[i] for i in range(n)], counts=[counts[i] for i in range(n)],
+                               rev=[rev[i] for i in range(n)], gates=flat[0::2] + 1j * flat[1::2], maxdim=maxdim,
+                               thr=thr))
+        return 0
+
+
+def test_layers_marshalled():
+    from tenetgb.mps import MPS
+
+    rng = np.random.default_rng(0)
+    g = [rng.standard_normal((2, 2, 2, 2)) + 1j * rng.standard_normal((2, 2, 2, 2)) for _ in range(5)]
+    m = MPS.__new__(MPS)
+    m.lib = Recorder()
+    m.h = None
+    m._chk = lambda st: None
+    m.evolve_brickwork_([(1, g[:3]), (2, g[3:], True)], maxdim=64, threshold=1e-12)
+    c = m.lib.calls[0]
+    assert c["n"] == 2 and c["starts"] == [1, 2] and c["counts"] == [3, 2] and c["rev"] == [0, 1]
+    want = np.concatenate([G.reshape(-1, order="F") for G in g])
+    assert np.array_equal(c["gates"], want)
+    assert c["maxdim"] == 64 and c["thr"] == 1e-12
+    m.evolve_brickwork_([(1, g[:1], False)])
+    c = m.lib.calls[1]
+    assert c["rev"] == [0] and c["maxdim"] == -1 and c["thr"] == -1.0
+
+
+def test_serpentine_workload_directions():
+    from tenetgb import workloads as W
+
+    layers = W.tebd_layers(10, 4, serpentine=True)
+    assert [ly[2] for ly in layers] == [False, True, False, True]
+    assert [ly[0] for ly in layers] == [1, 2, 1, 2] and [len(ly[1]) for ly in layers] == [5, 4, 5, 4]
+    assert all(not ly[2] for ly in W.tebd_layers(10, 4))
