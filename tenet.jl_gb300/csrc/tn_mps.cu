@@ -782,7 +782,7 @@ tn_status_t tn_mps_simple_update(tn_mps* p, int32_t n_sites, int32_t a, const vo
   tn_ctx* ctx = p->ctx;
   TN_ARG(ctx, h_G != nullptr, "simple_update: null gate");
   TN_ARG(ctx, n_sites == 1 || n_sites == 2, "Operator must act on one or two sites");
-  TN_ARG(ctx, a >= 1 && a + n_sites - 1 <= p->L, "Operator plugs must be present in the MPS");
+  TN_ARG(ctx, a >= 1 && (int64_t)a + n_sites - 1 <= p->L, "Operator plugs must be present in the MPS");
   size_t ge = n_sites == 1 ? (size_t)(p->d * p->d) : (size_t)(p->d * p->d * p->d * p->d);
   TN_RETURN_IF(upload_gates(p, h_G, ge));
   TN_RETURN_IF(canonize_mixed(p, a, a + n_sites - 1));
@@ -803,7 +803,7 @@ tn_status_t tn_mps_evolve_layers(tn_mps* p, int32_t n_layers, const int32_t* sta
   size_t total = 0;
   const size_t g4 = (size_t)p->d * p->d * p->d * p->d;
   for (int l = 0; l < n_layers; ++l) {
-    TN_ARG(ctx, n_gates[l] >= 0 && starts[l] >= 1 && starts[l] + 2 * n_gates[l] - 1 <= p->L,
+    TN_ARG(ctx, n_gates[l] >= 0 && starts[l] >= 1 && (int64_t)starts[l] + 2 * (int64_t)n_gates[l] - 1 <= p->L,
            "evolve: layer out of range");
     total += (size_t)n_gates[l] * g4;
   }
