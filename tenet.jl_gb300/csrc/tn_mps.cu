@@ -68,8 +68,15 @@ tn_status_t ensure_site(tn_mps* p, int i, size_t elems) {
   void* np = nullptr;
   TN_RETURN_IF(tn_dev_alloc(ctx, elems * sizeof(cxd) * p->B, &np));
   if (p->site[i]) {
-    TN_RETURN_IF(copy_instances(ctx, (cxd*)np, elems, p->site[i], p->cap[i], (size_t)sz(p, i), p->B));
-    TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    tn_status_t st = copy_instances(ctx, (cxd*)np, elems, p->site[i], p->cap[i], (size_t)sz(p, i), p->B);
+    if (st == TN_OK) {
+      const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+      if (e != cudaSuccess) st = tn_set_error(ctx, TN_ECUDA, "site growth: %s", cudaGetErrorString(e));
+    }
+    if (st != TN_OK) {  // the site keeps its old storage
+      tn_dev_free(ctx, np);
+      return st;
+    }
     TN_RETURN_IF(tn_dev_free(ctx, p->site[i]));
   }
   p->site[i] = (cxd*)np;
@@ -82,6 +89,9 @@ tn_status_t ensure_lam(tn_mps* p, int64_t n) {
   tn_ctx* ctx = p->ctx;
   TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
   if (p->lam) TN_RETURN_IF(tn_dev_free(ctx, p->lam));
+  p->lam = nullptr;  // (an allocation failure below leaves no Λ storage, not a freed one)
+  p->lam_cap = 0;
+  p->lam_len = 0;    // the growth does not keep the old values
   void* np = nullptr;
   size_t c = std::max<size_t>(n, 64);
   TN_RETURN_IF(tn_dev_alloc(ctx, c * sizeof(double) * p->B, &np));
@@ -561,15 +571,25 @@ tn_status_t tn_mps_create_batched(tn_ctx* ctx, int32_t B, int32_t L, int32_t d, 
   p->site.assign(L + 1, nullptr);
   p->cap.assign(L + 1, 0);
   for (int i = 1; i <= L; ++i) {
-    size_t e = (size_t)(p->cap_bond[i - 1] * d * p->cap_bond[i]);
-    tn_status_t st = ensure_site(p, i, e);
+    // elements per instance, checked against int64 overflow (a capacity is a bond the caller
+    // gave or d^min(i, L-i), both unbounded here)
+    const int64_t cl = p->cap_bond[i - 1], cr = p->cap_bond[i];
+    tn_status_t st = TN_OK;
+    if (cl > INT64_MAX / (int64_t)sizeof(cxd) / B / d / cr)
+      st = tn_set_error(ctx, TN_EINVAL, "tn_mps_create: site %d of %lld x %d x %lld elements is too large", i,
+                        (long long)cl, d, (long long)cr);
+    const size_t e = st == TN_OK ? (size_t)(cl * d * cr) : 0;
+    if (st == TN_OK) st = ensure_site(p, i, e);
+    if (st == TN_OK) {
+      const cudaError_t ce = cudaMemsetAsync(p->site[i], 0, e * B * sizeof(cxd), ctx->stream);
+      if (ce != cudaSuccess) st = tn_set_error(ctx, TN_ECUDA, "tn_mps_create: %s", cudaGetErrorString(ce));
+    }
     if (st != TN_OK) {
       for (int j = 1; j <= L; ++j)
         if (p->site[j]) tn_dev_free(ctx, p->site[j]);
       delete p;
       return st;
     }
-    TN_CHECK_CUDA(ctx, cudaMemsetAsync(p->site[i], 0, e * B * sizeof(cxd), ctx->stream));
   }
   p->kind = TN_FORM_MIXED;
   p->lo = 1;
@@ -622,9 +642,17 @@ tn_status_t tn_mps_copy(const tn_mps* src, tn_mps** out) {
   p->lo = src->lo;
   p->hi = src->hi;
   if (src->lam_len > 0) {
-    TN_RETURN_IF(ensure_lam(p, src->lam_len));
-    TN_CHECK_CUDA(ctx, cudaMemcpy2DAsync(p->lam, p->lam_cap * sizeof(double), src->lam, src->lam_cap * sizeof(double),
-                                         src->lam_len * sizeof(double), src->B, cudaMemcpyDeviceToDevice, ctx->stream));
+    tn_status_t st = ensure_lam(p, src->lam_len);
+    if (st == TN_OK) {
+      const cudaError_t e = cudaMemcpy2DAsync(p->lam, p->lam_cap * sizeof(double), src->lam,
+                                              src->lam_cap * sizeof(double), src->lam_len * sizeof(double), src->B,
+                                              cudaMemcpyDeviceToDevice, ctx->stream);
+      if (e != cudaSuccess) st = tn_set_error(ctx, TN_ECUDA, "tn_mps_copy: %s", cudaGetErrorString(e));
+    }
+    if (st != TN_OK) {
+      tn_mps_destroy(p);
+      return st;
+    }
     p->lam_len = src->lam_len;
   }
   *out = p;
