@@ -441,6 +441,8 @@ tn_status_t upload_gates(tn_mps* p, const void* h, size_t elems) {
   if (elems > p->gates_cap) {
     TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (p->gates) TN_RETURN_IF(tn_dev_free(ctx, p->gates));
+    p->gates = nullptr;  // a failed allocation below must not leave the freed buffer in use
+    p->gates_cap = 0;
     void* np = nullptr;
     TN_RETURN_IF(tn_dev_alloc(ctx, elems * sizeof(cxd), &np));
     p->gates = (cxd*)np;
@@ -1054,18 +1056,15 @@ tn_status_t evolve_mpo_direct(tn_mps* p, const std::vector<const cxd*>& hW, cons
   const int L = p->L, d = p->d, B = p->B;
   std::vector<cxd*> nsite(L + 1, nullptr);
   std::vector<size_t> ncap(L + 1, 0);
-  for (int i = 1; i <= L; ++i) {
+  // new site i into nsite[i]; on any failure the caller frees every nsite[] made so far
+  auto build_site = [&](int i) -> tn_status_t {
     const int64_t l = p->bond[i - 1], r = p->bond[i], a = w[i - 1], b = w[i];
     const int64_t nel = l * a * d * r * b;
     const size_t need = ws_round(sizeof(cxd) * (size_t)(a * d * d * b)) * 2 +
                         ws_round(sizeof(cxd) * (size_t)(l * r * d * B)) + 2 * ws_round(sizeof(cxd) * (size_t)(nel * B));
-    tn_status_t st = ws_reserve(ctx, need);
+    TN_RETURN_IF(ws_reserve(ctx, need));
     void* np = nullptr;
-    if (st == TN_OK) st = tn_dev_alloc(ctx, sizeof(cxd) * (size_t)nel * B, &np);
-    if (st != TN_OK) {
-      for (int j = 1; j < i; ++j) tn_dev_free(ctx, nsite[j]);
-      return st;
-    }
+    TN_RETURN_IF(tn_dev_alloc(ctx, sizeof(cxd) * (size_t)nel * B, &np));
     nsite[i] = (cxd*)np;
     ncap[i] = (size_t)nel;
     cxd* W0 = ws_take<cxd>(ctx, (size_t)(a * d * d * b));
@@ -1096,6 +1095,16 @@ tn_status_t evolve_mpo_direct(tn_mps* p, const std::vector<const cxd*>& hW, cons
       TN_RETURN_IF(permute_t<pd2>(ctx, 6, dims, nullptr, perm, (const pd2*)C1, (pd2*)nsite[i], false));
     }
     TN_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));  // W0 came from pageable host memory
+    return TN_OK;
+  };
+  for (int i = 1; i <= L; ++i) {
+    const tn_status_t st = build_site(i);
+    if (st != TN_OK) {
+      cudaStreamSynchronize(ctx->stream);
+      for (int j = 1; j <= i; ++j)
+        if (nsite[j]) tn_dev_free(ctx, nsite[j]);
+      return st;
+    }
   }
   for (int i = 1; i <= L; ++i) {
     TN_RETURN_IF(tn_dev_free(ctx, p->site[i]));
