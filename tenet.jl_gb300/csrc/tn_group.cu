@@ -756,7 +756,8 @@ extern "C" {
 
 tn_status_t tn_group_create(tn_ctx* ctx, int32_t B, const int32_t* L, int32_t d, const int64_t* bonds,
                             tn_group** out) {
-  if (!ctx || !out || !L || B < 1 || d < 1) return tn_set_error(ctx, TN_EINVAL, "tn_group_create: bad arguments");
+  if (!ctx || !out || !L || !bonds || B < 1 || d < 1)
+    return tn_set_error(ctx, TN_EINVAL, "tn_group_create: bad arguments");
   auto* g = new tn_group();
   g->ctx = ctx;
   g->B = B;
@@ -785,7 +786,14 @@ tn_status_t tn_group_create(tn_ctx* ctx, int32_t B, const int32_t* L, int32_t d,
     g->bond0.push_back(g->bond[b]);
     g->cap[b].assign(L[b] + 1, 0);
     for (int i = 1; i <= L[b]; ++i) {
-      g->cap[b][i] = g->bond[b][i - 1] * d * g->bond[b][i];
+      const int64_t bl = g->bond[b][i - 1], br = g->bond[b][i];
+      // a site's bytes, and their running total, must fit in 63 bits
+      if (bl > INT64_MAX / (int64_t)sizeof(cxd) / d / br / 2 ||
+          total > (size_t)INT64_MAX - al256(sizeof(cxd) * (size_t)(bl * d * br))) {
+        delete g;
+        return tn_set_error(ctx, TN_EINVAL, "tn_group_create: site %d of instance %d is too large", i, b);
+      }
+      g->cap[b][i] = bl * d * br;
       total += al256(sizeof(cxd) * (size_t)g->cap[b][i]);
     }
   }
