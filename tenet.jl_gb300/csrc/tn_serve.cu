@@ -735,11 +735,21 @@ tn_status_t pool_alloc(tn_server* S, int L, int d, const int64_t* bonds, PoolMPS
     p.bond[i] = bonds[i - 1];
     p.maxbond = std::max(p.maxbond, p.bond[i]);
   }
+  // every site's elements, and the pool entry's bytes, must stay far inside 63 bits
+  const int64_t kMaxElems = (int64_t)1 << 40;
+  int64_t elems = 0;
+  for (int i = 1; i <= L; ++i) {
+    const int64_t bl = p.bond[i - 1], br = p.bond[i];
+    if (bl > kMaxElems / d / br || elems > kMaxElems - bl * d * br)
+      return serr(TN_EINVAL, "serve: the MPS has more than 2^40 elements");
+    elems += bl * d * br;
+  }
   size_t bytes = 0;
   for (int i = 1; i <= L; ++i) bytes += cxb(p.bond[i - 1] * d * p.bond[i]);
   bytes *= 2;  // A_i and X_i
   if (S->prec == TN_PREC_MIXED)
-    for (int i = 1; i <= L; ++i) bytes += al(sizeof(cxf) * (size_t)(p.bond[i - 1] * d * p.bond[i]));  if (S->budget && ctx->in_use + bytes > S->budget)
+    for (int i = 1; i <= L; ++i) bytes += al(sizeof(cxf) * (size_t)(p.bond[i - 1] * d * p.bond[i]));
+  if (S->budget && ctx->in_use + bytes > S->budget)
     return serr(TN_ENOMEM, "serve: the MPS needs %zu bytes; %zu of the %zu-byte HBM budget are in use", bytes,
                 ctx->in_use, S->budget);
   tn_status_t st = tn_dev_alloc(ctx, bytes, &p.block);
