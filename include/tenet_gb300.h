@@ -99,7 +99,8 @@ tn_status_t tn_pipe_peak(tn_ctx* ctx, int32_t which, double* tflops);
 /* autotuner: with enable != 0 the first call of an unseen shape bucket times the
  * candidate launch configurations (QR panel and slab widths) and records the fastest.
  * tn_tuning_dump writes the table as text ("key v1 v2" lines; *needed = bytes incl. the
- * terminator); tn_tuning_load reads such text back (a tuning cache file). */
+ * terminator); tn_tuning_load reads such text back (a tuning cache file; QR entries hold a
+ * panel width in 1, 2, 4, …, 32 and a slab width in 1, 2, 4, anything else is TN_EINVAL). */
 tn_status_t tn_set_autotune(tn_ctx* ctx, int32_t enable);
 tn_status_t tn_tuning_dump(tn_ctx* ctx, char* buf, size_t len, size_t* needed);
 tn_status_t tn_tuning_load(tn_ctx* ctx, const char* text);

@@ -256,7 +256,10 @@ tn_status_t tn_tuning_load(tn_ctx* ctx, const char* text) {
     char key[128];
     int a = 0, b = 0, used = 0;
     if (sscanf(p, "%127s %d %d%n", key, &a, &b, &used) != 3) break;
-    if (a < 1 || a > 32 || b < 1 || b > 4) return tn_set_error(ctx, TN_EINVAL, "tn_tuning_load: bad entry %s", key);
+    // the autotuner's candidate set: panel widths 1…32 and slab widths 1, 2, 4 (powers of two)
+    const bool pow2 = (a & (a - 1)) == 0 && (b & (b - 1)) == 0;
+    if (a < 1 || a > 32 || b < 1 || b > 4 || !pow2)
+      return tn_set_error(ctx, TN_EINVAL, "tn_tuning_load: bad entry %s %d %d", key, a, b);
     ctx->tuning[key] = {a, b};
     p += used;
     while (*p == '\n' || *p == ' ') ++p;
