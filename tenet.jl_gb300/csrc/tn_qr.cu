@@ -357,25 +357,30 @@ tn_status_t qr_cx(tn_ctx* ctx, int64_t m, int64_t n, const cx<T>* A, int64_t lda
     lda = m;
     sA = m * n;
     float best = 1e30f;
-    cudaEvent_t e0, e1;
-    TN_CHECK_CUDA(ctx, cudaEventCreate(&e0));
-    TN_CHECK_CUDA(ctx, cudaEventCreate(&e1));
-    for (int cand_nb = 4; cand_nb <= nb_max; cand_nb *= 2)
-      for (int cand_slab = 1; cand_slab <= 4; cand_slab *= 2) {
-        TN_CHECK_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
-        TN_RETURN_IF(qr_run<T>(ctx, cand_nb, cand_slab, m, n, A, lda, sA, Q, sQ, R, sR, batch, W, tau, Tm));
-        TN_CHECK_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
-        TN_CHECK_CUDA(ctx, cudaEventSynchronize(e1));
-        float ms = 0;
-        TN_CHECK_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
-        if (ms < best) {
-          best = ms;
-          nb = cand_nb;
-          slab = cand_slab;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto sweep = [&]() -> tn_status_t {
+      TN_CHECK_CUDA(ctx, cudaEventCreate(&e0));
+      TN_CHECK_CUDA(ctx, cudaEventCreate(&e1));
+      for (int cand_nb = 4; cand_nb <= nb_max; cand_nb *= 2)
+        for (int cand_slab = 1; cand_slab <= 4; cand_slab *= 2) {
+          TN_CHECK_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+          TN_RETURN_IF(qr_run<T>(ctx, cand_nb, cand_slab, m, n, A, lda, sA, Q, sQ, R, sR, batch, W, tau, Tm));
+          TN_CHECK_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+          TN_CHECK_CUDA(ctx, cudaEventSynchronize(e1));
+          float ms = 0;
+          TN_CHECK_CUDA(ctx, cudaEventElapsedTime(&ms, e0, e1));
+          if (ms < best) {
+            best = ms;
+            nb = cand_nb;
+            slab = cand_slab;
+          }
         }
-      }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
+      return TN_OK;
+    };
+    const tn_status_t st = sweep();
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    TN_RETURN_IF(st);
     ctx->tuning[key] = {nb, slab};
   }
   const int slot = prof_begin(ctx);
