@@ -308,8 +308,14 @@ class MPS:
         index order [plug a, plug b, plug a', plug b'] (a < b adjacent)."""
         sites = sorted(int(s) for s in np.atleast_1d(sites))
         op = np.asfortranarray(np.asarray(op, dtype=np.complex128))
+        if len(sites) not in (1, 2):
+            raise ValueError("Operator must act on one or two sites")
         if len(sites) == 2 and sites[1] != sites[0] + 1:
             raise ValueError("2-site gates must act on adjacent sites")
+        # the library reads d^(2·nsites) entries from the host array
+        if op.size != self._d ** (2 * len(sites)):
+            raise ValueError(f"a {len(sites)}-site operator on sites of dimension {self._d} has "
+                             f"{self._d ** (2 * len(sites))} entries, got shape {op.shape}")
         self._chk(self.lib.tn_mps_simple_update(self.h, len(sites), sites[0], op.ctypes.data_as(C.c_void_p),
                                                 -1 if maxdim is None else int(maxdim),
                                                 -1.0 if threshold is None else float(threshold)))
@@ -329,6 +335,10 @@ class MPS:
         rev = (C.c_int32 * len(layers))(*[int(bool(ly[2])) if len(ly) > 2 else 0 for ly in layers])
         flat = [np.asfortranarray(np.asarray(G, dtype=np.complex128)).reshape(-1, order="F") for ly in layers
                 for G in ly[1]]
+        for G in flat:  # the library reads d⁴ entries per gate
+            if G.size != self._d ** 4:
+                raise ValueError(f"a two-site gate on sites of dimension {self._d} has {self._d ** 4} entries, "
+                                 f"got {G.size}")
         buf = np.ascontiguousarray(np.concatenate(flat)) if flat else np.zeros(1, np.complex128)
         self._chk(self.lib.tn_mps_evolve_layers(self.h, len(layers), starts, counts, rev,
                                                 buf.ctypes.data_as(C.c_void_p),
@@ -360,6 +370,8 @@ class MPS:
             vecs = _product_vectors(bits)
         else:
             vecs = [np.asarray(v, dtype=np.complex128) for v in bits]
+        if len(vecs) != self._L or any(x.shape != (self._d,) for x in vecs):
+            raise ValueError(f"a product state of {self._L} vectors of length {self._d} is needed")
         v = np.ascontiguousarray(np.stack(vecs))
         out = np.empty(2 * self.batch, dtype=np.float64)
         self._chk(self.lib.tn_mps_amplitude(self.h, v.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.POINTER(C.c_double))))
@@ -369,6 +381,8 @@ class MPS:
     def local_expectations(self, op):
         """⟨ψ|O_i|ψ⟩/⟨ψ|ψ⟩ for every site i."""
         o = np.asfortranarray(np.asarray(op, dtype=np.complex128))
+        if o.shape != (self._d, self._d):
+            raise ValueError(f"a one-site operator is {self._d}×{self._d}, got shape {o.shape}")
         out = np.empty(2 * self._L * self.batch, dtype=np.float64)
         self._chk(self.lib.tn_mps_local_expectations(self.h, o.ctypes.data_as(C.c_void_p),
                                                      out.ctypes.data_as(C.POINTER(C.c_double))))

@@ -22,15 +22,24 @@ class Recorder:
         return 0
 
 
+def fake_mps(lib, L=10, d=2):
+    """A host-side MPS object whose library calls go to ``lib`` (no device)."""
+    from tenetgb.mps import MPS
+
+    m = MPS.__new__(MPS)
+    m.lib = lib
+    m.h = None
+    m._chk = lambda st: None
+    m._L, m._d = L, d
+    return m
+
+
 def test_layers_marshalled():
     from tenetgb.mps import MPS
 
     rng = np.random.default_rng(0)
     g = [rng.standard_normal((2, 2, 2, 2)) + 1j * rng.standard_normal((2, 2, 2, 2)) for _ in range(5)]
-    m = MPS.__new__(MPS)
-    m.lib = Recorder()
-    m.h = None
-    m._chk = lambda st: None
+    m = fake_mps(Recorder())
     m.evolve_brickwork_([(1, g[:3]), (2, g[3:], True)], maxdim=64, threshold=1e-12)
     c = m.lib.calls[0]
     assert c["n"] == 2 and c["starts"] == [1, 2] and c["counts"] == [3, 2] and c["rev"] == [0, 1]
@@ -49,3 +58,33 @@ def test_serpentine_workload_directions():
     assert [ly[2] for ly in layers] == [False, True, False, True]
     assert [ly[0] for ly in layers] == [1, 2, 1, 2] and [len(ly[1]) for ly in layers] == [5, 4, 5, 4]
     assert all(not ly[2] for ly in W.tebd_layers(10, 4))
+
+
+class Refuser:
+    """Any library call is a failure: the host checks must stop bad arrays first."""
+
+    def __getattr__(self, name):
+        raise AssertionError(f"{name} reached the library with a malformed host array")
+
+
+def test_host_arrays_checked_before_the_library_reads_them():
+    """The library reads d^(2·nsites) gate entries, d⁴ per brickwork gate, L×d product
+    vectors and a d×d operator from host memory; wrong shapes are ValueErrors (Tenet's
+    @argcheck) instead of out-of-bounds host reads."""
+    import pytest
+
+    m = fake_mps(Refuser(), L=4, d=2)
+    with pytest.raises(ValueError):
+        m.simple_update_(np.eye(3), [1])
+    with pytest.raises(ValueError):
+        m.simple_update_(np.eye(2), [1, 2])
+    with pytest.raises(ValueError):
+        m.simple_update_(np.eye(4), [1, 2, 3])
+    with pytest.raises(ValueError):
+        m.evolve_brickwork_([(1, [np.eye(2)])])
+    with pytest.raises(ValueError):
+        m.amplitude("010")
+    with pytest.raises(ValueError):
+        m.amplitude([np.ones(3)] * 4)
+    with pytest.raises(ValueError):
+        m.local_expectations(np.eye(4))
