@@ -437,7 +437,10 @@ lifted to 3-D.)
 """
 function GB300MPS(arrays::Vector{Array{ComplexF64,3}}; max_bond=0, precision=TN_PREC_NATIVE, ctx=default_context())
     L = length(arrays)
+    L >= 2 || throw(ArgumentError("an MPS needs at least two sites"))
     d = size(arrays[1], 2)
+    # the library reads χl·d·χr entries of every site with one d for all of them
+    all(a -> size(a, 2) == d, arrays) || throw(ArgumentError("every site must have the same physical dimension"))
     bonds = Int64[size(a, 3) for a in arrays[1:(end - 1)]]
     r = Ref{Ptr{Cvoid}}(C_NULL)
     check(ccall((:tn_mps_create, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int32, Ptr{Int64}, Int64, Int32, Ref{Ptr{Cvoid}}),
@@ -460,6 +463,9 @@ compress!(ψ::GB300MPS; bond=0, maxdim=-1, threshold=-1.0) =
 
 function simple_update!(ψ::GB300MPS, G::Array{ComplexF64}, site::Integer; maxdim=-1, threshold=-1.0)
     nsites = ndims(G) == 2 ? 1 : 2
+    # the library reads d^(2·nsites) entries from G
+    length(G) == ψ.d^(2 * nsites) ||
+        throw(ArgumentError("a $nsites-site operator on sites of dimension $(ψ.d) has $(ψ.d^(2 * nsites)) entries"))
     check(ccall((:tn_mps_simple_update, libtenetgb), Int32, (Ptr{Cvoid}, Int32, Int32, Ptr{ComplexF64}, Int64, Float64),
                 ψ.h, nsites, site, G, maxdim, threshold), ψ.ctx.h)
     return ψ
