@@ -486,11 +486,24 @@ end
 
 LinearAlgebra.normalize!(ψ::GB300MPS) = (check(ccall((:tn_mps_normalize, libtenetgb), Int32, (Ptr{Cvoid},), ψ.h), ψ.ctx.h); ψ)
 
+# the library reads w_{i-1}·d·d·w_i entries of MPO site i (w_0 = w_L = 1): the sizes must chain
+function check_mpo(ψ, H)
+    length(H) == ψ.L || throw(ArgumentError("the MPO must have one site per MPS site"))
+    for (i, W) in enumerate(H)
+        (size(W, 2) == ψ.d && size(W, 3) == ψ.d) ||
+            throw(ArgumentError("MPO site $i: physical dimensions must be $(ψ.d)"))
+        size(W, 1) == (i == 1 ? 1 : size(H[i - 1], 4)) ||
+            throw(ArgumentError("MPO site $i: left virtual dimension does not match its neighbour"))
+    end
+    size(H[end], 4) == 1 || throw(ArgumentError("the last MPO site must have a right virtual dimension of 1"))
+    return nothing
+end
+
 # evolve!(ψ, op::MPO) — src/Operations/evolve.jl:19-137 (algorithm :direct or :zipup); the
 # MPO as its (w_l, d_out, d_in, w_r) site arrays
 function evolve!(ψ::GB300MPS, H::Vector{Array{ComplexF64,4}}; algorithm::Symbol=:direct, maxdim::Integer=0,
                  threshold::Real=0.0)
-    length(H) == ψ.L || throw(ArgumentError("the MPO must have one site per MPS site"))
+    check_mpo(ψ, H)
     ptrs = Ptr{ComplexF64}[pointer(W) for W in H]
     bonds = Int64[size(W, 4) for W in H[1:end-1]]
     GC.@preserve H begin
@@ -539,7 +552,7 @@ end
 # column-major (w_l, d_out, d_in, w_r) with w_0 = w_L = 1 (`MPO(arrays; order=(:l, :o, :i, :r))`).
 function dmrg!(ψ::GB300MPS, H::Vector{Array{ComplexF64,4}}, nsweeps::Integer=4; method::Symbol=:dmrg1,
                maxdim::Integer=128, krylovdim::Integer=3, maxiter::Integer=2, tol::Real=1e-12)
-    length(H) == ψ.L || throw(ArgumentError("the MPO must have one site per MPS site"))
+    check_mpo(ψ, H)
     ptrs = Ptr{ComplexF64}[pointer(W) for W in H]
     bonds = Int64[size(W, 4) for W in H[1:end-1]]
     energy = Ref{Float64}(0.0)

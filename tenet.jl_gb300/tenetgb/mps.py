@@ -513,6 +513,11 @@ def evolve_mpo_(psi, mpo, algorithm="direct", maxdim=None, threshold=None):
             W = W[None, :, :, None]
         if W.ndim != 4 or W.shape[1] != psi._d or W.shape[2] != psi._d:
             raise ValueError(f"MPO site {i + 1}: expected (w_l, {psi._d}, {psi._d}, w_r), got {W.shape}")
+        # the library reads w_{i-1}·d·d·w_i entries per site, w_0 = w_L = 1
+        w_left = 1 if i == 0 else arrs[-1].shape[3]
+        if W.shape[0] != w_left or (i == L - 1 and W.shape[3] != 1):
+            raise ValueError(f"MPO site {i + 1}: virtual dimensions {W.shape[0]}, {W.shape[3]} do not chain "
+                             f"(left neighbour {w_left}, open ends 1)")
         arrs.append(np.asfortranarray(W))
     wb = (C.c_int64 * max(1, L - 1))(*[a.shape[3] for a in arrs[:-1]])
     ptrs = (C.c_void_p * L)(*[a.ctypes.data for a in arrs])
