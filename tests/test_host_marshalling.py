@@ -88,3 +88,35 @@ def test_host_arrays_checked_before_the_library_reads_them():
         m.amplitude([np.ones(3)] * 4)
     with pytest.raises(ValueError):
         m.local_expectations(np.eye(4))
+
+
+class BondsOnly(Refuser):
+    """Answers the bond-dimension query of an L-site MPS; any other call is a failure."""
+
+    def __init__(self, L):
+        self.L = L
+
+    def tn_mps_bond_dims(self, h, out):
+        for i in range(self.L - 1):
+            out[i] = 2
+        return 0
+
+
+def test_mpo_sizes_must_chain_before_the_library_reads_them():
+    import pytest
+
+    from tenetgb.mps import evolve_mpo_
+
+    m = fake_mps(BondsOnly(3), L=3, d=2)
+
+    def site(wl, wr, d=2):
+        return np.zeros((wl, d, d, wr), np.complex128)
+
+    with pytest.raises(ValueError):  # middle site's left dimension differs from its neighbour's right one
+        evolve_mpo_(m, [site(1, 3), site(2, 3), site(3, 1)])
+    with pytest.raises(ValueError):  # open ends must be 1
+        evolve_mpo_(m, [site(1, 3), site(3, 3), site(3, 2)])
+    with pytest.raises(ValueError):  # physical dimension
+        evolve_mpo_(m, [site(1, 3), site(3, 3, d=3), site(3, 1)])
+    with pytest.raises(ValueError):  # one site per MPS site
+        evolve_mpo_(m, [site(1, 3), site(3, 1)])
